@@ -1,0 +1,127 @@
+/*
+ * scwatter_gb300 -- C ABI of the GB300 (sm_103a) build of scwatter's plane-wave field
+ * evaluation and per-layer coupled-wave solve.
+ *
+ * Every entry point returns an scw_status; SCW_OK is 0.  scw_last_error() gives a
+ * message for the calling thread's last failure.  No entry point exits the process.
+ * Plain pointers and sizes only.  Complex numbers are (re, im) pairs of float or
+ * double, interleaved.
+ *
+ * Wave records ("planewave") are 12 values: E0.x re, im, E0.y re, im, E0.z re, im,
+ * k.x re, im, k.y re, im, k.z re, im -- the record of the .cw file format
+ * (CoupledWaveStructure.h:7-55) and of UnpackedWave<float> (cpuEvaluator.h:6-10).
+ *
+ * Field outputs are N x N arrays of 3 complex64 values per point, row-major with the
+ * second axis as the row (E_xy[iy*N+ix], E_xz[iz*N+ix], E_yz[iz*N+iy]), exactly the
+ * layout written by gpu_cw_evaluate (gpuEvaluator.cu:76-88).
+ */
+#ifndef SCWATTER_GB300_H
+#define SCWATTER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SCW_API __attribute__((visibility("default")))
+#else
+#define SCW_API
+#endif
+
+typedef enum scw_status {
+    SCW_OK = 0,
+    SCW_ERR_ARG = 1,        /* bad argument (null pointer, size out of range, wrong device) */
+    SCW_ERR_IO = 2,         /* file cannot be opened / read / written */
+    SCW_ERR_FORMAT = 3,     /* truncated or inconsistent .cw data */
+    SCW_ERR_CUDA = 4,       /* a CUDA runtime call failed */
+    SCW_ERR_NOMEM = 5,      /* host or device allocation failed */
+    SCW_ERR_STATE = 6,      /* object not initialised / wrong object kind */
+    SCW_ERR_NUMERIC = 7,    /* singular system, non-finite values, eigen-solver did not converge */
+    SCW_ERR_TIMEOUT = 8,    /* a bounded device-side wait gave up */
+    SCW_ERR_UNSUPPORTED = 9 /* the requested shape is outside what the kernel supports */
+} scw_status;
+
+typedef struct scw_ctx_s* scw_ctx;       /* one CUDA device + one stream + cached scratch */
+typedef struct scw_cw_s* scw_cw;         /* host CoupledWaveStructure<double> */
+typedef struct scw_waves_s* scw_waves;   /* device-resident unpacked wave set */
+
+SCW_API const char* scw_last_error(void);
+SCW_API const char* scw_version(void);
+
+/* ---------------------------------------------------------------------------------- */
+/* Context                                                                             */
+/* ---------------------------------------------------------------------------------- */
+/* stream: a cudaStream_t to run on, or NULL to create a private non-blocking stream. */
+SCW_API scw_status scw_ctx_create(int device, void* stream, scw_ctx* out);
+SCW_API scw_status scw_ctx_destroy(scw_ctx ctx);
+SCW_API scw_status scw_ctx_synchronize(scw_ctx ctx);
+SCW_API scw_status scw_ctx_stream(scw_ctx ctx, void** stream);
+/* Number of kernels this context has launched since creation (evidence of GPU work). */
+SCW_API scw_status scw_ctx_launch_count(scw_ctx ctx, int64_t* count);
+
+/* ---------------------------------------------------------------------------------- */
+/* .cw coefficient files -- replaces CoupledWaveStructure<T>::save / load /            */
+/* getPlaneIndex (CoupledWaveStructure.h:72-147).  Records are read as double; the     */
+/* header's precision field is read and ignored, as the reference does (:107-108).     */
+/* ---------------------------------------------------------------------------------- */
+SCW_API scw_status scw_cw_create(scw_cw* out);
+SCW_API scw_status scw_cw_destroy(scw_cw cw);
+SCW_API scw_status scw_cw_load(const char* path, scw_cw* out);              /* CoupledWaveStructure.h:103-134 */
+SCW_API scw_status scw_cw_save(scw_cw cw, const char* path);                /* CoupledWaveStructure.h:72-101 */
+SCW_API scw_status scw_cw_set_incident(scw_cw cw, int64_t n, const double* waves);
+SCW_API scw_status scw_cw_set_layer_count(scw_cw cw, int64_t n_layers);
+SCW_API scw_status scw_cw_set_layer(scw_cw cw, int64_t l, double z, int64_t n_pr, const double* pr,
+                                    int64_t n_pt, const double* pt);
+SCW_API scw_status scw_cw_counts(scw_cw cw, int64_t* n_incident, int64_t* n_layers);
+SCW_API scw_status scw_cw_layer_counts(scw_cw cw, int64_t l, double* z, int64_t* n_pr, int64_t* n_pt);
+SCW_API scw_status scw_cw_get_incident(scw_cw cw, double* waves);
+SCW_API scw_status scw_cw_get_layer(scw_cw cw, int64_t l, double* pr, double* pt);
+SCW_API scw_status scw_cw_get_plane_index(scw_cw cw, double z, int64_t* index); /* CoupledWaveStructure.h:141-147 */
+
+/* ---------------------------------------------------------------------------------- */
+/* Unpacking -- replaces cw_allocate / cw_unpack (cpuEvaluator.cpp:34-102).            */
+/* waves_begin / waves_end have layers+1 entries; W has total_waves*12 floats.         */
+/* ---------------------------------------------------------------------------------- */
+SCW_API scw_status scw_cw_allocate(scw_cw cw, int* layers, int64_t* total_waves);
+SCW_API scw_status scw_cw_unpack(scw_cw cw, float* W, int* waves_begin, int* waves_end, float* z_layers);
+
+/* ---------------------------------------------------------------------------------- */
+/* GPU field evaluator -- replaces gpu_initialize / gpu_cw_evaluate                    */
+/* (gpuEvaluator.h:8-18, gpuEvaluator.cu:15-26, 131-165).                              */
+/* ---------------------------------------------------------------------------------- */
+/* gpu_initialize (gpuEvaluator.cu:15-26): uploads the unpacked float wave table, exactly
+ * as the reference globals hold it (waves wound to the origin). */
+SCW_API scw_status scw_gpu_initialize(scw_ctx ctx, int layers, const float* z_layers,
+                                      const int* waves_begin, const int* waves_end,
+                                      const float* W, int64_t n_waves, scw_waves* out);
+/* Same set from the double-precision .cw structure: each wave of layer l is re-referenced
+ * ("un-wound") to z_l in FP64 so no float exponent over- or under-flows. */
+SCW_API scw_status scw_gpu_initialize_cw(scw_ctx ctx, scw_cw cw, scw_waves* out);
+SCW_API scw_status scw_waves_destroy(scw_waves waves);
+/* Region rule: 0 = gpuEvaluator rule z >= z_l - 0.001 (default, gpuEvaluator.cu:34),
+ *              1 = cpuEvaluator rule z >= z_l (cpuEvaluator.cpp:303). */
+SCW_API scw_status scw_waves_set_region_rule(scw_waves waves, int rule);
+SCW_API scw_status scw_waves_info(scw_waves waves, int* layers, int64_t* n_waves);
+
+/* gpu_cw_evaluate (gpuEvaluator.cu:131-165): three N x N planes into HOST arrays
+ * (each N*N*6 floats); blocks until the results are in host memory. */
+SCW_API scw_status scw_gpu_cw_evaluate(scw_waves waves, float* E_xy, float* E_xz, float* E_yz,
+                                       float x_start, float y_start, float z_start,
+                                       float x, float y, float z, float d, int N, int device);
+/* One plane into DEVICE memory, asynchronous on the context stream.
+ * axis 0: xy plane at z = c (a = x, b = y); 1: yz plane at x = c (a = y, b = z);
+ * 2: xz plane at y = c (a = x, b = z).  Output [N][N][3] complex64, row = b. */
+SCW_API scw_status scw_eval_plane_device(scw_waves waves, int axis, float a_start, float b_start,
+                                         float c, float d, int N, float* dE);
+/* Nz x Ny x Nx grid into DEVICE memory [Nz][Ny][Nx][3] complex64, asynchronous;
+ * point (ix, iy, iz) = (x_start + dx*ix, y_start + dy*iy, z_start + dz*iz), each product
+ * and sum rounded to float separately. */
+SCW_API scw_status scw_eval_volume_device(scw_waves waves, float x_start, float y_start, float z_start,
+                                          float dx, float dy, float dz, int Nx, int Ny, int Nz, float* dE);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SCWATTER_GB300_H */

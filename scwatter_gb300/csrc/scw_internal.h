@@ -1,0 +1,83 @@
+// Internal definitions shared by the scwatter_gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/scwatter.h"
+
+namespace scw {
+
+// Thread-local last-error message behind scw_last_error().
+void set_error(const std::string& msg);
+scw_status fail(scw_status st, const std::string& msg);
+
+#define SCW_CUDA_TRY(expr)                                                                \
+    do {                                                                                  \
+        cudaError_t e_ = (expr);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return ::scw::fail(SCW_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Device buffer owned by a context; grows on demand, never shrinks.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    scw_status reserve(size_t n);
+    void release();
+};
+
+// Pinned host staging buffer for small per-call descriptor uploads.
+struct PinnedBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    scw_status reserve(size_t n);
+    void release();
+};
+
+}  // namespace scw
+
+struct scw_ctx_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sm_count = 0;
+    int64_t launches = 0;
+    scw::DevBuf scratch;        // split-K partial sums of the plain evaluator
+    scw::DevBuf desc;           // per-call work descriptors
+    scw::DevBuf planes_out;     // device staging of gpu_cw_evaluate's three planes
+    scw::PinnedBuf host_desc;   // pinned staging of the descriptors
+    cudaEvent_t desc_done = nullptr;  // the last descriptor upload has been consumed
+};
+
+struct scw_cw_s {
+    uint64_t sizeof_T = 8;
+    std::vector<double> Pi;                 // n * 12
+    struct Layer {
+        double z = 0.0;
+        std::vector<double> Pr, Pt;         // n * 12 each
+    };
+    std::vector<Layer> layers;
+};
+
+struct scw_waves_s {
+    scw_ctx ctx = nullptr;
+    int layers = 0;
+    int64_t n = 0;
+    int rule = 0;                           // 0: z >= z_l - 0.001, 1: z >= z_l
+    std::vector<float> z_layers;
+    std::vector<int64_t> begin, end;        // layers + 1 regions
+    // device SoA tables (n entries each)
+    double* kre = nullptr;                  // [3][n] Re k
+    double* kim = nullptr;                  // [3][n] Im k
+    double* zref = nullptr;                 // [n] reference plane of the amplitude
+    float2* amp = nullptr;                  // [3][n] E0 at the reference plane
+};
+
+namespace scw {
+// Implemented in eval_plain.cu
+scw_status waves_upload(scw_waves w, const std::vector<double>& kre, const std::vector<double>& kim,
+                        const std::vector<double>& zref, const std::vector<float2>& amp);
+}

@@ -200,13 +200,21 @@ def run_ours(args):
     from scwatter_gb300 import evaluator as ev
     from scwatter_gb300.cw import CoupledWaveStructure, HomogeneousLayer
 
-    cfg = CFG1
+    cfg = dict(CFG1)
     fs, (Pi, zs, Pr, Pt), d = build_workload(cfg)
     dx, dy, dz = d
+    if args.nz:     # small profiling case: the central nz z-planes of the grid
+        k0 = (cfg["Nz"] - args.nz) // 2
+        cfg["z0"] = float(grid_axis(cfg["z0"], dz, cfg["Nz"])[k0])
+        cfg["Nz"] = args.nz
+        cfg["name"] += f" (central {args.nz} z-planes)"
     S = CoupledWaveStructure()
     S.Pi = Pi
     S.Layers = [HomogeneousLayer(z=zs[l], Pr=Pr[l], Pt=Pt[l]) for l in range(len(zs))]
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the context launches on it and the CUDA events
+    # below are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = ev.Context(local, stream=stream.cuda_stream)
     wset = ev.WaveSet.from_cw(ctx, S)
     W, begin, end, zl = unpack_arrays(Pi, zs, Pr, Pt)
@@ -300,6 +308,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--nz", type=int, default=0, help="evaluate only this many z-planes (small profiling case)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -11,9 +11,10 @@
 //    region's waves.  Waves are staged through shared memory 256 at a time; while staging,
 //    each thread re-bases one wave to the tile centre r_c in FP64:
 //        theta_c = Re k . (r_c - r_ref)  reduced mod 2 pi,   A' = A exp(-Im k . (r_c - r_ref))
-//    so the per-(point, wave) work is FP32 over the small offset d = r - r_c only:
+//    so the per-(point, wave) work is FP32 over the small in-plane offset d = r - r_c only:
 //        theta = theta_c + Re k . d,  m = 2^(-Im k log2(e) . d),  E += A' m (cos theta, i sin theta)
-//    i.e. 3 MUFU ops (ex2, sin, cos) and ~19 FP32 ops per point x wave.
+//    i.e. 3 MUFU ops (ex2, sin, cos), 7 FP32 ops and 6 packed f32x2 FMAs per point x wave
+//    (2 MUFU and 4 FP32 ops when the batch's waves all have real k).
 //  * Tiles that see many waves are split over several CTAs (split-K over the wave list);
 //    their FP32 partial sums go to a scratch buffer and a second kernel adds them in a
 //    fixed order in FP64 (deterministic, run-to-run bitwise identical).
@@ -67,11 +68,16 @@ struct WaveSoA {
     long long n;
 };
 
+// One staged wave, re-based to the tile centre.  The plane's two in-plane axes are A (along
+// the tile columns) and B (along the rows); the out-of-plane offset is zero for every point.
+// Amplitudes are stored as duplicated pairs so the accumulation runs on packed f32x2 FMAs:
+// P_c += (Ar, Ar) * (ur, ui),  Q_c += (Ai, Ai) * (ur, ui);  E_c = (P.x - Q.y, P.y + Q.x).
 struct __align__(16) StagedWave {
-    float4 a;   // theta_c (rad, in [-pi, pi]), Re kx, Re ky, Re kz
-    float4 b;   // -Im kx log2e, -Im ky log2e, -Im kz log2e, 0
-    float4 c;   // A'x re, im, A'y re, im
-    float4 d;   // A'z re, im, 0, 0
+    float4 a;   // theta_c (rad, in [-pi, pi]), Re k_A, Re k_B, -Im k_A log2e
+    float4 x;   // A'x re, A'x re, A'x im, A'x im
+    float4 y;   // A'y ...
+    float4 z;   // A'z ...
+    float4 b;   // -Im k_B log2e, 0, 0, 0
 };
 
 __device__ __forceinline__ float ex2_approx(float x) {
@@ -79,6 +85,19 @@ __device__ __forceinline__ float ex2_approx(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+
+// d = a * b + c on packed float pairs (sm_100+ f32x2 FMA)
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)),
+          "l"(*reinterpret_cast<unsigned long long*>(&c)));
+    return *reinterpret_cast<float2*>(&d);
+}
+
+__device__ __forceinline__ float2 lo_pair(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi_pair(float4 v) { return make_float2(v.z, v.w); }
 
 // point coordinates in the reference's float arithmetic: start + d * index, each operation
 // rounded separately (no fused multiply-add).
@@ -92,57 +111,50 @@ __device__ __forceinline__ void to_xyz(int mode, float a, float b, float c, floa
     else { x = a; y = c; z = b; }
 }
 
+struct PointAcc {
+    float2 p[3], q[3];
+};
+
 template <bool kComplexK>
-__device__ __forceinline__ void accumulate_batch(const StagedWave* __restrict__ s, int nw, float dx0, float dy0,
-                                                 float dz0, float dx1, float dy1, float dz1, float (&e0)[6],
-                                                 float (&e1)[6]) {
+__device__ __forceinline__ void accumulate_point(const StagedWave& w, float kiB, float dA, float dB, PointAcc& acc) {
+    const float th = fmaf(w.a.z, dB, fmaf(w.a.y, dA, w.a.x));
+    float sn, cs;
+    __sincosf(th, &sn, &cs);
+    float2 u = make_float2(cs, sn);
+    if (kComplexK) {
+        const float m = ex2_approx(fmaf(kiB, dB, w.a.w * dA));
+        u.x *= m;
+        u.y *= m;
+    }
+    acc.p[0] = ffma2(lo_pair(w.x), u, acc.p[0]);
+    acc.q[0] = ffma2(hi_pair(w.x), u, acc.q[0]);
+    acc.p[1] = ffma2(lo_pair(w.y), u, acc.p[1]);
+    acc.q[1] = ffma2(hi_pair(w.y), u, acc.q[1]);
+    acc.p[2] = ffma2(lo_pair(w.z), u, acc.p[2]);
+    acc.q[2] = ffma2(hi_pair(w.z), u, acc.q[2]);
+}
+
+template <bool kComplexK>
+__device__ __forceinline__ void accumulate_batch(const StagedWave* __restrict__ s, int nw, float dA, float dB0,
+                                                 float dB1, PointAcc& a0, PointAcc& a1) {
 #pragma unroll 2
     for (int k = 0; k < nw; k++) {
-        const float4 wa = s[k].a;
-        const float4 wb = s[k].b;
-        const float4 wc = s[k].c;
-        const float4 wd = s[k].d;
-        {
-            float th = fmaf(wa.w, dz0, fmaf(wa.z, dy0, fmaf(wa.y, dx0, wa.x)));
-            float sn, cs;
-            __sincosf(th, &sn, &cs);
-            float ur = cs, ui = sn;
-            if (kComplexK) {
-                float m = ex2_approx(fmaf(wb.z, dz0, fmaf(wb.y, dy0, wb.x * dx0)));
-                ur *= m;
-                ui *= m;
-            }
-            e0[0] = fmaf(wc.x, ur, fmaf(-wc.y, ui, e0[0]));
-            e0[1] = fmaf(wc.x, ui, fmaf(wc.y, ur, e0[1]));
-            e0[2] = fmaf(wc.z, ur, fmaf(-wc.w, ui, e0[2]));
-            e0[3] = fmaf(wc.z, ui, fmaf(wc.w, ur, e0[3]));
-            e0[4] = fmaf(wd.x, ur, fmaf(-wd.y, ui, e0[4]));
-            e0[5] = fmaf(wd.x, ui, fmaf(wd.y, ur, e0[5]));
-        }
-        {
-            float th = fmaf(wa.w, dz1, fmaf(wa.z, dy1, fmaf(wa.y, dx1, wa.x)));
-            float sn, cs;
-            __sincosf(th, &sn, &cs);
-            float ur = cs, ui = sn;
-            if (kComplexK) {
-                float m = ex2_approx(fmaf(wb.z, dz1, fmaf(wb.y, dy1, wb.x * dx1)));
-                ur *= m;
-                ui *= m;
-            }
-            e1[0] = fmaf(wc.x, ur, fmaf(-wc.y, ui, e1[0]));
-            e1[1] = fmaf(wc.x, ui, fmaf(wc.y, ur, e1[1]));
-            e1[2] = fmaf(wc.z, ur, fmaf(-wc.w, ui, e1[2]));
-            e1[3] = fmaf(wc.z, ui, fmaf(wc.w, ur, e1[3]));
-            e1[4] = fmaf(wd.x, ur, fmaf(-wd.y, ui, e1[4]));
-            e1[5] = fmaf(wd.x, ui, fmaf(wd.y, ur, e1[5]));
-        }
+        StagedWave w;
+        w.a = s[k].a;
+        w.x = s[k].x;
+        w.y = s[k].y;
+        w.z = s[k].z;
+        const float kiB = kComplexK ? s[k].b.x : 0.f;
+        accumulate_point<kComplexK>(w, kiB, dA, dB0, a0);
+        accumulate_point<kComplexK>(w, kiB, dA, dB1, a1);
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, 4)
 plain_eval_kernel(const PlaneGeom* __restrict__ planes, const WorkItem* __restrict__ items, WaveSoA W,
                   float* __restrict__ partials) {
     __shared__ StagedWave sw[kBatch];
+    __shared__ double tot[12][kThreads];   // per-thread FP64 running sums (point 0: 0-5, point 1: 6-11)
     const WorkItem it = items[blockIdx.x];
     const PlaneGeom g = planes[it.plane];
     const int t = threadIdx.x;
@@ -152,22 +164,23 @@ plain_eval_kernel(const PlaneGeom* __restrict__ planes, const WorkItem* __restri
     const int j0 = it.j0 + lj;
     const int j1 = j0 + 16;
 
-    // tile centre (float grid coordinates of tile point (8, 16)) and per-point offsets
+    // tile centre: float grid coordinates of tile point (8, 16); per-point in-plane offsets
+    const float ac = grid_coord(g.a0, g.da, it.i0 + 8), bc = grid_coord(g.b0, g.db, it.j0 + 16);
+    const float dA = (float)((double)grid_coord(g.a0, g.da, i) - (double)ac);
+    const float dB0 = (float)((double)grid_coord(g.b0, g.db, j0) - (double)bc);
+    const float dB1 = (float)((double)grid_coord(g.b0, g.db, j1) - (double)bc);
     float xc, yc, zc;
-    to_xyz(g.mode, grid_coord(g.a0, g.da, it.i0 + 8), grid_coord(g.b0, g.db, it.j0 + 16), g.c, xc, yc, zc);
-    float x0, y0, z0, x1, y1, z1;
-    to_xyz(g.mode, grid_coord(g.a0, g.da, i), grid_coord(g.b0, g.db, j0), g.c, x0, y0, z0);
-    to_xyz(g.mode, grid_coord(g.a0, g.da, i), grid_coord(g.b0, g.db, j1), g.c, x1, y1, z1);
-    const float dx0 = (float)((double)x0 - (double)xc), dy0 = (float)((double)y0 - (double)yc),
-                dz0 = (float)((double)z0 - (double)zc);
-    const float dx1 = (float)((double)x1 - (double)xc), dy1 = (float)((double)y1 - (double)yc),
-                dz1 = (float)((double)z1 - (double)zc);
+    to_xyz(g.mode, ac, bc, g.c, xc, yc, zc);
+    // which k components lie along the plane's A and B axes
+    const int cA = (g.mode == 1) ? 1 : 0;
+    const int cB = (g.mode == 0) ? 1 : 2;
 
-    double acc0[6] = {0, 0, 0, 0, 0, 0}, acc1[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 12; c++) tot[c][t] = 0.0;
     const double two_pi_hi = 6.283185307179586232;
     const double two_pi_lo = 2.4492935982947064e-16;
     const double inv_two_pi = 0.15915494309189533577;
-    const double log2e = 1.4426950408889634074;
+    const float log2e = 1.44269504088896341f;
 
     for (long long wb = it.w0; wb < it.w1; wb += kBatch) {
         const int nw = (int)min((long long)kBatch, it.w1 - wb);
@@ -181,27 +194,36 @@ plain_eval_kernel(const PlaneGeom* __restrict__ planes, const WorkItem* __restri
             double th = fma(krz, rz, fma(kry, ry, krx * rx));
             const double q = rint(th * inv_two_pi);
             th = fma(-q, two_pi_lo, fma(-q, two_pi_hi, th));
-            const double ac = -fma(kiz, rz, fma(kiy, ry, kix * rx));
-            const double m = exp(ac);
+            const double ach = -fma(kiz, rz, fma(kiy, ry, kix * rx));
+            const float m = exp2f((float)(ach * 1.4426950408889634074));
             const float2 ax = W.amp[w], ay = W.amp[n + w], az = W.amp[2 * n + w];
+            const double krA = cA == 0 ? krx : kry, krB = cB == 1 ? kry : krz;
+            const double kiA = cA == 0 ? kix : kiy, kiB = cB == 1 ? kiy : kiz;
             StagedWave s;
-            s.a = make_float4((float)th, (float)krx, (float)kry, (float)krz);
-            s.b = make_float4((float)(-kix * log2e), (float)(-kiy * log2e), (float)(-kiz * log2e), 0.f);
-            s.c = make_float4((float)(ax.x * m), (float)(ax.y * m), (float)(ay.x * m), (float)(ay.y * m));
-            s.d = make_float4((float)(az.x * m), (float)(az.y * m), 0.f, 0.f);
+            s.a = make_float4((float)th, (float)krA, (float)krB, -(float)kiA * log2e);
+            s.x = make_float4(ax.x * m, ax.x * m, ax.y * m, ax.y * m);
+            s.y = make_float4(ay.x * m, ay.x * m, ay.y * m, ay.y * m);
+            s.z = make_float4(az.x * m, az.x * m, az.y * m, az.y * m);
+            s.b = make_float4(-(float)kiB * log2e, 0.f, 0.f, 0.f);
             sw[t] = s;
-            cplx = (kix != 0.0) | (kiy != 0.0) | (kiz != 0.0);
+            cplx = (kiA != 0.0) | (kiB != 0.0);
         }
         cplx = __syncthreads_or(cplx);
-        float e0[6] = {0, 0, 0, 0, 0, 0}, e1[6] = {0, 0, 0, 0, 0, 0};
-        if (cplx)
-            accumulate_batch<true>(sw, nw, dx0, dy0, dz0, dx1, dy1, dz1, e0, e1);
-        else
-            accumulate_batch<false>(sw, nw, dx0, dy0, dz0, dx1, dy1, dz1, e0, e1);
+        PointAcc a0, a1;
 #pragma unroll
-        for (int c = 0; c < 6; c++) {
-            acc0[c] += (double)e0[c];
-            acc1[c] += (double)e1[c];
+        for (int c = 0; c < 3; c++) {
+            a0.p[c] = a0.q[c] = a1.p[c] = a1.q[c] = make_float2(0.f, 0.f);
+        }
+        if (cplx)
+            accumulate_batch<true>(sw, nw, dA, dB0, dB1, a0, a1);
+        else
+            accumulate_batch<false>(sw, nw, dA, dB0, dB1, a0, a1);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            tot[2 * c][t] += (double)(a0.p[c].x - a0.q[c].y);
+            tot[2 * c + 1][t] += (double)(a0.p[c].y + a0.q[c].x);
+            tot[6 + 2 * c][t] += (double)(a1.p[c].x - a1.q[c].y);
+            tot[7 + 2 * c][t] += (double)(a1.p[c].y + a1.q[c].x);
         }
         __syncthreads();
     }
@@ -214,12 +236,12 @@ plain_eval_kernel(const PlaneGeom* __restrict__ planes, const WorkItem* __restri
             if (j0 < g.Nj && in0) {
                 float* o = g.out + 6 * ((long long)j0 * g.Ni + i);
 #pragma unroll
-                for (int c = 0; c < 6; c++) o[c] = (float)acc0[c];
+                for (int c = 0; c < 6; c++) o[c] = (float)tot[c][t];
             }
             if (j1 < g.Nj && in1) {
                 float* o = g.out + 6 * ((long long)j1 * g.Ni + i);
 #pragma unroll
-                for (int c = 0; c < 6; c++) o[c] = (float)acc1[c];
+                for (int c = 0; c < 6; c++) o[c] = (float)tot[6 + c][t];
             }
         }
     } else {
@@ -228,8 +250,8 @@ plain_eval_kernel(const PlaneGeom* __restrict__ planes, const WorkItem* __restri
         float* p1 = p + 6 * ((lj + 16) * kTI + li);
 #pragma unroll
         for (int c = 0; c < 6; c++) {
-            p0[c] = in0 ? (float)acc0[c] : 0.f;
-            p1[c] = in1 ? (float)acc1[c] : 0.f;
+            p0[c] = in0 ? (float)tot[c][t] : 0.f;
+            p1[c] = in1 ? (float)tot[6 + c][t] : 0.f;
         }
     }
 }
@@ -299,7 +321,7 @@ static void plan_planes(const scw_waves_s* w, const std::vector<PlaneGeom>& plan
             }
         }
     }
-    const double target_items = 6.0 * sm_count;
+    const double target_items = 48.0 * sm_count;
     long long chunk = (long long)std::ceil(work / std::max(1.0, target_items));
     chunk = std::max<long long>(chunk, 4 * kBatch);
     chunk = ((chunk + kBatch - 1) / kBatch) * kBatch;
@@ -369,6 +391,9 @@ static scw_status launch_planes(scw_waves w, std::vector<PlaneGeom>& planes) {
     Plan P;
     plan_planes(w, planes, ctx->sm_count, P);
     if (P.items.empty()) return SCW_OK;
+    // longest items first, so the short exterior-region items fill the tail of the grid
+    std::stable_sort(P.items.begin(), P.items.end(),
+                     [](const WorkItem& a, const WorkItem& b) { return (a.w1 - a.w0) > (b.w1 - b.w0); });
 
     const size_t planes_bytes = planes.size() * sizeof(PlaneGeom);
     const size_t items_off = (planes_bytes + 255) / 256 * 256;

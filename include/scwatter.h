@@ -46,6 +46,12 @@ typedef enum scw_status {
 typedef struct scw_ctx_s* scw_ctx;       /* one CUDA device + one stream + cached scratch */
 typedef struct scw_cw_s* scw_cw;         /* host CoupledWaveStructure<double> */
 typedef struct scw_waves_s* scw_waves;   /* device-resident unpacked wave set */
+typedef struct scw_sep_s* scw_sep;       /* device-resident separable (factored) coefficient set */
+
+/* Output-GEMM methods of the separable evaluator */
+#define SCW_SEP_FP32 1      /* FP32 SIMT */
+#define SCW_SEP_TF32X3 2    /* tcgen05 kind::tf32, 3 products of hi/lo splits, FP32 accumulation */
+#define SCW_SEP_BF16X3 3    /* tcgen05 kind::f16 (bf16), 3 products of hi/lo splits, FP32 accumulation */
 
 SCW_API const char* scw_last_error(void);
 SCW_API const char* scw_version(void);
@@ -120,6 +126,40 @@ SCW_API scw_status scw_eval_plane_device(scw_waves waves, int axis, float a_star
  * and sum rounded to float separately. */
 SCW_API scw_status scw_eval_volume_device(scw_waves waves, float x_start, float y_start, float z_start,
                                           float dx, float dy, float dz, int Nx, int Ny, int Nz, float* dE);
+
+/* ---------------------------------------------------------------------------------- */
+/* Separable ("GEMM form") evaluator -- no reference counterpart; evaluates the same    */
+/* field as gpu_cw_evaluate when the waves come from the volume solver (sCWatter.cpp:  */
+/* 890-956): inside slice l every wave is (harmonic p = (a, b), mode j) with           */
+/* kx = kx_a, ky = ky_b, kz = kz_j, so E = sum_a e^{i kx_a x} sum_b e^{i ky_b y} C(a,b;z). */
+/* Complex arrays are (re, im) doubles; Q blocks are [3][MF][J] with row p = a*M1 + b.  */
+/* ---------------------------------------------------------------------------------- */
+SCW_API scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half,
+                                  const double* kx, const double* ky, const double* z_boundaries, scw_sep* out);
+SCW_API scw_status scw_sep_destroy(scw_sep s);
+/* incident (referenced at z = 0), reflected (at z_0), transmitted (at z_Z): [3][MF] complex;
+ * kz_*: [MF] complex. */
+SCW_API scw_status scw_sep_set_exterior(scw_sep s, const double* inc, const double* kz_inc, const double* refl,
+                                        const double* kz_refl, const double* trans, const double* kz_trans);
+/* slice l: downward modes referenced at z_l, upward modes at z_{l+1}; kz: [J] complex, Q: [3][MF][J] */
+SCW_API scw_status scw_sep_set_slice(scw_sep s, int l, const double* kz_dn, const double* Q_dn,
+                                     const double* kz_up, const double* Q_up);
+/* same with Q already in complex64 (host or device memory) */
+SCW_API scw_status scw_sep_set_slice_device(scw_sep s, int l, const double* kz_dn, const void* Q_dn_c64,
+                                            const double* kz_up, const void* Q_up_c64);
+/* factors a .cw written by the volume solver; SCW_ERR_UNSUPPORTED if its waves do not have
+ * the separable structure (use the plain evaluator then). */
+SCW_API scw_status scw_sep_from_cw(scw_ctx ctx, scw_cw cw, scw_sep* out);
+SCW_API scw_status scw_sep_info(scw_sep s, int* M0, int* M1, int* n_slices, int* modes_per_half);
+SCW_API scw_status scw_sep_set_region_rule(scw_sep s, int rule);
+SCW_API scw_status scw_sep_eval_volume_device(scw_sep s, float x_start, float y_start, float z_start,
+                                              float dx, float dy, float dz, int Nx, int Ny, int Nz,
+                                              float* dE, int method);
+SCW_API scw_status scw_sep_eval_plane_device(scw_sep s, int axis, float a_start, float b_start, float c,
+                                             float d, int N, float* dE, int method);
+SCW_API scw_status scw_sep_gpu_cw_evaluate(scw_sep s, float* E_xy, float* E_xz, float* E_yz,
+                                           float x_start, float y_start, float z_start,
+                                           float x, float y, float z, float d, int N, int device, int method);
 
 #ifdef __cplusplus
 }

@@ -264,7 +264,8 @@ int orc_eval_points_f64(const double* W, const int64_t* begin, const int64_t* en
 /*   E_c(x,y,z) = sum_{a,b} e^{i kx_a x} e^{i ky_b y} sum_j Q_c(a*Mb+b, j)          */
 /*                 e^{i kz_j (z - zref_j)}                                          */
 /* kx, ky real; kz complex.  Used to check the GEMM-form evaluator on the same      */
-/* coefficients without materialising a 4 MF^2 wave list.                           */
+/* coefficients without materialising a 4 MF^2 wave list.  Points sharing a z       */
+/* (consecutive in the list) reuse the contracted coefficients C_c(m; z).           */
 /* ------------------------------------------------------------------------------ */
 typedef struct {
     int64_t Ma, Mb, J;
@@ -281,13 +282,25 @@ typedef struct {
 static void* sep_worker(void* arg) {
     sep_job* j = (sep_job*)arg;
     int64_t MF = j->Ma * j->Mb;
-    double complex* ph = (double complex*)malloc(sizeof(double complex) * (size_t)j->J);
+    double complex* C = (double complex*)malloc(sizeof(double complex) * (size_t)(3 * MF));
+    double complex* ph = (double complex*)malloc(sizeof(double complex) * (size_t)(j->J > 0 ? j->J : 1));
+    double zlast = NAN;
     for (int64_t p = j->p0; p < j->p1; p++) {
         double x = j->pts[3 * p], y = j->pts[3 * p + 1], z = j->pts[3 * p + 2];
-        for (int64_t jj = 0; jj < j->J; jj++) {
-            double complex kz = CMPLX(j->kz[2 * jj], j->kz[2 * jj + 1]);
-            double complex arg2 = kz * (z - j->zref[jj]);
-            ph[jj] = cexp(CMPLX(-cimag(arg2), creal(arg2)));
+        if (!(z == zlast)) {   /* C_c(m; z) = sum_j Q_c(m, j) exp(i kz_j (z - zref_j)), cached per z */
+            for (int64_t jj = 0; jj < j->J; jj++) {
+                double complex kz = CMPLX(j->kz[2 * jj], j->kz[2 * jj + 1]);
+                double complex arg2 = kz * (z - j->zref[jj]);
+                ph[jj] = cexp(CMPLX(-cimag(arg2), creal(arg2)));
+            }
+            for (int c = 0; c < 3; c++)
+                for (int64_t m = 0; m < MF; m++) {
+                    const double* q = j->Q + 2 * ((c * MF + m) * j->J);
+                    double complex s = 0;
+                    for (int64_t jj = 0; jj < j->J; jj++) s += CMPLX(q[2 * jj], q[2 * jj + 1]) * ph[jj];
+                    C[c * MF + m] = s;
+                }
+            zlast = z;
         }
         double complex E[3] = {0, 0, 0};
         for (int64_t a = 0; a < j->Ma; a++) {
@@ -295,12 +308,7 @@ static void* sep_worker(void* arg) {
                 double ang = j->kx[a] * x + j->ky[b] * y;
                 double complex exy = CMPLX(cos(ang), sin(ang));
                 int64_t m = a * j->Mb + b;
-                for (int c = 0; c < 3; c++) {
-                    const double* q = j->Q + 2 * ((c * MF + m) * j->J);
-                    double complex s = 0;
-                    for (int64_t jj = 0; jj < j->J; jj++) s += CMPLX(q[2 * jj], q[2 * jj + 1]) * ph[jj];
-                    E[c] += s * exy;
-                }
+                for (int c = 0; c < 3; c++) E[c] += C[c * MF + m] * exy;
             }
         }
         for (int c = 0; c < 3; c++) {
@@ -309,6 +317,7 @@ static void* sep_worker(void* arg) {
         }
     }
     free(ph);
+    free(C);
     return NULL;
 }
 

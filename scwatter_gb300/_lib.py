@@ -60,6 +60,17 @@ _SIGS = {
     "scw_gpu_cw_evaluate": [P, P, P, P, F32, F32, F32, F32, F32, F32, F32, I32, I32],
     "scw_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P],
     "scw_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P],
+    "scw_sep_create": [P, I32, I32, I32, I32, P, P, P, PP],
+    "scw_sep_destroy": [P],
+    "scw_sep_set_exterior": [P, P, P, P, P, P, P],
+    "scw_sep_set_slice": [P, I32, P, P, P, P],
+    "scw_sep_set_slice_device": [P, I32, P, P, P, P],
+    "scw_sep_from_cw": [P, P, PP],
+    "scw_sep_info": [P, ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32)],
+    "scw_sep_set_region_rule": [P, I32],
+    "scw_sep_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
+    "scw_sep_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P, I32],
+    "scw_sep_gpu_cw_evaluate": [P, P, P, P, F32, F32, F32, F32, F32, F32, F32, I32, I32, I32],
 }
 
 

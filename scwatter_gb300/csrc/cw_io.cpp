@@ -128,6 +128,7 @@ scw_status scw_ctx_destroy(scw_ctx c) {
     c->scratch.release();
     c->desc.release();
     c->planes_out.release();
+    c->sep_scratch.release();
     c->host_desc.release();
     if (c->desc_done) cudaEventDestroy(c->desc_done);
     if (c->own_stream) cudaStreamDestroy(c->stream);

@@ -1,0 +1,629 @@
+// Separable ("GEMM form") field evaluation.
+//
+// Inside slice l the solver's waves share kx, ky per harmonic p = (a, b) of an M0 x M1
+// grid and kz per eigenmode j (sCWatter.cpp:904-952), so
+//     E_c(x, y, z) = sum_a e^{i kx_a x} sum_b e^{i ky_b y} C_c(a, b; z),
+//     C_c(p; z)   = sum_j Qdn_c(p, j) e^{i kzdn_j (z - z_l)} + sum_j Qup_c(p, j) e^{i kzup_j (z - z_{l+1})}.
+// Stage 1 (HBM-bound): C for every evaluated z-plane (sep_phase_kernel + sep_contract_kernel;
+//   sep_exterior_kernel for the incident/reflected and transmitted regions).
+// Stage 2: T_c(row, a) = sum_b e^{i ky_b y_row} C_c(a, b; z_row) (sep_rows_kernel), then the
+//   output GEMM E_c(row, x) = sum_a T_c(row, a) e^{i kx_a x}: FP32 SIMT (sep_synth_kernel) or
+//   tcgen05 3xTF32 / split-BF16 (eval_sep_tc.cu).
+// Phases are reduced in FP64 before rounding to FP32.  The yz plane contracts a first and
+// keeps b (ky) as the output axis.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <new>
+
+#include "scw_internal.h"
+#include "scw_sep.h"
+
+namespace scw {
+
+constexpr int kPhaseChunk = 256;
+
+// exp(i kz (z - zref)) with the angle reduced in FP64
+__device__ __forceinline__ float2 phase_fp64(double kr, double ki, double dz) {
+    const double th = kr * dz;
+    const double q = rint(th * 0.15915494309189533577);
+    const double t = fma(-q, 2.4492935982947064e-16, fma(-q, 6.283185307179586232, th));
+    const float m = expf((float)(-ki * dz));
+    float s, c;
+    sincosf((float)t, &s, &c);
+    return make_float2(m * c, m * s);
+}
+
+__global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float* __restrict__ zlist,
+                                 const double2* __restrict__ kz, const double* __restrict__ zb, int J,
+                                 float2* __restrict__ Phi) {
+    const PGroup g = groups[blockIdx.y];
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= 2 * J) return;
+    const int l = g.region - 1;
+    const int half = j / J;
+    const double2 k = kz[((long long)l * 2 + half) * J + (j - half * J)];
+    const double zref = half == 0 ? zb[l] : zb[l + 1];
+    float2* out = Phi + ((long long)blockIdx.y * 2 * J + j) * kMaxGroup;
+#pragma unroll
+    for (int kk = 0; kk < kMaxGroup; kk++) {
+        if (kk < g.nk) {
+            const double dz = (double)zlist[g.zi[kk]] - zref;
+            out[kk] = phase_fp64(k.x, k.y, dz);
+        } else {
+            out[kk] = make_float2(0.f, 0.f);
+        }
+    }
+}
+
+// C[zi][c][p] = sum over the slice's 2J modes of Q[l][half][c][p][j] * Phi[g][half*J + j][kk]
+template <int NK>
+__global__ void __launch_bounds__(128)
+sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict__ Phi,
+                    const float2* __restrict__ Q, int MF, int J, float2* __restrict__ C) {
+    __shared__ float2 ph[kPhaseChunk][NK];
+    const PGroup g = groups[blockIdx.y];
+    const int l = g.region - 1;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = row < 3 * MF;
+    const int c = active ? row / MF : 0;
+    const int p = active ? row % MF : 0;
+    double tot[NK][2];
+#pragma unroll
+    for (int kk = 0; kk < NK; kk++) tot[kk][0] = tot[kk][1] = 0.0;
+    const float2* Pg = Phi + (long long)blockIdx.y * 2 * J * kMaxGroup;
+    for (int half = 0; half < 2; half++) {
+        const float2* qrow = Q + ((((long long)l * 2 + half) * 3 + c) * MF + p) * (long long)J;
+        for (int j0 = 0; j0 < J; j0 += kPhaseChunk) {
+            const int nj = min(kPhaseChunk, J - j0);
+            __syncthreads();
+            for (int e = threadIdx.x; e < nj * NK; e += blockDim.x) {
+                const int jj = e / NK, kk = e % NK;
+                ph[jj][kk] = Pg[((long long)half * J + j0 + jj) * kMaxGroup + kk];
+            }
+            __syncthreads();
+            if (active) {
+                float acc[NK][2];
+#pragma unroll
+                for (int kk = 0; kk < NK; kk++) acc[kk][0] = acc[kk][1] = 0.f;
+                int jj = 0;
+                for (; jj + 1 < nj; jj += 2) {
+                    const float4 q2 = __ldg(reinterpret_cast<const float4*>(qrow + j0 + jj));
+#pragma unroll
+                    for (int kk = 0; kk < NK; kk++) {
+                        const float2 f0 = ph[jj][kk], f1 = ph[jj + 1][kk];
+                        acc[kk][0] = fmaf(q2.x, f0.x, fmaf(-q2.y, f0.y, acc[kk][0]));
+                        acc[kk][1] = fmaf(q2.x, f0.y, fmaf(q2.y, f0.x, acc[kk][1]));
+                        acc[kk][0] = fmaf(q2.z, f1.x, fmaf(-q2.w, f1.y, acc[kk][0]));
+                        acc[kk][1] = fmaf(q2.z, f1.y, fmaf(q2.w, f1.x, acc[kk][1]));
+                    }
+                }
+                for (; jj < nj; jj++) {
+                    const float2 q = __ldg(qrow + j0 + jj);
+#pragma unroll
+                    for (int kk = 0; kk < NK; kk++) {
+                        const float2 f0 = ph[jj][kk];
+                        acc[kk][0] = fmaf(q.x, f0.x, fmaf(-q.y, f0.y, acc[kk][0]));
+                        acc[kk][1] = fmaf(q.x, f0.y, fmaf(q.y, f0.x, acc[kk][1]));
+                    }
+                }
+#pragma unroll
+                for (int kk = 0; kk < NK; kk++) {
+                    tot[kk][0] += (double)acc[kk][0];
+                    tot[kk][1] += (double)acc[kk][1];
+                }
+            }
+        }
+    }
+    if (!active) return;
+#pragma unroll
+    for (int kk = 0; kk < NK; kk++) {
+        if (kk < g.nk) C[((long long)g.zi[kk] * 3 + c) * MF + p] = make_float2((float)tot[kk][0], (float)tot[kk][1]);
+    }
+}
+
+// Exterior regions: region 0 = incident (referenced at the origin) + reflected (at z_0),
+// last region = transmitted (at z_Z).  One thread per (z entry, c, p), FP64.
+__global__ void sep_exterior_kernel(const int2* __restrict__ ext, int n_ext, const float* __restrict__ zlist,
+                                    const double2* __restrict__ xd, int MF, double z0, double zZ,
+                                    float2* __restrict__ C) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)n_ext * 3 * MF) return;
+    const int e = (int)(idx / (3 * MF));
+    const int rem = (int)(idx % (3 * MF));
+    const int c = rem / MF, p = rem % MF;
+    const int2 ent = ext[e];     // (zi, 0 = top exterior / 1 = bottom exterior)
+    const double z = (double)zlist[ent.x];
+    // xd layout: inc[3][MF], refl[3][MF], trans[3][MF], kz_inc[MF], kz_refl[MF], kz_trans[MF]
+    const double2* inc = xd;
+    const double2* refl = xd + 3 * MF;
+    const double2* trans = xd + 6 * MF;
+    const double2* kzi = xd + 9 * MF;
+    const double2* kzr = xd + 10 * MF;
+    const double2* kzt = xd + 11 * MF;
+    double sr = 0.0, si = 0.0;
+    auto add = [&](double2 a, double2 k, double dz) {
+        const float2 f = phase_fp64(k.x, k.y, dz);
+        sr += a.x * (double)f.x - a.y * (double)f.y;
+        si += a.x * (double)f.y + a.y * (double)f.x;
+    };
+    if (ent.y == 0) {
+        add(inc[c * MF + p], kzi[p], z);
+        add(refl[c * MF + p], kzr[p], z - z0);
+    } else {
+        add(trans[c * MF + p], kzt[p], z - zZ);
+    }
+    C[((long long)ent.x * 3 + c) * MF + p] = make_float2((float)sr, (float)si);
+}
+
+// tab[m][i] = exp(i k_m x_i), x_i = s + d * i in float (one rounding per operation)
+__global__ void sep_table_kernel(const double* __restrict__ k, int M, float s, float d, int N, float2* __restrict__ tab) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)M * N) return;
+    const int m = (int)(idx / N), i = (int)(idx % N);
+    const float x = __fadd_rn(s, __fmul_rn(d, (float)i));
+    tab[idx] = phase_fp64(k[m], 0.0, (double)x);
+}
+
+// Stage 2a: T[r][c][m] = sum_n R(r, n) * C[zi(r)][c][p(m, n)]
+//   ctype 0: m = a (keep), n = b (contract), p = a*M1 + b
+//   ctype 1: m = b (keep), n = a (contract)
+// R(r, n) = Rtab[n * rld + r % rmod];  zi(r) = zoff + r / rdiv
+__global__ void sep_rows_kernel(const float2* __restrict__ C, const float2* __restrict__ Rtab, int rld, int rmod,
+                                int rdiv, int zoff, int nrows, int ctype, int M0, int M1, float2* __restrict__ T) {
+    const int Mk = ctype == 0 ? M0 : M1;
+    const int Mn = ctype == 0 ? M1 : M0;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nrows * 3 * Mk) return;
+    const int r = (int)(idx / (3 * Mk));
+    const int rem = (int)(idx % (3 * Mk));
+    const int c = rem / Mk, m = rem % Mk;
+    const int zi = zoff + r / rdiv;
+    const float2* Cz = C + ((long long)zi * 3 + c) * M0 * M1;
+    const int ro = r % rmod;
+    float sr = 0.f, si = 0.f;
+    for (int n = 0; n < Mn; n++) {
+        const float2 rv = Rtab[(long long)n * rld + ro];
+        const float2 cv = ctype == 0 ? Cz[m * M1 + n] : Cz[n * M1 + m];
+        sr = fmaf(rv.x, cv.x, fmaf(-rv.y, cv.y, sr));
+        si = fmaf(rv.x, cv.y, fmaf(rv.y, cv.x, si));
+    }
+    T[idx] = make_float2(sr, si);
+}
+
+// Stage 2b (FP32 SIMT): E[r][col][c] = sum_m T[r][c][m] * F[m][col]
+// CTA: 32 rows x 64 columns; thread: 2 rows x 4 columns x 3 components.
+constexpr int kSynRows = 32, kSynCols = 64, kSynMaxK = 64;
+
+__global__ void __launch_bounds__(256)
+sep_synth_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int nrows, int ncols, int Mk,
+                 float* __restrict__ out) {
+    extern __shared__ float2 smem[];
+    float2* sT = smem;                                  // [kSynRows][3][Mk]
+    float2* sF = smem + kSynRows * 3 * kSynMaxK;        // [Mk][kSynCols]
+    const int r0 = blockIdx.y * kSynRows, c0 = blockIdx.x * kSynCols;
+    for (int e = threadIdx.x; e < kSynRows * 3 * Mk; e += blockDim.x) {
+        const int rr = e / (3 * Mk);
+        sT[e] = (r0 + rr < nrows) ? T[(long long)r0 * 3 * Mk + e] : make_float2(0.f, 0.f);
+    }
+    for (int e = threadIdx.x; e < Mk * kSynCols; e += blockDim.x) {
+        const int m = e / kSynCols, cc = e % kSynCols;
+        sF[e] = (c0 + cc < ncols) ? F[(long long)m * ncols + c0 + cc] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
+    float acc[2][4][3][2];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) acc[a][b][c][0] = acc[a][b][c][1] = 0.f;
+    for (int m = 0; m < Mk; m++) {
+        float2 f[4];
+#pragma unroll
+        for (int b = 0; b < 4; b++) f[b] = sF[m * kSynCols + tc + 16 * b];
+#pragma unroll
+        for (int a = 0; a < 2; a++) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const float2 t = sT[((tr * 2 + a) * 3 + c) * Mk + m];
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    acc[a][b][c][0] = fmaf(t.x, f[b].x, fmaf(-t.y, f[b].y, acc[a][b][c][0]));
+                    acc[a][b][c][1] = fmaf(t.x, f[b].y, fmaf(t.y, f[b].x, acc[a][b][c][1]));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        const int r = r0 + tr * 2 + a;
+        if (r >= nrows) continue;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int col = c0 + tc + 16 * b;
+            if (col >= ncols) continue;
+            float* o = out + ((long long)r * ncols + col) * 6;
+            const float2 v0 = make_float2(acc[a][b][0][0], acc[a][b][0][1]);
+            const float2 v1 = make_float2(acc[a][b][1][0], acc[a][b][1][1]);
+            const float2 v2 = make_float2(acc[a][b][2][0], acc[a][b][2][1]);
+            reinterpret_cast<float2*>(o)[0] = v0;
+            reinterpret_cast<float2*>(o)[1] = v1;
+            reinterpret_cast<float2*>(o)[2] = v2;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------
+static int64_t sep_region(const scw_sep_s* s, float z) {
+    int64_t l = 0;
+    const double zd = (double)z;
+    for (int li = 0; li <= s->Z; li++) {
+        const double thr = (s->rule == 0) ? (double)s->z_layers[li] - 0.001 : (double)s->z_layers[li];
+        if (zd >= thr) l = li + 1;
+    }
+    return l;
+}
+
+static float host_coord(float s, float d, int i) {
+    volatile float p = d * (float)i;
+    volatile float r = s + p;
+    return r;
+}
+
+static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Stage 1 for a list of z-values: fills C [nz][3][MF] in the context's scratch.
+static scw_status stage1(scw_sep s, const std::vector<float>& zlist, float2* dC, char*& cursor) {
+    scw_ctx ctx = s->ctx;
+    const int MF = s->MF, J = s->J;
+    std::vector<PGroup> groups;
+    std::vector<int2> ext;
+    std::map<int64_t, std::vector<int>> by_region;
+    for (int i = 0; i < (int)zlist.size(); i++) by_region[sep_region(s, zlist[i])].push_back(i);
+    int max_nk = 1;
+    for (auto& kv : by_region) {
+        const int64_t r = kv.first;
+        if (r == 0 || r == s->Z + 1) {
+            for (int zi : kv.second) ext.push_back(make_int2(zi, r == 0 ? 0 : 1));
+            continue;
+        }
+        for (size_t o = 0; o < kv.second.size(); o += kMaxGroup) {
+            PGroup g{};
+            g.region = (int)r;
+            g.nk = (int)std::min<size_t>(kMaxGroup, kv.second.size() - o);
+            for (int kk = 0; kk < g.nk; kk++) g.zi[kk] = kv.second[o + kk];
+            max_nk = std::max(max_nk, g.nk);
+            groups.push_back(g);
+        }
+    }
+    // descriptors to the device (pinned staging, guarded by the context's event)
+    const size_t gbytes = groups.size() * sizeof(PGroup), ebytes = ext.size() * sizeof(int2),
+                 zbytes = zlist.size() * sizeof(float);
+    const size_t off_e = align256(gbytes), off_z = off_e + align256(ebytes), total = off_z + align256(zbytes);
+    SCW_CUDA_TRY(cudaEventSynchronize(ctx->desc_done));
+    scw_status st = ctx->host_desc.reserve(total);
+    if (st != SCW_OK) return st;
+    st = ctx->desc.reserve(total);
+    if (st != SCW_OK) return st;
+    char* h = (char*)ctx->host_desc.ptr;
+    if (gbytes) std::memcpy(h, groups.data(), gbytes);
+    if (ebytes) std::memcpy(h + off_e, ext.data(), ebytes);
+    std::memcpy(h + off_z, zlist.data(), zbytes);
+    SCW_CUDA_TRY(cudaMemcpyAsync(ctx->desc.ptr, h, total, cudaMemcpyHostToDevice, ctx->stream));
+    SCW_CUDA_TRY(cudaEventRecord(ctx->desc_done, ctx->stream));
+    const PGroup* dg = (const PGroup*)ctx->desc.ptr;
+    const int2* de = (const int2*)((char*)ctx->desc.ptr + off_e);
+    const float* dz = (const float*)((char*)ctx->desc.ptr + off_z);
+
+    if (!groups.empty()) {
+        if (J > 0) {
+            float2* dPhi = (float2*)cursor;
+            cursor += align256(groups.size() * 2 * (size_t)J * kMaxGroup * sizeof(float2));
+            dim3 gp((2 * J + 255) / 256, (unsigned)groups.size());
+            sep_phase_kernel<<<gp, 256, 0, ctx->stream>>>(dg, dz, s->dKz, s->dzb, J, dPhi);
+            SCW_CUDA_TRY(cudaGetLastError());
+            ctx->launches++;
+            dim3 gc((3 * MF + 127) / 128, (unsigned)groups.size());
+            if (max_nk <= 1)
+                sep_contract_kernel<1><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+            else if (max_nk <= 2)
+                sep_contract_kernel<2><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+            else if (max_nk <= 4)
+                sep_contract_kernel<4><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+            else
+                sep_contract_kernel<8><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+            SCW_CUDA_TRY(cudaGetLastError());
+            ctx->launches++;
+        } else {
+            // no interior waves (--external files): interior coefficients are zero
+            for (const auto& g : groups)
+                for (int kk = 0; kk < g.nk; kk++)
+                    SCW_CUDA_TRY(cudaMemsetAsync(dC + (size_t)g.zi[kk] * 3 * MF, 0, 3 * MF * sizeof(float2),
+                                                 ctx->stream));
+        }
+    }
+    if (!ext.empty()) {
+        const long long n = (long long)ext.size() * 3 * MF;
+        sep_exterior_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(de, (int)ext.size(), dz, s->dExt, MF,
+                                                                                 s->zb[0], s->zb[s->Z], dC);
+        SCW_CUDA_TRY(cudaGetLastError());
+        ctx->launches++;
+    }
+    return SCW_OK;
+}
+
+static scw_status launch_table(scw_ctx ctx, const double* dk, int M, float st, float d, int N, float2* tab) {
+    const long long n = (long long)M * N;
+    sep_table_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(dk, M, st, d, N, tab);
+    SCW_CUDA_TRY(cudaGetLastError());
+    ctx->launches++;
+    return SCW_OK;
+}
+
+static scw_status launch_rows(scw_ctx ctx, const float2* C, const float2* Rtab, int rld, int rmod, int rdiv, int zoff,
+                              int nrows, int ctype, int M0, int M1, float2* T) {
+    const int Mk = ctype == 0 ? M0 : M1;
+    const long long n = (long long)nrows * 3 * Mk;
+    sep_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(C, Rtab, rld, rmod, rdiv, zoff, nrows, ctype,
+                                                                          M0, M1, T);
+    SCW_CUDA_TRY(cudaGetLastError());
+    ctx->launches++;
+    return SCW_OK;
+}
+
+scw_status sep_synth(scw_ctx ctx, const float2* T, const float2* F, int nrows, int ncols, int Mk, float* out,
+                     int method) {
+    if (method == SCW_SEP_TF32X3 || method == SCW_SEP_BF16X3) {
+        scw_status st = sep_synth_tc(ctx, T, F, nrows, ncols, Mk, out, method);
+        if (st != SCW_ERR_UNSUPPORTED) return st;
+        return fail(SCW_ERR_UNSUPPORTED, "tensor-core synthesis does not support this shape");
+    }
+    if (Mk > kSynMaxK) return fail(SCW_ERR_UNSUPPORTED, "more than 64 harmonics along the synthesis axis");
+    const size_t smem = (size_t)(kSynRows * 3 * kSynMaxK + kSynMaxK * kSynCols) * sizeof(float2);
+    static bool attr_set = false;
+    if (!attr_set) {
+        SCW_CUDA_TRY(cudaFuncSetAttribute(sep_synth_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    dim3 grid((ncols + kSynCols - 1) / kSynCols, (nrows + kSynRows - 1) / kSynRows);
+    sep_synth_kernel<<<grid, 256, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, out);
+    SCW_CUDA_TRY(cudaGetLastError());
+    ctx->launches++;
+    return SCW_OK;
+}
+
+// One evaluation "sheet" family: a volume of xy planes, or an xz / yz plane.
+scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, float db, float dz, int Na, int Nb,
+                    int Nz, float* dE, int method) {
+    scw_ctx ctx = s->ctx;
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int M0 = s->M0, M1 = s->M1, MF = s->MF;
+    // z-values needed
+    std::vector<float> zlist;
+    if (kind == 0) {            // volume: Nz xy planes at z = c + dz*k; a = x (Na), b = y (Nb)
+        for (int k = 0; k < Nz; k++) zlist.push_back(host_coord(c, dz, k));
+    } else {                    // kind 1: xz plane at y = c (a = x, rows = z); kind 2: yz plane at x = c (a = y)
+        for (int k = 0; k < Nb; k++) zlist.push_back(host_coord(b0, db, k));
+    }
+    const int nz = (int)zlist.size();
+    // scratch layout
+    int nrows = 0, ncols = 0, Mk = 0;
+    if (kind == 0) { nrows = Nz * Nb; ncols = Na; Mk = M0; }
+    else if (kind == 1) { nrows = Nb; ncols = Na; Mk = M0; }
+    else { nrows = Nb; ncols = Na; Mk = M1; }
+    // phases for the PGroups: at most nz groups
+    const size_t phi_bytes = align256((size_t)nz * 2 * (size_t)s->J * kMaxGroup * sizeof(float2));
+    const size_t c_bytes = align256((size_t)nz * 3 * MF * sizeof(float2));
+    const size_t t_bytes = align256((size_t)nrows * 3 * Mk * sizeof(float2) + 4096);
+    const size_t tab_bytes = align256((size_t)(M0 + M1) * (Na + Nb + 2) * sizeof(float2));
+    scw_status st = ctx->sep_scratch.reserve(phi_bytes + c_bytes + t_bytes + 2 * tab_bytes);
+    if (st != SCW_OK) return st;
+    char* cursor = (char*)ctx->sep_scratch.ptr;
+    float2* dC = (float2*)cursor;
+    cursor += c_bytes;
+    float2* dT = (float2*)cursor;
+    cursor += t_bytes;
+    float2* tabA = (float2*)cursor;
+    cursor += tab_bytes;
+    float2* tabB = (float2*)cursor;
+    cursor += tab_bytes;
+    st = stage1(s, zlist, dC, cursor);
+    if (st != SCW_OK) return st;
+    if (kind == 0) {
+        // F = Ex table [a][x]; R = Ey table [b][y]
+        if ((st = launch_table(ctx, s->dkx, M0, a0, da, Na, tabA)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dky, M1, b0, db, Nb, tabB)) != SCW_OK) return st;
+        if ((st = launch_rows(ctx, dC, tabB, Nb, Nb, Nb, 0, nrows, 0, M0, M1, dT)) != SCW_OK) return st;
+        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, method);
+    } else if (kind == 1) {
+        // xz plane at y = c: R = Ey(c) [b]; F = Ex table [a][x]
+        if ((st = launch_table(ctx, s->dkx, M0, a0, da, Na, tabA)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dky, M1, c, 0.f, 1, tabB)) != SCW_OK) return st;
+        if ((st = launch_rows(ctx, dC, tabB, 1, 1, 1, 0, nrows, 0, M0, M1, dT)) != SCW_OK) return st;
+        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, method);
+    } else {
+        // yz plane at x = c: R = Ex(c) [a]; F = Ey table [b][y]
+        if ((st = launch_table(ctx, s->dky, M1, a0, da, Na, tabA)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dkx, M0, c, 0.f, 1, tabB)) != SCW_OK) return st;
+        if ((st = launch_rows(ctx, dC, tabB, 1, 1, 1, 0, nrows, 1, M0, M1, dT)) != SCW_OK) return st;
+        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, method);
+    }
+}
+
+}  // namespace scw
+
+using scw::fail;
+
+// ------------------------------------------------------------------------------------
+// C ABI
+// ------------------------------------------------------------------------------------
+static void sep_free(scw_sep s) {
+    if (!s) return;
+    if (s->ctx) cudaSetDevice(s->ctx->device);
+    if (s->dQ && s->own_Q) cudaFree(s->dQ);
+    if (s->dKz) cudaFree(s->dKz);
+    if (s->dExt) cudaFree(s->dExt);
+    if (s->dkx) cudaFree(s->dkx);
+    if (s->dky) cudaFree(s->dky);
+    if (s->dzb) cudaFree(s->dzb);
+    delete s;
+}
+
+extern "C" {
+
+scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half, const double* kx,
+                          const double* ky, const double* z_boundaries, scw_sep* out) {
+    if (!ctx || !out || M0 <= 0 || M1 <= 0 || n_slices < 0 || modes_per_half < 0 || !kx || !ky || !z_boundaries)
+        return fail(SCW_ERR_ARG, "scw_sep_create: bad arguments");
+    *out = nullptr;
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    scw_sep s = new (std::nothrow) scw_sep_s();
+    if (!s) return fail(SCW_ERR_NOMEM, "host allocation");
+    s->ctx = ctx;
+    s->M0 = M0;
+    s->M1 = M1;
+    s->MF = M0 * M1;
+    s->Z = n_slices;
+    s->J = modes_per_half;
+    s->kx.assign(kx, kx + M0);
+    s->ky.assign(ky, ky + M1);
+    s->zb.assign(z_boundaries, z_boundaries + n_slices + 1);
+    s->z_layers.resize(n_slices + 1);
+    for (int l = 0; l <= n_slices; l++) s->z_layers[l] = (float)z_boundaries[l];
+    const size_t nQ = (size_t)n_slices * 2 * 3 * s->MF * (size_t)s->J;
+    bool ok = cudaMalloc(&s->dkx, M0 * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&s->dky, M1 * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&s->dzb, (n_slices + 1) * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&s->dExt, 12 * (size_t)s->MF * sizeof(double2)) == cudaSuccess &&
+              cudaMalloc(&s->dKz, ((size_t)n_slices * 2 * s->J + 1) * sizeof(double2)) == cudaSuccess;
+    if (ok && nQ) {
+        ok = cudaMalloc(&s->dQ, nQ * sizeof(float2)) == cudaSuccess;
+        s->own_Q = true;
+    }
+    if (!ok) {
+        sep_free(s);
+        return fail(SCW_ERR_NOMEM, "cudaMalloc of the separable coefficient set");
+    }
+    cudaMemcpy(s->dkx, kx, M0 * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->dky, ky, M1 * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->dzb, z_boundaries, (n_slices + 1) * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemset(s->dExt, 0, 12 * (size_t)s->MF * sizeof(double2));
+    if (nQ) cudaMemset(s->dQ, 0, nQ * sizeof(float2));
+    cudaMemset(s->dKz, 0, ((size_t)n_slices * 2 * s->J + 1) * sizeof(double2));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        sep_free(s);
+        return fail(SCW_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *out = s;
+    return SCW_OK;
+}
+
+scw_status scw_sep_destroy(scw_sep s) {
+    sep_free(s);
+    return SCW_OK;
+}
+
+scw_status scw_sep_set_exterior(scw_sep s, const double* inc, const double* kz_inc, const double* refl,
+                                const double* kz_refl, const double* trans, const double* kz_trans) {
+    if (!s || !inc || !kz_inc || !refl || !kz_refl || !trans || !kz_trans)
+        return fail(SCW_ERR_ARG, "scw_sep_set_exterior: null argument");
+    const size_t MF = (size_t)s->MF;
+    std::vector<double> h(24 * MF);
+    std::memcpy(h.data(), inc, 6 * MF * 8);
+    std::memcpy(h.data() + 6 * MF, refl, 6 * MF * 8);
+    std::memcpy(h.data() + 12 * MF, trans, 6 * MF * 8);
+    std::memcpy(h.data() + 18 * MF, kz_inc, 2 * MF * 8);
+    std::memcpy(h.data() + 20 * MF, kz_refl, 2 * MF * 8);
+    std::memcpy(h.data() + 22 * MF, kz_trans, 2 * MF * 8);
+    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    SCW_CUDA_TRY(cudaMemcpy(s->dExt, h.data(), 24 * MF * 8, cudaMemcpyHostToDevice));
+    return SCW_OK;
+}
+
+scw_status scw_sep_set_slice(scw_sep s, int l, const double* kz_dn, const double* Q_dn, const double* kz_up,
+                             const double* Q_up) {
+    if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_sep_set_slice: slice out of range");
+    const size_t J = (size_t)s->J, MF = (size_t)s->MF;
+    if (J == 0) return SCW_OK;
+    if (!kz_dn || !Q_dn || !kz_up || !Q_up) return fail(SCW_ERR_ARG, "scw_sep_set_slice: null argument");
+    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    std::vector<double> kz(4 * J);
+    std::memcpy(kz.data(), kz_dn, 2 * J * 8);
+    std::memcpy(kz.data() + 2 * J, kz_up, 2 * J * 8);
+    SCW_CUDA_TRY(cudaMemcpy(s->dKz + (size_t)l * 2 * J, kz.data(), 4 * J * 8, cudaMemcpyHostToDevice));
+    std::vector<float2> q(3 * MF * J);
+    for (int half = 0; half < 2; half++) {
+        const double* src = half == 0 ? Q_dn : Q_up;
+        for (size_t i = 0; i < 3 * MF * J; i++) q[i] = make_float2((float)src[2 * i], (float)src[2 * i + 1]);
+        SCW_CUDA_TRY(cudaMemcpy(s->dQ + ((size_t)l * 2 + half) * 3 * MF * J, q.data(), q.size() * sizeof(float2),
+                                cudaMemcpyHostToDevice));
+    }
+    return SCW_OK;
+}
+
+scw_status scw_sep_set_slice_device(scw_sep s, int l, const double* kz_dn, const void* Q_dn_c64, const double* kz_up,
+                                    const void* Q_up_c64) {
+    if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_sep_set_slice_device: slice out of range");
+    const size_t J = (size_t)s->J, MF = (size_t)s->MF;
+    if (J == 0) return SCW_OK;
+    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    std::vector<double> kz(4 * J);
+    std::memcpy(kz.data(), kz_dn, 2 * J * 8);
+    std::memcpy(kz.data() + 2 * J, kz_up, 2 * J * 8);
+    SCW_CUDA_TRY(cudaMemcpy(s->dKz + (size_t)l * 2 * J, kz.data(), 4 * J * 8, cudaMemcpyHostToDevice));
+    const size_t blk = 3 * MF * J * sizeof(float2);
+    SCW_CUDA_TRY(cudaMemcpyAsync(s->dQ + ((size_t)l * 2 + 0) * 3 * MF * J, Q_dn_c64, blk, cudaMemcpyDefault,
+                                 s->ctx->stream));
+    SCW_CUDA_TRY(cudaMemcpyAsync(s->dQ + ((size_t)l * 2 + 1) * 3 * MF * J, Q_up_c64, blk, cudaMemcpyDefault,
+                                 s->ctx->stream));
+    return SCW_OK;
+}
+
+scw_status scw_sep_set_region_rule(scw_sep s, int rule) {
+    if (!s || (rule != 0 && rule != 1)) return fail(SCW_ERR_ARG, "region rule must be 0 or 1");
+    s->rule = rule;
+    return SCW_OK;
+}
+
+scw_status scw_sep_eval_volume_device(scw_sep s, float x_start, float y_start, float z_start, float dx, float dy,
+                                      float dz, int Nx, int Ny, int Nz, float* dE, int method) {
+    if (!s || !dE || Nx <= 0 || Ny <= 0 || Nz <= 0) return fail(SCW_ERR_ARG, "scw_sep_eval_volume_device: bad arguments");
+    return scw::sep_eval(s, 0, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, Nz, dE, method);
+}
+
+scw_status scw_sep_eval_plane_device(scw_sep s, int axis, float a_start, float b_start, float c, float d, int N,
+                                     float* dE, int method) {
+    if (!s || !dE || N <= 0 || axis < 0 || axis > 2) return fail(SCW_ERR_ARG, "scw_sep_eval_plane_device: bad arguments");
+    if (axis == 0) return scw::sep_eval(s, 0, a_start, b_start, c, d, d, 0.f, N, N, 1, dE, method);
+    if (axis == 2) return scw::sep_eval(s, 1, a_start, b_start, c, d, d, 0.f, N, N, 1, dE, method);
+    return scw::sep_eval(s, 2, a_start, b_start, c, d, d, 0.f, N, N, 1, dE, method);
+}
+
+scw_status scw_sep_gpu_cw_evaluate(scw_sep s, float* E_xy, float* E_xz, float* E_yz, float x_start, float y_start,
+                                   float z_start, float x, float y, float z, float d, int N, int device, int method) {
+    if (!s || !E_xy || !E_xz || !E_yz || N <= 0) return fail(SCW_ERR_ARG, "scw_sep_gpu_cw_evaluate: bad arguments");
+    scw_ctx ctx = s->ctx;
+    if (device != ctx->device) return fail(SCW_ERR_ARG, "scw_sep_gpu_cw_evaluate: device differs from the set's device");
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    const size_t plane = (size_t)N * N * 6;
+    scw_status st = ctx->planes_out.reserve(3 * plane * sizeof(float));
+    if (st != SCW_OK) return st;
+    float* d0 = (float*)ctx->planes_out.ptr;
+    if ((st = scw_sep_eval_plane_device(s, 0, x_start, y_start, z, d, N, d0, method)) != SCW_OK) return st;
+    if ((st = scw_sep_eval_plane_device(s, 2, x_start, z_start, y, d, N, d0 + plane, method)) != SCW_OK) return st;
+    if ((st = scw_sep_eval_plane_device(s, 1, y_start, z_start, x, d, N, d0 + 2 * plane, method)) != SCW_OK) return st;
+    SCW_CUDA_TRY(cudaMemcpyAsync(E_xy, d0, plane * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SCW_CUDA_TRY(cudaMemcpyAsync(E_xz, d0 + plane, plane * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SCW_CUDA_TRY(cudaMemcpyAsync(E_yz, d0 + 2 * plane, plane * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SCW_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return SCW_OK;
+}
+
+}  // extern "C"

@@ -48,6 +48,7 @@ struct scw_ctx_s {
     scw::DevBuf scratch;        // split-K partial sums of the plain evaluator
     scw::DevBuf desc;           // per-call work descriptors
     scw::DevBuf planes_out;     // device staging of gpu_cw_evaluate's three planes
+    scw::DevBuf sep_scratch;    // separable evaluator: phases, coefficients C, row products T, tables
     scw::PinnedBuf host_desc;   // pinned staging of the descriptors
     cudaEvent_t desc_done = nullptr;  // the last descriptor upload has been consumed
 };

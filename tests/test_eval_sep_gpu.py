@@ -1,0 +1,88 @@
+"""Separable (GEMM-form) evaluator vs the FP64 oracle (same field as gpu_cw_evaluate)."""
+import numpy as np
+import pytest
+
+from oracle import oracle_lib as ol
+from oracle import solve_oracle as so
+from tests._util import rel_l2, solved_case, to_structure
+
+pytestmark = pytest.mark.gpu
+
+# Separable form: FP64-reduced phases rounded to FP32; FP32 stage-1 sums per 256-mode chunk
+# with FP64 running sums; FP32 (SIMT) or 3-product split tensor-core output GEMM.
+TOL_SEP = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from scwatter_gb300 import evaluator as ev
+    return ev.Context(0)
+
+
+def _planes_oracle(c, rule, xs, ys, zs, x, y, z, d, N):
+    W, b, e, zl = so.unpack(c)
+    thr = ol.thresholds(zl, rule)
+    out = []
+    for axis, a0, b0, cc in [(ol.AXIS_XY, xs, ys, z), (ol.AXIS_XZ, xs, zs, y), (ol.AXIS_YZ, ys, zs, x)]:
+        P = ol.plane_points(axis, a0, b0, cc, d, N)
+        out.append(ol.eval_points_f64(W, b, e, thr, P.reshape(-1, 3)).reshape(N, N, 3))
+    return out
+
+
+@pytest.mark.parametrize("method", [1])
+@pytest.mark.parametrize("shape,coef,direction", [((3, 16, 16), (5, 5), (0, 0, 1)),
+                                                  ((2, 12, 16), (5, 3), (0.2, 0.1, 1.0))])
+def test_solved_cw_planes(ctx, shape, coef, direction, method):
+    from scwatter_gb300.separable import SeparableSet
+    _, _, _, c = solved_case(shape=shape, coef=coef, seed=2, direction=direction)
+    sep = SeparableSet.from_cw(ctx, to_structure(c))
+    M0, M1, Z, J = sep.info()
+    assert (M0, M1, Z) == (coef[0], coef[1], shape[0])
+    N = 48
+    ext = float(max(shape[1], shape[2]) + 8)
+    d = np.float32(ext / (N - 1))
+    xs = ys = zs = np.float32(-ext / 2)
+    got = sep.evaluate_planes_host(xs, ys, zs, 0.3, -0.6, 0.2, d, N, method=method)
+    ref = _planes_oracle(c, "gpu", xs, ys, zs, 0.3, -0.6, 0.2, d, N)
+    for g, r, name in zip(got, ref, ["xy", "xz", "yz"]):
+        err = rel_l2(g, r)
+        assert max(err) < TOL_SEP, (name, err)
+
+
+@pytest.mark.parametrize("method", [1])
+def test_synthetic_volume(ctx, method):
+    import torch
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import SeparableSet
+    fs = synthetic.make_factored(M0=6, M1=4, Z=3, size=(12.0, 10.0, 3.0), seed=5)
+    sep = SeparableSet.from_factored(ctx, fs)
+    Nx, Ny, Nz = 37, 21, 11
+    x0, y0, z0 = np.float32(-7), np.float32(-6), np.float32(-2.5)
+    dx, dy, dz = np.float32(0.4), np.float32(0.55), np.float32(0.5)
+    out = torch.zeros((Nz, Ny, Nx, 3), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    sep.eval_volume_device(x0, y0, z0, dx, dy, dz, Nx, Ny, Nz, out.data_ptr(), method=method)
+    ctx.synchronize()
+    got = out.cpu().numpy()
+    Pi, zsl, Pr, Pt = synthetic.to_cw_arrays(fs)
+    c = so.CW(Pi=Pi, z=zsl, Pr=Pr, Pt=Pt)
+    W, b, e, zl = so.unpack(c)
+    ix = (x0 + dx * np.arange(Nx, dtype=np.float32)).astype(np.float32)
+    iy = (y0 + dy * np.arange(Ny, dtype=np.float32)).astype(np.float32)
+    iz = (z0 + dz * np.arange(Nz, dtype=np.float32)).astype(np.float32)
+    P = np.stack(np.meshgrid(iz, iy, ix, indexing="ij"), -1)[..., ::-1]   # [Nz, Ny, Nx, (x, y, z)]
+    ref = ol.eval_points_f64(W, b, e, ol.thresholds(zl, "gpu"), P.reshape(-1, 3)).reshape(Nz, Ny, Nx, 3)
+    assert max(rel_l2(got, ref)) < TOL_SEP
+
+
+def test_not_separable_is_rejected(ctx):
+    """A .cw whose waves do not share a harmonic grid is refused with SCW_ERR_UNSUPPORTED."""
+    from scwatter_gb300 import _lib
+    from scwatter_gb300.separable import SeparableSet
+    _, _, _, c = solved_case(shape=(2, 12, 12), coef=(3, 3), seed=3)
+    S = to_structure(c)
+    S.Layers[1].Pr = S.Layers[1].Pr.copy()
+    S.Layers[1].Pr[5, 5] += 0.125        # one mode's kz differs across harmonics
+    with pytest.raises(_lib.ScwError) as ei:
+        SeparableSet.from_cw(ctx, S)
+    assert ei.value.status == 9

@@ -130,6 +130,7 @@ scw_status scw_ctx_destroy(scw_ctx c) {
     c->planes_out.release();
     c->sep_scratch.release();
     c->host_desc.release();
+    if (c->tc_err) cudaFree(c->tc_err);
     if (c->desc_done) cudaEventDestroy(c->desc_done);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -139,6 +140,12 @@ scw_status scw_ctx_destroy(scw_ctx c) {
 scw_status scw_ctx_synchronize(scw_ctx c) {
     if (!c) return fail(SCW_ERR_ARG, "null context");
     SCW_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (c->tc_pending_check && c->tc_err) {
+        int flag = 0;
+        SCW_CUDA_TRY(cudaMemcpy(&flag, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+        c->tc_pending_check = false;
+        if (flag) return fail(SCW_ERR_TIMEOUT, "a tensor-core kernel's bounded mbarrier wait gave up");
+    }
     return SCW_OK;
 }
 

@@ -622,8 +622,7 @@ scw_status scw_sep_gpu_cw_evaluate(scw_sep s, float* E_xy, float* E_xz, float* E
     SCW_CUDA_TRY(cudaMemcpyAsync(E_xy, d0, plane * 4, cudaMemcpyDeviceToHost, ctx->stream));
     SCW_CUDA_TRY(cudaMemcpyAsync(E_xz, d0 + plane, plane * 4, cudaMemcpyDeviceToHost, ctx->stream));
     SCW_CUDA_TRY(cudaMemcpyAsync(E_yz, d0 + 2 * plane, plane * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    SCW_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    return SCW_OK;
+    return scw_ctx_synchronize(ctx);
 }
 
 }  // extern "C"

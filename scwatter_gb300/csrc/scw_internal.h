@@ -51,6 +51,8 @@ struct scw_ctx_s {
     scw::DevBuf sep_scratch;    // separable evaluator: phases, coefficients C, row products T, tables
     scw::PinnedBuf host_desc;   // pinned staging of the descriptors
     cudaEvent_t desc_done = nullptr;  // the last descriptor upload has been consumed
+    int* tc_err = nullptr;            // device flag: a tensor-core kernel's bounded wait gave up
+    bool tc_pending_check = false;    // a tensor-core kernel ran since the flag was last read
 };
 
 struct scw_cw_s {

@@ -11,6 +11,7 @@ pytestmark = pytest.mark.gpu
 # Separable form: FP64-reduced phases rounded to FP32; FP32 stage-1 sums per 256-mode chunk
 # with FP64 running sums; FP32 (SIMT) or 3-product split tensor-core output GEMM.
 TOL_SEP = 1e-5
+TOL = {1: TOL_SEP, 2: TOL_SEP, 3: 1e-4}     # FP32 SIMT, 3xTF32, split-BF16 (16-bit operands)
 
 
 @pytest.fixture(scope="module")
@@ -29,7 +30,7 @@ def _planes_oracle(c, rule, xs, ys, zs, x, y, z, d, N):
     return out
 
 
-@pytest.mark.parametrize("method", [1])
+@pytest.mark.parametrize("method", [1, 2, 3])
 @pytest.mark.parametrize("shape,coef,direction", [((3, 16, 16), (5, 5), (0, 0, 1)),
                                                   ((2, 12, 16), (5, 3), (0.2, 0.1, 1.0))])
 def test_solved_cw_planes(ctx, shape, coef, direction, method):
@@ -46,10 +47,10 @@ def test_solved_cw_planes(ctx, shape, coef, direction, method):
     ref = _planes_oracle(c, "gpu", xs, ys, zs, 0.3, -0.6, 0.2, d, N)
     for g, r, name in zip(got, ref, ["xy", "xz", "yz"]):
         err = rel_l2(g, r)
-        assert max(err) < TOL_SEP, (name, err)
+        assert max(err) < TOL[method], (name, err)
 
 
-@pytest.mark.parametrize("method", [1])
+@pytest.mark.parametrize("method", [1, 2, 3])
 def test_synthetic_volume(ctx, method):
     import torch
     from scwatter_gb300 import synthetic
@@ -72,7 +73,29 @@ def test_synthetic_volume(ctx, method):
     iz = (z0 + dz * np.arange(Nz, dtype=np.float32)).astype(np.float32)
     P = np.stack(np.meshgrid(iz, iy, ix, indexing="ij"), -1)[..., ::-1]   # [Nz, Ny, Nx, (x, y, z)]
     ref = ol.eval_points_f64(W, b, e, ol.thresholds(zl, "gpu"), P.reshape(-1, 3)).reshape(Nz, Ny, Nx, 3)
-    assert max(rel_l2(got, ref)) < TOL_SEP
+    assert max(rel_l2(got, ref)) < TOL[method]
+
+
+@pytest.mark.parametrize("method,tol", [(2, 2e-6), (3, 5e-5)])
+def test_tensor_core_matches_simt_many_tiles(ctx, method, tol):
+    """Enough rows that every CTA runs several row tiles (both TMEM accumulators, both
+    operand buffers), columns not a multiple of the 128-wide tile."""
+    import torch
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import SeparableSet
+    fs = synthetic.make_factored(M0=10, M1=8, Z=4, size=(20.0, 16.0, 4.0), seed=9)
+    sep = SeparableSet.from_factored(ctx, fs)
+    Nx, Ny, Nz = 200, 64, 40
+    args = (np.float32(-10), np.float32(-8), np.float32(-3), np.float32(0.1), np.float32(0.25), np.float32(0.15),
+            Nx, Ny, Nz)
+    outs = []
+    for m in (1, method):
+        o = torch.zeros((Nz, Ny, Nx, 3), dtype=torch.complex64, device="cuda")
+        torch.cuda.synchronize()
+        sep.eval_volume_device(*args, o.data_ptr(), method=m)
+        ctx.synchronize()
+        outs.append(o.cpu().numpy())
+    assert max(rel_l2(outs[1], outs[0])) < tol
 
 
 def test_not_separable_is_rejected(ctx):

@@ -66,6 +66,11 @@ SCW_API scw_status scw_ctx_synchronize(scw_ctx ctx);
 SCW_API scw_status scw_ctx_stream(scw_ctx ctx, void** stream);
 /* Number of kernels this context has launched since creation (evidence of GPU work). */
 SCW_API scw_status scw_ctx_launch_count(scw_ctx ctx, int64_t* count);
+/* Per-kernel CUDA-event timing of every launch while on; the report synchronises the stream,
+ * sums milliseconds and launch counts per kernel name ('\n'-separated in names) and clears. */
+SCW_API scw_status scw_ctx_set_timing(scw_ctx ctx, int on);
+SCW_API scw_status scw_ctx_timing_report(scw_ctx ctx, char* names, int64_t name_bytes, double* ms,
+                                         int64_t* counts, int max_entries, int* n);
 
 /* ---------------------------------------------------------------------------------- */
 /* .cw coefficient files -- replaces CoupledWaveStructure<T>::save / load /            */

@@ -38,6 +38,8 @@ _SIGS = {
     "scw_ctx_synchronize": [P],
     "scw_ctx_stream": [P, PP],
     "scw_ctx_launch_count": [P, ctypes.POINTER(I64)],
+    "scw_ctx_set_timing": [P, I32],
+    "scw_ctx_timing_report": [P, ctypes.c_char_p, I64, P, P, I32, ctypes.POINTER(I32)],
     "scw_cw_create": [PP],
     "scw_cw_destroy": [P],
     "scw_cw_load": [ctypes.c_char_p, PP],

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <fstream>
 #include <limits>
+#include <algorithm>
 #include <new>
 
 #include "scw_internal.h"
@@ -70,6 +71,30 @@ void PinnedBuf::release() {
     if (ptr) cudaFreeHost(ptr);
     ptr = nullptr;
     bytes = 0;
+}
+
+static cudaEvent_t pool_event(scw_ctx c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+LaunchTimer::LaunchTimer(scw_ctx c, const char* n) : ctx(c), name(n) {
+    if (!ctx->timing) return;
+    a = pool_event(ctx);
+    b = pool_event(ctx);
+    cudaEventRecord(a, ctx->stream);
+}
+
+LaunchTimer::~LaunchTimer() {
+    if (!a) return;
+    cudaEventRecord(b, ctx->stream);
+    ctx->timings.push_back(KernelTiming{name, a, b});
 }
 
 }  // namespace scw
@@ -131,6 +156,11 @@ scw_status scw_ctx_destroy(scw_ctx c) {
     c->sep_scratch.release();
     c->host_desc.release();
     if (c->tc_err) cudaFree(c->tc_err);
+    for (auto& t : c->timings) {
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.stop);
+    }
+    for (auto e : c->event_pool) cudaEventDestroy(e);
     if (c->desc_done) cudaEventDestroy(c->desc_done);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -152,6 +182,56 @@ scw_status scw_ctx_synchronize(scw_ctx c) {
 scw_status scw_ctx_stream(scw_ctx c, void** stream) {
     if (!c || !stream) return fail(SCW_ERR_ARG, "null argument");
     *stream = (void*)c->stream;
+    return SCW_OK;
+}
+
+scw_status scw_ctx_set_timing(scw_ctx c, int on) {
+    if (!c) return fail(SCW_ERR_ARG, "null context");
+    c->timing = on != 0;
+    return SCW_OK;
+}
+
+// Sums the recorded per-kernel times by name (after synchronising the stream) and clears
+// them.  names: '\n'-separated list written to a buffer of name_bytes; ms/counts: up to max
+// entries.  *n receives the number of distinct kernels.
+scw_status scw_ctx_timing_report(scw_ctx c, char* names, int64_t name_bytes, double* ms, int64_t* counts,
+                                 int max_entries, int* n) {
+    if (!c || !n) return fail(SCW_ERR_ARG, "null argument");
+    SCW_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    std::vector<std::string> keys;
+    std::vector<double> tot;
+    std::vector<int64_t> cnt;
+    for (auto& t : c->timings) {
+        float v = 0.f;
+        cudaEventElapsedTime(&v, t.start, t.stop);
+        size_t i = 0;
+        while (i < keys.size() && keys[i] != t.name) i++;
+        if (i == keys.size()) {
+            keys.push_back(t.name);
+            tot.push_back(0.0);
+            cnt.push_back(0);
+        }
+        tot[i] += v;
+        cnt[i] += 1;
+        c->event_pool.push_back(t.start);
+        c->event_pool.push_back(t.stop);
+    }
+    c->timings.clear();
+    *n = (int)keys.size();
+    std::string joined;
+    for (size_t i = 0; i < keys.size(); i++) {
+        if ((int)i < max_entries) {
+            if (ms) ms[i] = tot[i];
+            if (counts) counts[i] = cnt[i];
+        }
+        joined += keys[i];
+        joined += "\n";
+    }
+    if (names && name_bytes > 0) {
+        size_t m = std::min<size_t>((size_t)name_bytes - 1, joined.size());
+        std::memcpy(names, joined.data(), m);
+        names[m] = 0;
+    }
     return SCW_OK;
 }
 

@@ -423,11 +423,15 @@ static scw_status launch_planes(scw_waves w, std::vector<PlaneGeom>& planes) {
     const WorkItem* ditems = (const WorkItem*)(d + items_off);
     const ReduceTile* drt = (const ReduceTile*)(d + rt_off);
     WaveSoA soa{w->kre, w->kim, w->zref, w->amp, (long long)w->n};
-    plain_eval_kernel<<<(unsigned)P.items.size(), kThreads, 0, ctx->stream>>>(dplanes, ditems, soa,
-                                                                            (float*)ctx->scratch.ptr);
+    {
+        LaunchTimer lt(ctx, "plain_eval_kernel");
+        plain_eval_kernel<<<(unsigned)P.items.size(), kThreads, 0, ctx->stream>>>(dplanes, ditems, soa,
+                                                                                (float*)ctx->scratch.ptr);
+    }
     SCW_CUDA_TRY(cudaGetLastError());
     ctx->launches++;
     if (!P.rtiles.empty()) {
+        LaunchTimer lt(ctx, "plain_reduce_kernel");
         plain_reduce_kernel<<<(unsigned)P.rtiles.size(), kThreads, 0, ctx->stream>>>(dplanes, drt,
                                                                                    (const float*)ctx->scratch.ptr);
         SCW_CUDA_TRY(cudaGetLastError());

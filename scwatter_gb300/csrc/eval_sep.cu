@@ -326,10 +326,14 @@ static scw_status stage1(scw_sep s, const std::vector<float>& zlist, float2* dC,
             float2* dPhi = (float2*)cursor;
             cursor += align256(groups.size() * 2 * (size_t)J * kMaxGroup * sizeof(float2));
             dim3 gp((2 * J + 255) / 256, (unsigned)groups.size());
-            sep_phase_kernel<<<gp, 256, 0, ctx->stream>>>(dg, dz, s->dKz, s->dzb, J, dPhi);
+            {
+                LaunchTimer lt(ctx, "sep_phase_kernel");
+                sep_phase_kernel<<<gp, 256, 0, ctx->stream>>>(dg, dz, s->dKz, s->dzb, J, dPhi);
+            }
             SCW_CUDA_TRY(cudaGetLastError());
             ctx->launches++;
             dim3 gc((3 * MF + 127) / 128, (unsigned)groups.size());
+            LaunchTimer lt(ctx, "sep_contract_kernel");
             if (max_nk <= 1)
                 sep_contract_kernel<1><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
             else if (max_nk <= 2)
@@ -350,6 +354,7 @@ static scw_status stage1(scw_sep s, const std::vector<float>& zlist, float2* dC,
     }
     if (!ext.empty()) {
         const long long n = (long long)ext.size() * 3 * MF;
+        LaunchTimer lt(ctx, "sep_exterior_kernel");
         sep_exterior_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(de, (int)ext.size(), dz, s->dExt, MF,
                                                                                  s->zb[0], s->zb[s->Z], dC);
         SCW_CUDA_TRY(cudaGetLastError());
@@ -360,6 +365,7 @@ static scw_status stage1(scw_sep s, const std::vector<float>& zlist, float2* dC,
 
 static scw_status launch_table(scw_ctx ctx, const double* dk, int M, float st, float d, int N, float2* tab) {
     const long long n = (long long)M * N;
+    LaunchTimer lt(ctx, "sep_table_kernel");
     sep_table_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(dk, M, st, d, N, tab);
     SCW_CUDA_TRY(cudaGetLastError());
     ctx->launches++;
@@ -370,6 +376,7 @@ static scw_status launch_rows(scw_ctx ctx, const float2* C, const float2* Rtab, 
                               int nrows, int ctype, int M0, int M1, float2* T) {
     const int Mk = ctype == 0 ? M0 : M1;
     const long long n = (long long)nrows * 3 * Mk;
+    LaunchTimer lt(ctx, "sep_rows_kernel");
     sep_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(C, Rtab, rld, rmod, rdiv, zoff, nrows, ctype,
                                                                           M0, M1, T);
     SCW_CUDA_TRY(cudaGetLastError());
@@ -392,6 +399,7 @@ scw_status sep_synth(scw_ctx ctx, const float2* T, const float2* F, int nrows, i
         attr_set = true;
     }
     dim3 grid((ncols + kSynCols - 1) / kSynCols, (nrows + kSynRows - 1) / kSynRows);
+    LaunchTimer lt(ctx, "sep_synth_kernel");
     sep_synth_kernel<<<grid, 256, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, out);
     SCW_CUDA_TRY(cudaGetLastError());
     ctx->launches++;

@@ -340,6 +340,7 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     int yt = std::max(1, ctx->sm_count / xt);
     yt = std::min(yt, ntiles);
     dim3 grid(xt, yt);
+    LaunchTimer lt(ctx, kind == 0 ? "synth_tc_kernel<tf32x3>" : "synth_tc_kernel<bf16x3>");
     if (kind == 0) {
         SCW_CUDA_TRY(cudaFuncSetAttribute(tc::synth_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         tc::synth_tc_kernel<0><<<grid, tc::kThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, out, ctx->tc_err);

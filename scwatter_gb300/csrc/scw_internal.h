@@ -39,6 +39,12 @@ struct PinnedBuf {
 
 }  // namespace scw
 
+// Optional per-kernel CUDA-event timing (scw_ctx_set_timing): one record per launch.
+struct KernelTiming {
+    const char* name;
+    cudaEvent_t start, stop;
+};
+
 struct scw_ctx_s {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -53,7 +59,21 @@ struct scw_ctx_s {
     cudaEvent_t desc_done = nullptr;  // the last descriptor upload has been consumed
     int* tc_err = nullptr;            // device flag: a tensor-core kernel's bounded wait gave up
     bool tc_pending_check = false;    // a tensor-core kernel ran since the flag was last read
+    bool timing = false;
+    std::vector<KernelTiming> timings;
+    std::vector<cudaEvent_t> event_pool;
 };
+
+namespace scw {
+// brackets one kernel launch with events when the context's timing is on
+struct LaunchTimer {
+    scw_ctx ctx;
+    const char* name;
+    cudaEvent_t a = nullptr, b = nullptr;
+    LaunchTimer(scw_ctx c, const char* n);
+    ~LaunchTimer();
+};
+}  // namespace scw
 
 struct scw_cw_s {
     uint64_t sizeof_T = 8;

@@ -59,6 +59,19 @@ class Context:
         _lib.call("scw_ctx_launch_count", self.handle, ctypes.byref(n))
         return n.value
 
+    def set_timing(self, on: bool = True):
+        _lib.call("scw_ctx_set_timing", self.handle, 1 if on else 0)
+
+    def timing_report(self) -> dict:
+        """{kernel name: (total ms, launches)} since the last report (synchronises)."""
+        names = ctypes.create_string_buffer(4096)
+        ms = (ctypes.c_double * 64)()
+        cnt = (ctypes.c_int64 * 64)()
+        n = ctypes.c_int()
+        _lib.call("scw_ctx_timing_report", self.handle, names, 4096, ms, cnt, 64, ctypes.byref(n))
+        keys = names.value.decode().split("\n")[: n.value]
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(keys)}
+
     def close(self):
         if self.handle:
             _lib.load().scw_ctx_destroy(self.handle)

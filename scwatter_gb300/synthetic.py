@@ -128,3 +128,36 @@ def to_structure(fs: FactoredSample):
     S.Pi = Pi
     S.Layers = [HomogeneousLayer(z=zs[l], Pr=Pr[l], Pt=Pt[l]) for l in range(len(zs))]
     return S
+
+
+def device_factored(M0, M1, Z, size, lam=1.0, z_center=0.0, seed=0, device="cuda"):
+    """Same structure and value ranges as :func:`make_factored`, with the large Q blocks
+    drawn on the GPU (torch, seeded) as complex64 [Z, 3, MF, 2MF] tensors; everything else
+    on the host in float64/complex128.  Returns (fs, Q_dn, Q_up) with fs.Q_dn / fs.Q_up None."""
+    import torch
+    rng = np.random.default_rng(seed)
+    k = 2 * PI_REF / lam
+    MF = M0 * M1
+    J = 2 * MF
+    p = np.arange(M0) - M0 // 2
+    q = np.arange(M1) - M1 // 2
+    kx = 2 * PI_REF * p / size[0]
+    ky = 2 * PI_REF * q / size[1]
+    z = z_center - size[2] / 2 + np.arange(Z + 1) * (size[2] / Z)
+    re = rng.uniform(1.0, 1.4, size=(Z, J))
+    im = rng.uniform(0.0, 0.02, size=(Z, J))
+    gamma_dn = (re + 1j * im).astype(np.complex128)
+    gamma_up = (-re - 1j * im).astype(np.complex128)
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    scale = 1.0 / (2 * MF)
+    Q_dn = torch.randn((Z, 3, MF, J), dtype=torch.complex64, device=device, generator=g) * scale
+    Q_up = torch.randn((Z, 3, MF, J), dtype=torch.complex64, device=device, generator=g) * (0.3 * scale)
+    sz = np.sqrt((1.0 + 0j) - (np.repeat(kx, M1) / k) ** 2 - (np.tile(ky, M0) / k) ** 2)
+    inc = np.zeros((3, MF), np.complex128)
+    inc[0, (M0 // 2) * M1 + M1 // 2] = 1.0
+    refl = (rng.standard_normal((3, MF)) + 1j * rng.standard_normal((3, MF))) * 0.05
+    trans = (rng.standard_normal((3, MF)) + 1j * rng.standard_normal((3, MF))) * 0.5
+    fs = FactoredSample(M0, M1, k, kx, ky, z, gamma_dn, gamma_up, None, None, inc, refl, trans,
+                        sz * k, -sz * k, sz * k)
+    return fs, Q_dn, Q_up

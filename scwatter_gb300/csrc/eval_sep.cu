@@ -36,8 +36,9 @@ __device__ __forceinline__ float2 phase_fp64(double kr, double ki, double dz) {
     return make_float2(m * c, m * s);
 }
 
+// Phi[g][j][kk] (kk < nks) = exp(i kz_j (z_kk - zref_j)) for the group's planes, zero past g.nk
 __global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float* __restrict__ zlist,
-                                 const double2* __restrict__ kz, const double* __restrict__ zb, int J,
+                                 const double2* __restrict__ kz, const double* __restrict__ zb, int J, int nks,
                                  float2* __restrict__ Phi) {
     const PGroup g = groups[blockIdx.y];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -46,9 +47,8 @@ __global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float*
     const int half = j / J;
     const double2 k = kz[((long long)l * 2 + half) * J + (j - half * J)];
     const double zref = half == 0 ? zb[l] : zb[l + 1];
-    float2* out = Phi + ((long long)blockIdx.y * 2 * J + j) * kMaxGroup;
-#pragma unroll
-    for (int kk = 0; kk < kMaxGroup; kk++) {
+    float2* out = Phi + ((long long)blockIdx.y * 2 * J + j) * nks;
+    for (int kk = 0; kk < nks; kk++) {
         if (kk < g.nk) {
             const double dz = (double)zlist[g.zi[kk]] - zref;
             out[kk] = phase_fp64(k.x, k.y, dz);
@@ -59,68 +59,77 @@ __global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float*
 }
 
 // C[zi][c][p] = sum over the slice's 2J modes of Q[l][half][c][p][j] * Phi[g][half*J + j][kk]
-template <int NK>
-__global__ void __launch_bounds__(128)
+//
+// HBM-streaming contraction: one warp owns RW rows (c, p) at a time; its lanes read 2
+// consecutive complex Q entries each (512 contiguous bytes per warp and row per step) and
+// multiply them with the group's phases, staged in shared memory per chunk of kChunk modes
+// and shared by the CTA's 8 warps.  Lane partial sums are reduced with warp shuffles.
+constexpr int kCtrWarps = 8;
+constexpr int kCtrChunk = 512;
+
+template <int NK, int RW>
+__global__ void __launch_bounds__(kCtrWarps * 32, 2)
 sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict__ Phi,
                     const float2* __restrict__ Q, int MF, int J, float2* __restrict__ C) {
-    __shared__ float2 ph[kPhaseChunk][NK];
+    __shared__ float4 ph[kCtrChunk / 2][NK];    // (phi[j][kk], phi[j+1][kk]) pairs
     const PGroup g = groups[blockIdx.y];
     const int l = g.region - 1;
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = row < 3 * MF;
-    const int c = active ? row / MF : 0;
-    const int p = active ? row % MF : 0;
-    double tot[NK][2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row0 = (blockIdx.x * kCtrWarps + warp) * RW;
+    float acc[RW][NK][2];
 #pragma unroll
-    for (int kk = 0; kk < NK; kk++) tot[kk][0] = tot[kk][1] = 0.0;
-    const float2* Pg = Phi + (long long)blockIdx.y * 2 * J * kMaxGroup;
+    for (int r = 0; r < RW; r++)
+#pragma unroll
+        for (int kk = 0; kk < NK; kk++) acc[r][kk][0] = acc[r][kk][1] = 0.f;
+    const float2* Pg = Phi + (long long)blockIdx.y * 2 * J * NK;
     for (int half = 0; half < 2; half++) {
-        const float2* qrow = Q + ((((long long)l * 2 + half) * 3 + c) * MF + p) * (long long)J;
-        for (int j0 = 0; j0 < J; j0 += kPhaseChunk) {
-            const int nj = min(kPhaseChunk, J - j0);
+        for (int j0 = 0; j0 < J; j0 += kCtrChunk) {
+            const int nj = min(kCtrChunk, J - j0);
             __syncthreads();
-            for (int e = threadIdx.x; e < nj * NK; e += blockDim.x) {
-                const int jj = e / NK, kk = e % NK;
-                ph[jj][kk] = Pg[((long long)half * J + j0 + jj) * kMaxGroup + kk];
+            for (int e = threadIdx.x; e < (nj / 2) * NK; e += blockDim.x) {
+                const int jp = e / NK, kk = e % NK;
+                const float2 a = Pg[((long long)half * J + j0 + 2 * jp) * NK + kk];
+                const float2 b = Pg[((long long)half * J + j0 + 2 * jp + 1) * NK + kk];
+                ph[jp][kk] = make_float4(a.x, a.y, b.x, b.y);
             }
             __syncthreads();
-            if (active) {
-                float acc[NK][2];
 #pragma unroll
-                for (int kk = 0; kk < NK; kk++) acc[kk][0] = acc[kk][1] = 0.f;
-                int jj = 0;
-                for (; jj + 1 < nj; jj += 2) {
-                    const float4 q2 = __ldg(reinterpret_cast<const float4*>(qrow + j0 + jj));
-#pragma unroll
-                    for (int kk = 0; kk < NK; kk++) {
-                        const float2 f0 = ph[jj][kk], f1 = ph[jj + 1][kk];
-                        acc[kk][0] = fmaf(q2.x, f0.x, fmaf(-q2.y, f0.y, acc[kk][0]));
-                        acc[kk][1] = fmaf(q2.x, f0.y, fmaf(q2.y, f0.x, acc[kk][1]));
-                        acc[kk][0] = fmaf(q2.z, f1.x, fmaf(-q2.w, f1.y, acc[kk][0]));
-                        acc[kk][1] = fmaf(q2.z, f1.y, fmaf(q2.w, f1.x, acc[kk][1]));
-                    }
-                }
-                for (; jj < nj; jj++) {
-                    const float2 q = __ldg(qrow + j0 + jj);
+            for (int r = 0; r < RW; r++) {
+                const int row = min(row0 + r, 3 * MF - 1);    // rows past the end repeat the last (not written)
+                const int c = row / MF, p = row % MF;
+                const float4* qrow = reinterpret_cast<const float4*>(
+                    Q + ((((long long)l * 2 + half) * 3 + c) * MF + p) * (long long)J + j0);
+#pragma unroll 4
+                for (int jp = lane; jp < nj / 2; jp += 32) {
+                    const float4 q = __ldcs(qrow + jp);       // streamed once: evict-first
 #pragma unroll
                     for (int kk = 0; kk < NK; kk++) {
-                        const float2 f0 = ph[jj][kk];
-                        acc[kk][0] = fmaf(q.x, f0.x, fmaf(-q.y, f0.y, acc[kk][0]));
-                        acc[kk][1] = fmaf(q.x, f0.y, fmaf(q.y, f0.x, acc[kk][1]));
+                        const float4 f = ph[jp][kk];
+                        acc[r][kk][0] = fmaf(q.x, f.x, fmaf(-q.y, f.y, acc[r][kk][0]));
+                        acc[r][kk][1] = fmaf(q.x, f.y, fmaf(q.y, f.x, acc[r][kk][1]));
+                        acc[r][kk][0] = fmaf(q.z, f.z, fmaf(-q.w, f.w, acc[r][kk][0]));
+                        acc[r][kk][1] = fmaf(q.z, f.w, fmaf(q.w, f.z, acc[r][kk][1]));
                     }
-                }
-#pragma unroll
-                for (int kk = 0; kk < NK; kk++) {
-                    tot[kk][0] += (double)acc[kk][0];
-                    tot[kk][1] += (double)acc[kk][1];
                 }
             }
         }
     }
-    if (!active) return;
 #pragma unroll
-    for (int kk = 0; kk < NK; kk++) {
-        if (kk < g.nk) C[((long long)g.zi[kk] * 3 + c) * MF + p] = make_float2((float)tot[kk][0], (float)tot[kk][1]);
+    for (int r = 0; r < RW; r++) {
+        const int row = row0 + r;
+#pragma unroll
+        for (int kk = 0; kk < NK; kk++) {
+            float vr = acc[r][kk][0], vi = acc[r][kk][1];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, o);
+                vi += __shfl_xor_sync(0xffffffffu, vi, o);
+            }
+            if (lane == 0 && row < 3 * MF && kk < g.nk) {
+                const int c = row / MF, p = row % MF;
+                C[((long long)g.zi[kk] * 3 + c) * MF + p] = make_float2(vr, vi);
+            }
+        }
     }
 }
 
@@ -191,6 +200,47 @@ __global__ void sep_rows_kernel(const float2* __restrict__ C, const float2* __re
         si = fmaf(rv.x, cv.y, fmaf(rv.y, cv.x, si));
     }
     T[idx] = make_float2(sr, si);
+}
+
+// Stage 2a for a volume: T[k*Ny + j][c][a] = sum_b Ey[b][j] C[k][c][a*M1 + b].
+// One CTA per (z-plane k, block of kRowsBlk rows j): C[k] is staged transposed ([c][b][a],
+// so lanes with consecutive a read consecutive words) with the block's Ey phases.
+constexpr int kRowsBlk = 64;
+
+__global__ void __launch_bounds__(256)
+sep_rows_volume_kernel(const float2* __restrict__ C, const float2* __restrict__ tabY, int Ny, int M0, int M1,
+                       float2* __restrict__ T) {
+    extern __shared__ float2 sm2[];
+    float2* sC = sm2;                              // [3][M1][M0]
+    float2* sR = sm2 + 3 * M0 * M1;                // [kRowsBlk][M1]
+    const int k = blockIdx.y;
+    const int j0 = blockIdx.x * kRowsBlk;
+    const int MF = M0 * M1;
+    const float2* Ck = C + (long long)k * 3 * MF;
+    for (int e = threadIdx.x; e < 3 * MF; e += blockDim.x) {
+        const int c = e / MF, p = e % MF, a = p / M1, b = p % M1;
+        sC[(c * M1 + b) * M0 + a] = Ck[e];
+    }
+    for (int e = threadIdx.x; e < kRowsBlk * M1; e += blockDim.x) {
+        const int r = e / M1, b = e % M1;
+        sR[e] = (j0 + r < Ny) ? tabY[(long long)b * Ny + j0 + r] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int ncol = 3 * M0;
+    for (int e = threadIdx.x; e < kRowsBlk * ncol; e += blockDim.x) {
+        const int r = e / ncol, col = e % ncol;
+        if (j0 + r >= Ny) continue;
+        const int c = col / M0, a = col % M0;
+        const float2* cp = sC + c * M1 * M0 + a;
+        const float2* rp = sR + r * M1;
+        float sr = 0.f, si = 0.f;
+        for (int b = 0; b < M1; b++) {
+            const float2 rv = rp[b], cv = cp[b * M0];
+            sr = fmaf(rv.x, cv.x, fmaf(-rv.y, cv.y, sr));
+            si = fmaf(rv.x, cv.y, fmaf(rv.y, cv.x, si));
+        }
+        T[(((long long)k * Ny + j0 + r) * 3 + c) * M0 + a] = make_float2(sr, si);
+    }
 }
 
 // Stage 2b (FP32 SIMT): E[r][col][c] = sum_m T[r][c][m] * F[m][col]
@@ -281,7 +331,7 @@ static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 // Stage 1 for a list of z-values: fills C [nz][3][MF] in the context's scratch.
 static scw_status stage1(scw_sep s, const std::vector<float>& zlist, float2* dC, char*& cursor) {
     scw_ctx ctx = s->ctx;
-    const int MF = s->MF, J = s->J;
+    const int MF = s->MF, J = s->Jp;          // device row stride (even)
     std::vector<PGroup> groups;
     std::vector<int2> ext;
     std::map<int64_t, std::vector<int>> by_region;
@@ -323,25 +373,26 @@ static scw_status stage1(scw_sep s, const std::vector<float>& zlist, float2* dC,
 
     if (!groups.empty()) {
         if (J > 0) {
+            const int nks = max_nk <= 1 ? 1 : max_nk <= 2 ? 2 : max_nk <= 4 ? 4 : 8;
             float2* dPhi = (float2*)cursor;
-            cursor += align256(groups.size() * 2 * (size_t)J * kMaxGroup * sizeof(float2));
+            cursor += align256(groups.size() * 2 * (size_t)J * nks * sizeof(float2));
             dim3 gp((2 * J + 255) / 256, (unsigned)groups.size());
             {
                 LaunchTimer lt(ctx, "sep_phase_kernel");
-                sep_phase_kernel<<<gp, 256, 0, ctx->stream>>>(dg, dz, s->dKz, s->dzb, J, dPhi);
+                sep_phase_kernel<<<gp, 256, 0, ctx->stream>>>(dg, dz, s->dKz, s->dzb, J, nks, dPhi);
             }
             SCW_CUDA_TRY(cudaGetLastError());
             ctx->launches++;
-            dim3 gc((3 * MF + 127) / 128, (unsigned)groups.size());
+            auto grid_for = [&](int rw) { return dim3((3 * MF + kCtrWarps * rw - 1) / (kCtrWarps * rw), (unsigned)groups.size()); };
             LaunchTimer lt(ctx, "sep_contract_kernel");
-            if (max_nk <= 1)
-                sep_contract_kernel<1><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
-            else if (max_nk <= 2)
-                sep_contract_kernel<2><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
-            else if (max_nk <= 4)
-                sep_contract_kernel<4><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+            if (nks == 1)
+                sep_contract_kernel<1, 8><<<grid_for(8), kCtrWarps * 32, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+            else if (nks == 2)
+                sep_contract_kernel<2, 8><<<grid_for(8), kCtrWarps * 32, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+            else if (nks == 4)
+                sep_contract_kernel<4, 4><<<grid_for(4), kCtrWarps * 32, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
             else
-                sep_contract_kernel<8><<<gc, 128, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+                sep_contract_kernel<8, 2><<<grid_for(2), kCtrWarps * 32, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
             SCW_CUDA_TRY(cudaGetLastError());
             ctx->launches++;
         } else {
@@ -426,7 +477,7 @@ scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, 
     else if (kind == 1) { nrows = Nb; ncols = Na; Mk = M0; }
     else { nrows = Nb; ncols = Na; Mk = M1; }
     // phases for the PGroups: at most nz groups
-    const size_t phi_bytes = align256((size_t)nz * 2 * (size_t)s->J * kMaxGroup * sizeof(float2));
+    const size_t phi_bytes = align256((size_t)nz * 2 * (size_t)s->Jp * kMaxGroup * sizeof(float2));
     const size_t c_bytes = align256((size_t)nz * 3 * MF * sizeof(float2));
     const size_t t_bytes = align256((size_t)nrows * 3 * Mk * sizeof(float2) + 4096);
     const size_t tab_bytes = align256((size_t)(M0 + M1) * (Na + Nb + 2) * sizeof(float2));
@@ -447,7 +498,17 @@ scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, 
         // F = Ex table [a][x]; R = Ey table [b][y]
         if ((st = launch_table(ctx, s->dkx, M0, a0, da, Na, tabA)) != SCW_OK) return st;
         if ((st = launch_table(ctx, s->dky, M1, b0, db, Nb, tabB)) != SCW_OK) return st;
-        if ((st = launch_rows(ctx, dC, tabB, Nb, Nb, Nb, 0, nrows, 0, M0, M1, dT)) != SCW_OK) return st;
+        {
+            const size_t smem = (size_t)(3 * M0 * M1 + kRowsBlk * M1) * sizeof(float2);
+            if (smem > 200 * 1024) return fail(SCW_ERR_UNSUPPORTED, "harmonic grid too large for the row stage");
+            SCW_CUDA_TRY(cudaFuncSetAttribute(sep_rows_volume_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+            dim3 grid((Nb + kRowsBlk - 1) / kRowsBlk, Nz);
+            LaunchTimer lt(ctx, "sep_rows_volume_kernel");
+            sep_rows_volume_kernel<<<grid, 256, smem, ctx->stream>>>(dC, tabB, Nb, M0, M1, dT);
+            SCW_CUDA_TRY(cudaGetLastError());
+            ctx->launches++;
+        }
         return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, method);
     } else if (kind == 1) {
         // xz plane at y = c: R = Ey(c) [b]; F = Ex table [a][x]
@@ -499,17 +560,18 @@ scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_p
     s->MF = M0 * M1;
     s->Z = n_slices;
     s->J = modes_per_half;
+    s->Jp = modes_per_half + (modes_per_half & 1);
     s->kx.assign(kx, kx + M0);
     s->ky.assign(ky, ky + M1);
     s->zb.assign(z_boundaries, z_boundaries + n_slices + 1);
     s->z_layers.resize(n_slices + 1);
     for (int l = 0; l <= n_slices; l++) s->z_layers[l] = (float)z_boundaries[l];
-    const size_t nQ = (size_t)n_slices * 2 * 3 * s->MF * (size_t)s->J;
+    const size_t nQ = (size_t)n_slices * 2 * 3 * s->MF * (size_t)s->Jp;
     bool ok = cudaMalloc(&s->dkx, M0 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&s->dky, M1 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&s->dzb, (n_slices + 1) * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&s->dExt, 12 * (size_t)s->MF * sizeof(double2)) == cudaSuccess &&
-              cudaMalloc(&s->dKz, ((size_t)n_slices * 2 * s->J + 1) * sizeof(double2)) == cudaSuccess;
+              cudaMalloc(&s->dKz, ((size_t)n_slices * 2 * s->Jp + 1) * sizeof(double2)) == cudaSuccess;
     if (ok && nQ) {
         ok = cudaMalloc(&s->dQ, nQ * sizeof(float2)) == cudaSuccess;
         s->own_Q = true;
@@ -523,7 +585,7 @@ scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_p
     cudaMemcpy(s->dzb, z_boundaries, (n_slices + 1) * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemset(s->dExt, 0, 12 * (size_t)s->MF * sizeof(double2));
     if (nQ) cudaMemset(s->dQ, 0, nQ * sizeof(float2));
-    cudaMemset(s->dKz, 0, ((size_t)n_slices * 2 * s->J + 1) * sizeof(double2));
+    cudaMemset(s->dKz, 0, ((size_t)n_slices * 2 * s->Jp + 1) * sizeof(double2));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         sep_free(s);
@@ -555,6 +617,35 @@ scw_status scw_sep_set_exterior(scw_sep s, const double* inc, const double* kz_i
     return SCW_OK;
 }
 
+static scw_status upload_kz(scw_sep s, int l, const double* kz_dn, const double* kz_up) {
+    const size_t J = (size_t)s->J, Jp = (size_t)s->Jp;
+    std::vector<double> kz(4 * Jp, 0.0);
+    std::memcpy(kz.data(), kz_dn, 2 * J * 8);
+    std::memcpy(kz.data() + 2 * Jp, kz_up, 2 * J * 8);
+    SCW_CUDA_TRY(cudaMemcpy(s->dKz + (size_t)l * 2 * Jp, kz.data(), 4 * Jp * 8, cudaMemcpyHostToDevice));
+    return SCW_OK;
+}
+
+// copies a [3][MF][J] complex64 block into the [3][MF][Jp] device slot (pitched when J is odd)
+static scw_status upload_q(scw_sep s, int l, int half, const void* src, cudaMemcpyKind kind, bool async) {
+    const size_t J = (size_t)s->J, Jp = (size_t)s->Jp, MF = (size_t)s->MF;
+    float2* dst = s->dQ + ((size_t)l * 2 + half) * 3 * MF * Jp;
+    if (J == Jp) {
+        if (async)
+            SCW_CUDA_TRY(cudaMemcpyAsync(dst, src, 3 * MF * J * sizeof(float2), kind, s->ctx->stream));
+        else
+            SCW_CUDA_TRY(cudaMemcpy(dst, src, 3 * MF * J * sizeof(float2), kind));
+    } else {
+        if (async)
+            SCW_CUDA_TRY(cudaMemcpy2DAsync(dst, Jp * sizeof(float2), src, J * sizeof(float2), J * sizeof(float2),
+                                           3 * MF, kind, s->ctx->stream));
+        else
+            SCW_CUDA_TRY(cudaMemcpy2D(dst, Jp * sizeof(float2), src, J * sizeof(float2), J * sizeof(float2), 3 * MF,
+                                      kind));
+    }
+    return SCW_OK;
+}
+
 scw_status scw_sep_set_slice(scw_sep s, int l, const double* kz_dn, const double* Q_dn, const double* kz_up,
                              const double* Q_up) {
     if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_sep_set_slice: slice out of range");
@@ -562,16 +653,13 @@ scw_status scw_sep_set_slice(scw_sep s, int l, const double* kz_dn, const double
     if (J == 0) return SCW_OK;
     if (!kz_dn || !Q_dn || !kz_up || !Q_up) return fail(SCW_ERR_ARG, "scw_sep_set_slice: null argument");
     SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
-    std::vector<double> kz(4 * J);
-    std::memcpy(kz.data(), kz_dn, 2 * J * 8);
-    std::memcpy(kz.data() + 2 * J, kz_up, 2 * J * 8);
-    SCW_CUDA_TRY(cudaMemcpy(s->dKz + (size_t)l * 2 * J, kz.data(), 4 * J * 8, cudaMemcpyHostToDevice));
+    scw_status st = upload_kz(s, l, kz_dn, kz_up);
+    if (st != SCW_OK) return st;
     std::vector<float2> q(3 * MF * J);
     for (int half = 0; half < 2; half++) {
         const double* src = half == 0 ? Q_dn : Q_up;
         for (size_t i = 0; i < 3 * MF * J; i++) q[i] = make_float2((float)src[2 * i], (float)src[2 * i + 1]);
-        SCW_CUDA_TRY(cudaMemcpy(s->dQ + ((size_t)l * 2 + half) * 3 * MF * J, q.data(), q.size() * sizeof(float2),
-                                cudaMemcpyHostToDevice));
+        if ((st = upload_q(s, l, half, q.data(), cudaMemcpyHostToDevice, false)) != SCW_OK) return st;
     }
     return SCW_OK;
 }
@@ -579,19 +667,13 @@ scw_status scw_sep_set_slice(scw_sep s, int l, const double* kz_dn, const double
 scw_status scw_sep_set_slice_device(scw_sep s, int l, const double* kz_dn, const void* Q_dn_c64, const double* kz_up,
                                     const void* Q_up_c64) {
     if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_sep_set_slice_device: slice out of range");
-    const size_t J = (size_t)s->J, MF = (size_t)s->MF;
-    if (J == 0) return SCW_OK;
+    if (s->J == 0) return SCW_OK;
+    if (!kz_dn || !Q_dn_c64 || !kz_up || !Q_up_c64) return fail(SCW_ERR_ARG, "scw_sep_set_slice_device: null argument");
     SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
-    std::vector<double> kz(4 * J);
-    std::memcpy(kz.data(), kz_dn, 2 * J * 8);
-    std::memcpy(kz.data() + 2 * J, kz_up, 2 * J * 8);
-    SCW_CUDA_TRY(cudaMemcpy(s->dKz + (size_t)l * 2 * J, kz.data(), 4 * J * 8, cudaMemcpyHostToDevice));
-    const size_t blk = 3 * MF * J * sizeof(float2);
-    SCW_CUDA_TRY(cudaMemcpyAsync(s->dQ + ((size_t)l * 2 + 0) * 3 * MF * J, Q_dn_c64, blk, cudaMemcpyDefault,
-                                 s->ctx->stream));
-    SCW_CUDA_TRY(cudaMemcpyAsync(s->dQ + ((size_t)l * 2 + 1) * 3 * MF * J, Q_up_c64, blk, cudaMemcpyDefault,
-                                 s->ctx->stream));
-    return SCW_OK;
+    scw_status st = upload_kz(s, l, kz_dn, kz_up);
+    if (st != SCW_OK) return st;
+    if ((st = upload_q(s, l, 0, Q_dn_c64, cudaMemcpyDefault, true)) != SCW_OK) return st;
+    return upload_q(s, l, 1, Q_up_c64, cudaMemcpyDefault, true);
 }
 
 scw_status scw_sep_set_region_rule(scw_sep s, int rule) {

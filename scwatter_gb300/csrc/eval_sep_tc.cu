@@ -16,11 +16,13 @@
 // lo = tf32(x - hi); BF16: bf16 hi, bf16 lo) and D = Ahi.Bhi + Ahi.Blo + Alo.Bhi, FP32
 // accumulation in TMEM.
 //
-// Pipeline (one CTA per SM, 128 threads, persistent over row tiles of one 128-column x tile):
-// A (hi, lo) is built once in shared memory; per row tile all threads build B (hi, lo) in one
-// of two shared buffers, thread 0 issues the MMAs into one of two TMEM accumulators and
-// commits them to an mbarrier, and the epilogue of the previous tile (all 4 warps, one TMEM
-// lane quarter each) runs while the tensor cores work.  Operands use the SWIZZLE_NONE
+// Pipeline (one CTA per SM, persistent over the row tiles of one 128-column x tile), warp
+// specialised with mbarrier hand-offs:
+//   warps 0-3  epilogue: TMEM lane quarter w -> registers -> global (accumulator full/empty)
+//   warps 4-7  producers: build B (hi, lo) of the next tile into one of two shared buffers,
+//              writing whole 16-byte core rows in address order (no bank conflicts)
+//   warp 8     one thread issues the MMAs into one of two TMEM accumulators and commits them
+// A (hi, lo) is built once by all warps before the roles split.  Operands use the SWIZZLE_NONE
 // K-major canonical layout: 8-row x 16-byte core matrices stored contiguously, LBO = 128 B
 // between core matrices along K, SBO = (K bytes / 16) * 128 B between 8-row groups.
 // Every mbarrier wait is bounded; on timeout the kernel records an error, waits (bounded)
@@ -38,7 +40,6 @@ namespace tc {
 constexpr int kM = 128;          // x-values per tile (TMEM lanes)
 constexpr int kRows = 16;        // output rows per tile
 constexpr int kN = kRows * 6;    // 96 accumulator columns per tile
-constexpr int kThreads = 128;
 constexpr uint32_t kTmemCols = 512;     // two 96-column accumulators at columns 0 and 128; whole TMEM (1 CTA / SM)
 constexpr long long kSpinLimit = 1ll << 22;   // polls per mbarrier wait before giving up
 
@@ -161,159 +162,210 @@ struct Split<1> {           // bf16
     }
 };
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 template <int kKind>
-__global__ void __launch_bounds__(kThreads, 1)
+__device__ __forceinline__ uint4 pack4(const typename Split<kKind>::T* v);
+
+template <>
+__device__ __forceinline__ uint4 pack4<0>(const float* v) {        // 4 tf32 values
+    return make_uint4(__float_as_uint(v[0]), __float_as_uint(v[1]), __float_as_uint(v[2]), __float_as_uint(v[3]));
+}
+
+template <>
+__device__ __forceinline__ uint4 pack4<1>(const __nv_bfloat16* v) { // 8 bf16 values
+    uint4 r;
+    r.x = (uint32_t)__bfloat16_as_ushort(v[0]) | ((uint32_t)__bfloat16_as_ushort(v[1]) << 16);
+    r.y = (uint32_t)__bfloat16_as_ushort(v[2]) | ((uint32_t)__bfloat16_as_ushort(v[3]) << 16);
+    r.z = (uint32_t)__bfloat16_as_ushort(v[4]) | ((uint32_t)__bfloat16_as_ushort(v[5]) << 16);
+    r.w = (uint32_t)__bfloat16_as_ushort(v[6]) | ((uint32_t)__bfloat16_as_ushort(v[7]) << 16);
+    return r;
+}
+
+constexpr int kEpiWarps = 4, kProdWarps = 4;
+constexpr int kWsThreads = (kEpiWarps + kProdWarps + 1) * 32;
+
+template <int kKind>
+__global__ void __launch_bounds__(kWsThreads, 1)
 synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int nrows, int ncols, int Mk, int Kp,
                 float* __restrict__ out, int* __restrict__ err) {
     using E = typename Split<kKind>::T;
     constexpr int EB = Split<kKind>::kBytes;
+    constexpr int EPC = 16 / EB;                              // elements per 16-byte core row
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t kbytes = (uint32_t)Kp * EB;              // bytes of K per row
-    const uint32_t sbo = (kbytes / 16) * 128;               // 8-row group stride
+    const uint32_t kbytes = (uint32_t)Kp * EB;
+    const int KC = (int)(kbytes / 16);                        // 16-byte core columns along K
+    const uint32_t sbo = (uint32_t)KC * 128;
     const uint32_t a_bytes = (kM / 8) * sbo;
     const uint32_t b_bytes = (kN / 8) * sbo;
     unsigned char* sA_hi = smem;
     unsigned char* sA_lo = sA_hi + a_bytes;
-    unsigned char* sB[2][2] = {{sA_lo + a_bytes, sA_lo + a_bytes + b_bytes},
-                               {sA_lo + a_bytes + 2 * b_bytes, sA_lo + a_bytes + 3 * b_bytes}};   // [slot][hi/lo]
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(sA_lo + a_bytes + 4 * b_bytes);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
+    unsigned char* sB0 = sA_lo + a_bytes;                     // slot s, part h: sB0 + (2 s + h) b_bytes
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sB0 + 4 * b_bytes);
+    uint64_t* full_b = bar;          // [2] producers -> MMA
+    uint64_t* empty_b = bar + 2;     // [2] MMA completion -> producers
+    uint64_t* acc_full = bar + 4;    // [2] MMA completion -> epilogue
+    uint64_t* acc_empty = bar + 6;   // [2] epilogue -> MMA
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 8);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(bar + 9);
 
     const int x0 = blockIdx.x * kM;
     const int ntiles = (nrows + kRows - 1) / kRows;
+    const int n_my = blockIdx.y < ntiles ? (ntiles - 1 - (int)blockIdx.y) / (int)gridDim.y + 1 : 0;
 
-    // zero all operand memory (covers the K padding and out-of-range rows / columns)
-    for (uint32_t o = tid * 16; o < 2 * a_bytes + 4 * b_bytes; o += kThreads * 16)
+    for (uint32_t o = tid * 16; o < 2 * a_bytes + 4 * b_bytes; o += kWsThreads * 16)
         *reinterpret_cast<uint4*>(smem + o) = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        for (int i = 0; i < 2; i++) {
+            mbar_init(&full_b[i], kProdWarps * 32);     // every producer thread arrives after its fence
+            mbar_init(&empty_b[i], 1);
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], kEpiWarps * 32);   // every epilogue thread arrives after its TMEM reads
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
         tmem_alloc(tmem_slot, kTmemCols);
         tmem_relinquish();
     }
+    __syncthreads();
+    // A: the phase table of this x tile, written as whole core rows
+    for (int g = tid; g < kM * KC; g += kWsThreads) {
+        const int x = g & 7 | ((g / (8 * KC)) << 3);         // g = ((x / 8) * KC + kc) * 8 + x % 8
+        const int kc = (g >> 3) % KC;
+        const int xg = x0 + x;
+        E hi[EPC], lo[EPC];
+#pragma unroll
+        for (int e = 0; e < EPC; e++) {
+            const int k = kc * EPC + e;
+            float v = 0.f;
+            if (xg < ncols && k < 2 * Mk) {
+                const float2 f = F[(long long)(k < Mk ? k : k - Mk) * ncols + xg];
+                v = k < Mk ? f.x : f.y;
+            }
+            Split<kKind>::split(v, hi[e], lo[e]);
+        }
+        *reinterpret_cast<uint4*>(sA_hi + (uint32_t)g * 16) = pack4<kKind>(hi);
+        *reinterpret_cast<uint4*>(sA_lo + (uint32_t)g * 16) = pack4<kKind>(lo);
+    }
+    fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    // A: the phase table of this x tile
-    for (int e = tid; e < kM * Mk; e += kThreads) {
-        const int x = e / Mk, m = e % Mk;
-        const int xg = x0 + x;
-        const float2 f = xg < ncols ? F[(long long)m * ncols + xg] : make_float2(0.f, 0.f);
-        E rh, rl, ih, il;
-        Split<kKind>::split(f.x, rh, rl);
-        Split<kKind>::split(f.y, ih, il);
-        *reinterpret_cast<E*>(sA_hi + core_offset(x, m * EB, sbo)) = rh;
-        *reinterpret_cast<E*>(sA_lo + core_offset(x, m * EB, sbo)) = rl;
-        *reinterpret_cast<E*>(sA_hi + core_offset(x, (Mk + m) * EB, sbo)) = ih;
-        *reinterpret_cast<E*>(sA_lo + core_offset(x, (Mk + m) * EB, sbo)) = il;
-    }
-
-    // instruction descriptor: D f32, A/B tf32 (2) or bf16 (1), both K-major, N = 96, M = 128
-    const uint32_t ab_fmt = kKind == 0 ? 2u : 1u;
-    const uint32_t idesc = (1u << 4) | (ab_fmt << 7) | (ab_fmt << 10) | ((uint32_t)(kN >> 3) << 17) |
-                           ((uint32_t)(kM >> 4) << 24);
-    const int kstep_bytes = 32;                               // K per MMA instruction: 32 bytes
-    const int nksteps = (int)(kbytes / kstep_bytes);
-    bool ok = true;              // CTA-uniform between the barriers of the tile loop
-    int issued = 0;              // MMA groups committed (group i: slot i & 1, parity (i >> 1) & 1)
-    int waited = 0;              // MMA groups awaited
-
-    // epilogue of the tile whose MMA group index is `grp`
-    auto epilogue = [&](int tile, int grp) {
-        const int slot = grp & 1;
-        bool got = mbar_wait(&mbar[slot], (uint32_t)((grp >> 1) & 1));
-        got = __all_sync(0xffffffffu, got);
-        waited = grp + 1;
-        tc_fence_after();
-        if (!got) {
-            ok = false;
-            return;
-        }
-        const int r0 = tile * kRows;
-        const int xg = x0 + warp * 32 + lane;
-        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(slot * 128);
-        uint32_t v[32];
-#pragma unroll 1
-        for (int q = 0; q < kN / 32; q++) {
-            tmem_ld32(tbase + (uint32_t)(q * 32), v);
-            tmem_ld_wait();
-#pragma unroll
-            for (int cc = 0; cc < 32; cc += 2) {
-                const int col = q * 32 + cc;          // even column: (row r, component c, re); odd: im
-                const int r = col / 6, w = col % 6;
+    if (warp >= kEpiWarps && warp < kEpiWarps + kProdWarps) {
+        // ---------------- producers ----------------
+        const int pt = tid - kEpiWarps * 32;                  // 0 .. 127
+        for (int i = 0; i < n_my; i++) {
+            if (*abort_flag) break;
+            const int s = i & 1;
+            if (i >= 2 && !mbar_wait(&empty_b[s], (uint32_t)(((i >> 1) - 1) & 1))) {
+                *abort_flag = 1;
+                break;
+            }
+            const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
+            unsigned char* bh = sB0 + (2 * s + 0) * b_bytes;
+            unsigned char* bl = sB0 + (2 * s + 1) * b_bytes;
+            for (int g = pt; g < kN * KC; g += kProdWarps * 32) {
+                const int n = g & 7 | ((g / (8 * KC)) << 3);
+                const int kc = (g >> 3) % KC;
+                const int r = n / 6, c = (n % 6) >> 1, sri = n & 1;
                 const int row = r0 + r;
-                if (xg < ncols && row < nrows) {
-                    const float2 val = make_float2(__uint_as_float(v[cc]), __uint_as_float(v[cc + 1]));
-                    *reinterpret_cast<float2*>(out + ((long long)row * ncols + xg) * 6 + w) = val;
+                E hi[EPC], lo[EPC];
+#pragma unroll
+                for (int e = 0; e < EPC; e++) {
+                    const int k = kc * EPC + e;
+                    float v = 0.f;
+                    if (row < nrows && k < 2 * Mk) {
+                        const int m = k < Mk ? k : k - Mk;
+                        const float2 t = T[((long long)row * 3 + c) * Mk + m];
+                        // s = 0 (Re E): [Re T | -Im T];  s = 1 (Im E): [Im T | Re T]
+                        v = sri == 0 ? (k < Mk ? t.x : -t.y) : (k < Mk ? t.y : t.x);
+                    }
+                    Split<kKind>::split(v, hi[e], lo[e]);
+                }
+                *reinterpret_cast<uint4*>(bh + (uint32_t)g * 16) = pack4<kKind>(hi);
+                *reinterpret_cast<uint4*>(bl + (uint32_t)g * 16) = pack4<kKind>(lo);
+            }
+            fence_proxy_async();
+            mbar_arrive(&full_b[s]);
+        }
+    } else if (warp == kEpiWarps + kProdWarps) {
+        // ---------------- MMA issuer ----------------
+        const uint32_t ab_fmt = kKind == 0 ? 2u : 1u;
+        const uint32_t idesc = (1u << 4) | (ab_fmt << 7) | (ab_fmt << 10) | ((uint32_t)(kN >> 3) << 17) |
+                               ((uint32_t)(kM >> 4) << 24);
+        const int nksteps = (int)(kbytes / 32);
+        int issued = 0;
+        if (lane == 0) {
+            for (int i = 0; i < n_my; i++) {
+                if (*abort_flag) break;
+                const int s = i & 1;
+                if (!mbar_wait(&full_b[s], (uint32_t)((i >> 1) & 1)) ||
+                    (i >= 2 && !mbar_wait(&acc_empty[s], (uint32_t)(((i >> 1) - 1) & 1)))) {
+                    *abort_flag = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(s * 128);
+                const uint32_t a_hi = smem_u32(sA_hi), a_lo = smem_u32(sA_lo);
+                const uint32_t b_hi = smem_u32(sB0 + (2 * s) * b_bytes), b_lo = smem_u32(sB0 + (2 * s + 1) * b_bytes);
+                for (int ks = 0; ks < nksteps; ks++) {
+                    const uint32_t ko = (uint32_t)ks * 256u;    // 32 bytes of K = two 16-byte core columns
+                    umma<kKind>(d, make_desc(a_hi + ko, 128, sbo), make_desc(b_hi + ko, 128, sbo), idesc, ks > 0);
+                    umma<kKind>(d, make_desc(a_hi + ko, 128, sbo), make_desc(b_lo + ko, 128, sbo), idesc, 1);
+                    umma<kKind>(d, make_desc(a_lo + ko, 128, sbo), make_desc(b_hi + ko, 128, sbo), idesc, 1);
+                }
+                umma_commit(&empty_b[s]);
+                umma_commit(&acc_full[s]);
+                issued = i + 1;
+            }
+            // the accumulators must be idle before TMEM is freed: wait for the last commit
+            if (issued > 0) mbar_wait(&acc_full[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1));
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue (warps 0-3, TMEM lanes 32 w .. 32 w + 31) ----------------
+        const int xg = x0 + warp * 32 + lane;
+        for (int i = 0; i < n_my; i++) {
+            if (*abort_flag) break;
+            const int a = i & 1;
+            bool got = mbar_wait(&acc_full[a], (uint32_t)((i >> 1) & 1));
+            got = __all_sync(0xffffffffu, got);
+            if (!got) {
+                *abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
+            const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * 128);
+            uint32_t v[32];
+#pragma unroll 1
+            for (int q = 0; q < kN / 32; q++) {
+                tmem_ld32(tbase + (uint32_t)(q * 32), v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int cc = 0; cc < 32; cc += 2) {
+                    const int col = q * 32 + cc;               // even column: (row r, component c, re); odd: im
+                    const int r = col / 6, w = col % 6;
+                    const int row = r0 + r;
+                    if (xg < ncols && row < nrows) {
+                        const float2 val = make_float2(__uint_as_float(v[cc]), __uint_as_float(v[cc + 1]));
+                        *reinterpret_cast<float2*>(out + ((long long)row * ncols + xg) * 6 + w) = val;
+                    }
                 }
             }
+            tc_fence_before();
+            mbar_arrive(&acc_empty[a]);
         }
-        tc_fence_before();
-    };
-
-    int prev_tile = -1;
-    for (int tile = blockIdx.y; tile < ntiles; tile += gridDim.y) {
-        if (!ok) break;
-        const int s = issued & 1;
-        // B for this tile into buffer s (the MMA group that last read it was awaited by the
-        // previous epilogue)
-        const int r0 = tile * kRows;
-        for (int e = tid; e < kRows * 3 * Mk; e += kThreads) {
-            const int r = e / (3 * Mk);
-            const int rem = e % (3 * Mk);
-            const int c = rem / Mk, m = rem % Mk;
-            const int row = r0 + r;
-            const float2 tv = row < nrows ? T[((long long)row * 3 + c) * Mk + m] : make_float2(0.f, 0.f);
-            E reh, rel, imh, iml, nimh, niml;
-            Split<kKind>::split(tv.x, reh, rel);
-            Split<kKind>::split(tv.y, imh, iml);
-            Split<kKind>::split(-tv.y, nimh, niml);
-            const int n_re = r * 6 + c * 2, n_im = n_re + 1;
-            unsigned char* bh = sB[s][0];
-            unsigned char* bl = sB[s][1];
-            *reinterpret_cast<E*>(bh + core_offset(n_re, m * EB, sbo)) = reh;
-            *reinterpret_cast<E*>(bl + core_offset(n_re, m * EB, sbo)) = rel;
-            *reinterpret_cast<E*>(bh + core_offset(n_re, (Mk + m) * EB, sbo)) = nimh;
-            *reinterpret_cast<E*>(bl + core_offset(n_re, (Mk + m) * EB, sbo)) = niml;
-            *reinterpret_cast<E*>(bh + core_offset(n_im, m * EB, sbo)) = imh;
-            *reinterpret_cast<E*>(bl + core_offset(n_im, m * EB, sbo)) = iml;
-            *reinterpret_cast<E*>(bh + core_offset(n_im, (Mk + m) * EB, sbo)) = reh;
-            *reinterpret_cast<E*>(bl + core_offset(n_im, (Mk + m) * EB, sbo)) = rel;
-        }
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            tc_fence_after();
-            const uint32_t d = tmem + (uint32_t)(s * 128);
-            const uint32_t a_hi = smem_u32(sA_hi), a_lo = smem_u32(sA_lo);
-            const uint32_t b_hi = smem_u32(sB[s][0]), b_lo = smem_u32(sB[s][1]);
-            for (int ks = 0; ks < nksteps; ks++) {
-                const uint32_t ko = (uint32_t)ks * 256u;    // 32 bytes of K = two 16-byte core columns
-                umma<kKind>(d, make_desc(a_hi + ko, 128, sbo), make_desc(b_hi + ko, 128, sbo), idesc, ks > 0);
-                umma<kKind>(d, make_desc(a_hi + ko, 128, sbo), make_desc(b_lo + ko, 128, sbo), idesc, 1);
-                umma<kKind>(d, make_desc(a_lo + ko, 128, sbo), make_desc(b_hi + ko, 128, sbo), idesc, 1);
-            }
-            umma_commit(&mbar[s]);
-        }
-        issued++;
-        if (prev_tile >= 0) epilogue(prev_tile, issued - 2);
-        ok = __syncthreads_and(ok) != 0;
-        prev_tile = tile;
     }
-    if (prev_tile >= 0 && ok) epilogue(prev_tile, issued - 1);
-    ok = __syncthreads_and(ok) != 0;
-    if (!ok) {
-        if (tid == 0) atomicExch(err, 1);
-        // drain: wait (bounded) for every committed MMA group before freeing TMEM
-        for (int g = waited; g < issued; g++) mbar_wait(&mbar[g & 1], (uint32_t)((g >> 1) & 1));
-    }
-    tc_fence_before();
     __syncthreads();
+    if (tid == 0 && *abort_flag) atomicExch(err, 1);
     if (warp == 0) {
         tc_fence_after();
         tmem_dealloc(tmem, kTmemCols);
@@ -329,7 +381,7 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int kalign = kind == 0 ? 8 : 16;                  // K per MMA instruction
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
-    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + 64;
+    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + 128;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     if (!ctx->tc_err) {
         if (cudaMalloc(&ctx->tc_err, sizeof(int)) != cudaSuccess) return fail(SCW_ERR_NOMEM, "cudaMalloc error flag");
@@ -343,10 +395,10 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     LaunchTimer lt(ctx, kind == 0 ? "synth_tc_kernel<tf32x3>" : "synth_tc_kernel<bf16x3>");
     if (kind == 0) {
         SCW_CUDA_TRY(cudaFuncSetAttribute(tc::synth_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        tc::synth_tc_kernel<0><<<grid, tc::kThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, out, ctx->tc_err);
+        tc::synth_tc_kernel<0><<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, out, ctx->tc_err);
     } else {
         SCW_CUDA_TRY(cudaFuncSetAttribute(tc::synth_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        tc::synth_tc_kernel<1><<<grid, tc::kThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, out, ctx->tc_err);
+        tc::synth_tc_kernel<1><<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, out, ctx->tc_err);
     }
     SCW_CUDA_TRY(cudaGetLastError());
     ctx->launches++;

@@ -29,6 +29,7 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
 struct scw_sep_s {
     scw_ctx ctx = nullptr;
     int M0 = 0, M1 = 0, MF = 0, Z = 0, J = 0;
+    int Jp = 0;                            // J rounded up to even: row stride of Q / kz on the device (zero padded)
     int rule = 0;
     std::vector<double> kx, ky, zb;
     std::vector<float> z_layers;           // Z + 1 boundaries as float (region rule)
@@ -36,7 +37,7 @@ struct scw_sep_s {
     double* dky = nullptr;
     double* dzb = nullptr;
     double2* dExt = nullptr;               // inc[3][MF], refl[3][MF], trans[3][MF], kz_inc, kz_refl, kz_trans
-    double2* dKz = nullptr;                // [Z][2][J] kz of the downward / upward modes
-    float2* dQ = nullptr;                  // [Z][2][3][MF][J] amplitudes at the modes' reference planes
+    double2* dKz = nullptr;                // [Z][2][Jp] kz of the downward / upward modes
+    float2* dQ = nullptr;                  // [Z][2][3][MF][Jp] amplitudes at the modes' reference planes
     bool own_Q = false;
 };

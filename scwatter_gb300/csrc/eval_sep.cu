@@ -83,6 +83,13 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
         for (int kk = 0; kk < NK; kk++) acc[r][kk][0] = acc[r][kk][1] = 0.f;
     const float2* Pg = Phi + (long long)blockIdx.y * 2 * J * NK;
     for (int half = 0; half < 2; half++) {
+        const float4* qrow[RW];
+#pragma unroll
+        for (int r = 0; r < RW; r++) {
+            const int row = min(row0 + r, 3 * MF - 1);    // rows past the end repeat the last (not written)
+            const int c = row / MF, p = row % MF;
+            qrow[r] = reinterpret_cast<const float4*>(Q + ((((long long)l * 2 + half) * 3 + c) * MF + p) * (long long)J);
+        }
         for (int j0 = 0; j0 < J; j0 += kCtrChunk) {
             const int nj = min(kCtrChunk, J - j0);
             __syncthreads();
@@ -93,22 +100,23 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
                 ph[jp][kk] = make_float4(a.x, a.y, b.x, b.y);
             }
             __syncthreads();
+            // each lane keeps one phase pair in registers and applies it to the warp's RW rows
+#pragma unroll 2
+            for (int jp = lane; jp < nj / 2; jp += 32) {
+                float4 f[NK];
 #pragma unroll
-            for (int r = 0; r < RW; r++) {
-                const int row = min(row0 + r, 3 * MF - 1);    // rows past the end repeat the last (not written)
-                const int c = row / MF, p = row % MF;
-                const float4* qrow = reinterpret_cast<const float4*>(
-                    Q + ((((long long)l * 2 + half) * 3 + c) * MF + p) * (long long)J + j0);
-#pragma unroll 4
-                for (int jp = lane; jp < nj / 2; jp += 32) {
-                    const float4 q = __ldcs(qrow + jp);       // streamed once: evict-first
+                for (int kk = 0; kk < NK; kk++) f[kk] = ph[jp][kk];
+                float4 q[RW];
+#pragma unroll
+                for (int r = 0; r < RW; r++) q[r] = __ldcs(qrow[r] + j0 / 2 + jp);     // streamed once: evict-first
+#pragma unroll
+                for (int r = 0; r < RW; r++) {
 #pragma unroll
                     for (int kk = 0; kk < NK; kk++) {
-                        const float4 f = ph[jp][kk];
-                        acc[r][kk][0] = fmaf(q.x, f.x, fmaf(-q.y, f.y, acc[r][kk][0]));
-                        acc[r][kk][1] = fmaf(q.x, f.y, fmaf(q.y, f.x, acc[r][kk][1]));
-                        acc[r][kk][0] = fmaf(q.z, f.z, fmaf(-q.w, f.w, acc[r][kk][0]));
-                        acc[r][kk][1] = fmaf(q.z, f.w, fmaf(q.w, f.z, acc[r][kk][1]));
+                        acc[r][kk][0] = fmaf(q[r].x, f[kk].x, fmaf(-q[r].y, f[kk].y, acc[r][kk][0]));
+                        acc[r][kk][1] = fmaf(q[r].x, f[kk].y, fmaf(q[r].y, f[kk].x, acc[r][kk][1]));
+                        acc[r][kk][0] = fmaf(q[r].z, f[kk].z, fmaf(-q[r].w, f[kk].w, acc[r][kk][0]));
+                        acc[r][kk][1] = fmaf(q[r].z, f[kk].w, fmaf(q[r].w, f[kk].z, acc[r][kk][1]));
                     }
                 }
             }

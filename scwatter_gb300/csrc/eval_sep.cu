@@ -65,7 +65,7 @@ __global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float*
 // multiply them with the group's phases, staged in shared memory per chunk of kChunk modes
 // and shared by the CTA's 8 warps.  Lane partial sums are reduced with warp shuffles.
 constexpr int kCtrWarps = 8;
-constexpr int kCtrChunk = 512;
+constexpr int kCtrChunk = 1024;
 
 template <int NK, int RW>
 __global__ void __launch_bounds__(kCtrWarps * 32, 2)
@@ -446,9 +446,11 @@ static scw_status launch_rows(scw_ctx ctx, const float2* C, const float2* Rtab, 
 scw_status sep_synth(scw_ctx ctx, const float2* T, const float2* F, int nrows, int ncols, int Mk, float* out,
                      int method) {
     if (method == SCW_SEP_TF32X3 || method == SCW_SEP_BF16X3) {
+        // shapes whose operands do not fit the tensor-core kernel's shared memory (more than
+        // 40 harmonics along the synthesis axis for 3xTF32, 72 for split-BF16) run the FP32 SIMT
+        // GEMM below, which is at least as accurate
         scw_status st = sep_synth_tc(ctx, T, F, nrows, ncols, Mk, out, method);
         if (st != SCW_ERR_UNSUPPORTED) return st;
-        return fail(SCW_ERR_UNSUPPORTED, "tensor-core synthesis does not support this shape");
     }
     if (Mk > kSynMaxK) return fail(SCW_ERR_UNSUPPORTED, "more than 64 harmonics along the synthesis axis");
     const size_t smem = (size_t)(kSynRows * 3 * kSynMaxK + kSynMaxK * kSynCols) * sizeof(float2);
@@ -487,7 +489,8 @@ scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, 
     // phases for the PGroups: at most nz groups
     const size_t phi_bytes = align256((size_t)nz * 2 * (size_t)s->Jp * kMaxGroup * sizeof(float2));
     const size_t c_bytes = align256((size_t)nz * 3 * MF * sizeof(float2));
-    const size_t t_bytes = align256((size_t)nrows * 3 * Mk * sizeof(float2) + 4096);
+    // slack past the last row: the tensor-core producer reads whole 16-row tiles of T
+    const size_t t_bytes = align256((size_t)nrows * 3 * Mk * sizeof(float2) + 16 * 3 * 64 * sizeof(float2) + 4096);
     const size_t tab_bytes = align256((size_t)(M0 + M1) * (Na + Nb + 2) * sizeof(float2));
     scw_status st = ctx->sep_scratch.reserve(phi_bytes + c_bytes + t_bytes + 2 * tab_bytes);
     if (st != SCW_OK) return st;

@@ -185,6 +185,19 @@ __device__ __forceinline__ uint4 pack4<1>(const __nv_bfloat16* v) { // 8 bf16 va
 }
 
 constexpr int kEpiWarps = 4, kProdWarps = 4;
+
+// OR of v over the producer warps (named barrier 1): keeps their loop decisions uniform so
+// every producer thread reaches the same named barriers
+__device__ __forceinline__ int producers_any(int v) {
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 q, %1, 0;\n\t"
+        "bar.red.or.pred p, 1, %2, q;\n\tselp.s32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"(v), "n"(kProdWarps * 32)
+        : "memory");
+    return r;
+}
 constexpr int kWsThreads = (kEpiWarps + kProdWarps + 1) * 32;
 
 template <int kKind>
@@ -204,7 +217,9 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     unsigned char* sA_hi = smem;
     unsigned char* sA_lo = sA_hi + a_bytes;
     unsigned char* sB0 = sA_lo + a_bytes;                     // slot s, part h: sB0 + (2 s + h) b_bytes
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sB0 + 4 * b_bytes);
+    float2* sT = reinterpret_cast<float2*>(sB0 + 4 * b_bytes);   // staged T tile [kRows][3][Mk]
+    const int t_tile = kRows * 3 * Mk;                           // float2 per tile (multiple of 2)
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sB0 + 4 * b_bytes + ((t_tile * 8 + 127) / 128) * 128);
     uint64_t* full_b = bar;          // [2] producers -> MMA
     uint64_t* empty_b = bar + 2;     // [2] MMA completion -> producers
     uint64_t* acc_full = bar + 4;    // [2] MMA completion -> epilogue
@@ -262,15 +277,24 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         // ---------------- producers ----------------
         const int pt = tid - kEpiWarps * 32;                  // 0 .. 127
         for (int i = 0; i < n_my; i++) {
-            if (*abort_flag) break;
             const int s = i & 1;
-            if (i >= 2 && !mbar_wait(&empty_b[s], (uint32_t)(((i >> 1) - 1) & 1))) {
+            int stop = *abort_flag;
+            if (!stop && i >= 2 && !mbar_wait(&empty_b[s], (uint32_t)(((i >> 1) - 1) & 1))) stop = 1;
+            if (producers_any(stop)) {
                 *abort_flag = 1;
                 break;
             }
             const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
             unsigned char* bh = sB0 + (2 * s + 0) * b_bytes;
             unsigned char* bl = sB0 + (2 * s + 1) * b_bytes;
+            // stage the tile's rows of T (one contiguous block; the buffer has slack past the
+            // last row, whose values are masked below) with coalesced 16-byte loads
+            {
+                const float4* src = reinterpret_cast<const float4*>(T + (long long)r0 * 3 * Mk);
+                float4* dst = reinterpret_cast<float4*>(sT);
+                for (int e = pt; e < t_tile / 2; e += kProdWarps * 32) dst[e] = __ldg(src + e);
+                asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");
+            }
             for (int g = pt; g < kN * KC; g += kProdWarps * 32) {
                 const int n = g & 7 | ((g / (8 * KC)) << 3);
                 const int kc = (g >> 3) % KC;
@@ -283,7 +307,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                     float v = 0.f;
                     if (row < nrows && k < 2 * Mk) {
                         const int m = k < Mk ? k : k - Mk;
-                        const float2 t = T[((long long)row * 3 + c) * Mk + m];
+                        const float2 t = sT[(r * 3 + c) * Mk + m];
                         // s = 0 (Re E): [Re T | -Im T];  s = 1 (Im E): [Im T | Re T]
                         v = sri == 0 ? (k < Mk ? t.x : -t.y) : (k < Mk ? t.y : t.x);
                     }
@@ -294,6 +318,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             }
             fence_proxy_async();
             mbar_arrive(&full_b[s]);
+            asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");   // sT reusable
         }
     } else if (warp == kEpiWarps + kProdWarps) {
         // ---------------- MMA issuer ----------------
@@ -381,7 +406,8 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int kalign = kind == 0 ? 8 : 16;                  // K per MMA instruction
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
-    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + 128;
+    const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * Mk * 8 + 127) / 128 * 128;
+    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + t_tile_bytes + 128;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     if (!ctx->tc_err) {
         if (cudaMalloc(&ctx->tc_err, sizeof(int)) != cudaSuccess) return fail(SCW_ERR_NOMEM, "cudaMalloc error flag");

@@ -133,10 +133,16 @@ __device__ __forceinline__ uint32_t core_offset(int row, int kbyte, uint32_t sbo
     return (uint32_t)(row >> 3) * sbo + (uint32_t)(kbyte >> 4) * 128u + (uint32_t)(row & 7) * 16u + (uint32_t)(kbyte & 15);
 }
 
-__device__ __forceinline__ float tf32_rna(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+// round-to-nearest-even to the 10-bit tf32 mantissa with integer operations (keeps the split
+// off the conversion pipe); finite inputs only, which is all the operands ever are
+__device__ __forceinline__ float tf32_rn(float x) {
+    const uint32_t b = __float_as_uint(x);
+    return __uint_as_float((b + 0xFFFu + ((b >> 13) & 1u)) & 0xFFFFE000u);
+}
+
+__device__ __forceinline__ __nv_bfloat16 bf16_rn(float x) {
+    const uint32_t b = __float_as_uint(x);
+    return __ushort_as_bfloat16((unsigned short)((b + 0x7FFFu + ((b >> 16) & 1u)) >> 16));
 }
 
 template <int kKind>
@@ -147,8 +153,8 @@ struct Split<0> {           // tf32 in fp32 containers
     using T = float;
     static constexpr int kBytes = 4;
     __device__ static void split(float x, float& hi, float& lo) {
-        hi = tf32_rna(x);
-        lo = tf32_rna(x - hi);
+        hi = tf32_rn(x);
+        lo = tf32_rn(x - hi);
     }
 };
 
@@ -157,8 +163,8 @@ struct Split<1> {           // bf16
     using T = __nv_bfloat16;
     static constexpr int kBytes = 2;
     __device__ static void split(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-        hi = __float2bfloat16_rn(x);
-        lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+        hi = bf16_rn(x);
+        lo = bf16_rn(x - __bfloat162float(hi));
     }
 };
 
@@ -219,7 +225,8 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     unsigned char* sB0 = sA_lo + a_bytes;                     // slot s, part h: sB0 + (2 s + h) b_bytes
     float2* sT = reinterpret_cast<float2*>(sB0 + 4 * b_bytes);   // staged T tile [kRows][3][Mk]
     const int t_tile = kRows * 3 * Mk;                           // float2 per tile (multiple of 2)
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sB0 + 4 * b_bytes + ((t_tile * 8 + 127) / 128) * 128);
+    float* sOut = reinterpret_cast<float*>(sB0 + 4 * b_bytes + ((t_tile * 8 + 127) / 128) * 128);   // [4 warps][192]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sOut + kEpiWarps * 192);
     uint64_t* full_b = bar;          // [2] producers -> MMA
     uint64_t* empty_b = bar + 2;     // [2] MMA completion -> producers
     uint64_t* acc_full = bar + 4;    // [2] MMA completion -> epilogue
@@ -356,7 +363,6 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         __syncwarp();
     } else {
         // ---------------- epilogue (warps 0-3, TMEM lanes 32 w .. 32 w + 31) ----------------
-        const int xg = x0 + warp * 32 + lane;
         for (int i = 0; i < n_my; i++) {
             if (*abort_flag) break;
             const int a = i & 1;
@@ -369,21 +375,32 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             tc_fence_after();
             const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
             const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * 128);
-            uint32_t v[32];
-#pragma unroll 1
-            for (int q = 0; q < kN / 32; q++) {
-                tmem_ld32(tbase + (uint32_t)(q * 32), v);
-                tmem_ld_wait();
+            // TMEM -> registers (16 rows x 6 floats per lane) -> per-row staging in shared memory
+            // (lane l at float offset 6 l) -> 768 contiguous bytes per row with 16-byte stores
+            uint32_t v[kN];
+            tmem_ld32(tbase + 0u, *reinterpret_cast<uint32_t(*)[32]>(&v[0]));
+            tmem_ld32(tbase + 32u, *reinterpret_cast<uint32_t(*)[32]>(&v[32]));
+            tmem_ld32(tbase + 64u, *reinterpret_cast<uint32_t(*)[32]>(&v[64]));
+            tmem_ld_wait();
+            float* stage = sOut + warp * 192;
+            const int xw = x0 + warp * 32;                     // first x of this warp
+            const int nx = min(32, ncols - xw);               // valid x of this warp
 #pragma unroll
-                for (int cc = 0; cc < 32; cc += 2) {
-                    const int col = q * 32 + cc;               // even column: (row r, component c, re); odd: im
-                    const int r = col / 6, w = col % 6;
-                    const int row = r0 + r;
-                    if (xg < ncols && row < nrows) {
-                        const float2 val = make_float2(__uint_as_float(v[cc]), __uint_as_float(v[cc + 1]));
-                        *reinterpret_cast<float2*>(out + ((long long)row * ncols + xg) * 6 + w) = val;
-                    }
+            for (int r = 0; r < kRows; r++) {
+                const int row = r0 + r;
+                if (row >= nrows || nx <= 0) break;           // warp-uniform
+                reinterpret_cast<float2*>(stage)[3 * lane + 0] = make_float2(__uint_as_float(v[6 * r + 0]), __uint_as_float(v[6 * r + 1]));
+                reinterpret_cast<float2*>(stage)[3 * lane + 1] = make_float2(__uint_as_float(v[6 * r + 2]), __uint_as_float(v[6 * r + 3]));
+                reinterpret_cast<float2*>(stage)[3 * lane + 2] = make_float2(__uint_as_float(v[6 * r + 4]), __uint_as_float(v[6 * r + 5]));
+                __syncwarp();
+                float* dst = out + ((long long)row * ncols + xw) * 6;
+                if (nx == 32 && ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0)) {
+                    reinterpret_cast<float4*>(dst)[lane] = reinterpret_cast<const float4*>(stage)[lane];
+                    if (lane < 16) reinterpret_cast<float4*>(dst)[32 + lane] = reinterpret_cast<const float4*>(stage)[32 + lane];
+                } else {
+                    for (int f = lane; f < nx * 6; f += 32) dst[f] = stage[f];
                 }
+                __syncwarp();
             }
             tc_fence_before();
             mbar_arrive(&acc_empty[a]);
@@ -407,7 +424,7 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
     const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * Mk * 8 + 127) / 128 * 128;
-    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + t_tile_bytes + 128;
+    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + t_tile_bytes + tc::kEpiWarps * 192 * 4 + 128;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     if (!ctx->tc_err) {
         if (cudaMalloc(&ctx->tc_err, sizeof(int)) != cudaSuccess) return fail(SCW_ERR_NOMEM, "cudaMalloc error flag");

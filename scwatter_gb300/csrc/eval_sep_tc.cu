@@ -190,7 +190,7 @@ __device__ __forceinline__ uint4 pack4<1>(const __nv_bfloat16* v) { // 8 bf16 va
     return r;
 }
 
-constexpr int kEpiWarps = 4, kProdWarps = 4;
+constexpr int kEpiWarps = 4, kProdWarps = 8;
 
 // OR of v over the producer warps (named barrier 1): keeps their loop decisions uniform so
 // every producer thread reaches the same named barriers
@@ -295,33 +295,59 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             unsigned char* bh = sB0 + (2 * s + 0) * b_bytes;
             unsigned char* bl = sB0 + (2 * s + 1) * b_bytes;
             // stage the tile's rows of T (one contiguous block; the buffer has slack past the
-            // last row, whose values are masked below) with coalesced 16-byte loads
+            // last row, whose values are masked below) with coalesced 16-byte loads, all issued
+            // before the first shared-memory store
             {
                 const float4* src = reinterpret_cast<const float4*>(T + (long long)r0 * 3 * Mk);
                 float4* dst = reinterpret_cast<float4*>(sT);
-                for (int e = pt; e < t_tile / 2; e += kProdWarps * 32) dst[e] = __ldg(src + e);
+                const int n4 = t_tile / 2;
+                constexpr int kPer = (kRows * 3 * 64 / 2 + kProdWarps * 32 - 1) / (kProdWarps * 32);
+                float4 buf[kPer];
+#pragma unroll
+                for (int u = 0; u < kPer; u++) {
+                    const int e = pt + u * kProdWarps * 32;
+                    if (e < n4) buf[u] = __ldg(src + e);
+                }
+#pragma unroll
+                for (int u = 0; u < kPer; u++) {
+                    const int e = pt + u * kProdWarps * 32;
+                    if (e < n4) dst[e] = buf[u];
+                }
                 asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");
             }
-            for (int g = pt; g < kN * KC; g += kProdWarps * 32) {
-                const int n = g & 7 | ((g / (8 * KC)) << 3);
-                const int kc = (g >> 3) % KC;
-                const int r = n / 6, c = (n % 6) >> 1, sri = n & 1;
-                const int row = r0 + r;
-                E hi[EPC], lo[EPC];
+            // groups g = pt + t * (threads): q = g / 8 advances by threads / 8 per step, so the
+            // core column kc = q % KC and the 8-row block nb = q / KC update without division
+            {
+                int q = pt >> 3;
+                int nb = q / KC, kc = q - nb * KC;
+                const int nlo = pt & 7;
+                constexpr int kStepQ = kProdWarps * 32 / 8;
+                for (int g = pt; g < kN * KC; g += kProdWarps * 32) {
+                    const int n = (nb << 3) | nlo;
+                    const int r = n / 6, c = (n - 6 * r) >> 1, sri = n & 1;
+                    const bool live = (r0 + r) < nrows;
+                    const float2* trow = sT + (r * 3 + c) * Mk;
+                    E hi[EPC], lo[EPC];
 #pragma unroll
-                for (int e = 0; e < EPC; e++) {
-                    const int k = kc * EPC + e;
-                    float v = 0.f;
-                    if (row < nrows && k < 2 * Mk) {
-                        const int m = k < Mk ? k : k - Mk;
-                        const float2 t = sT[(r * 3 + c) * Mk + m];
-                        // s = 0 (Re E): [Re T | -Im T];  s = 1 (Im E): [Im T | Re T]
-                        v = sri == 0 ? (k < Mk ? t.x : -t.y) : (k < Mk ? t.y : t.x);
+                    for (int e = 0; e < EPC; e++) {
+                        const int k = kc * EPC + e;
+                        float v = 0.f;
+                        if (live && k < 2 * Mk) {
+                            const bool first = k < Mk;
+                            const float2 t = trow[first ? k : k - Mk];
+                            // s = 0 (Re E): [Re T | -Im T];  s = 1 (Im E): [Im T | Re T]
+                            v = sri == 0 ? (first ? t.x : -t.y) : (first ? t.y : t.x);
+                        }
+                        Split<kKind>::split(v, hi[e], lo[e]);
                     }
-                    Split<kKind>::split(v, hi[e], lo[e]);
+                    *reinterpret_cast<uint4*>(bh + (uint32_t)g * 16) = pack4<kKind>(hi);
+                    *reinterpret_cast<uint4*>(bl + (uint32_t)g * 16) = pack4<kKind>(lo);
+                    kc += kStepQ;
+                    while (kc >= KC) {
+                        kc -= KC;
+                        nb++;
+                    }
                 }
-                *reinterpret_cast<uint4*>(bh + (uint32_t)g * 16) = pack4<kKind>(hi);
-                *reinterpret_cast<uint4*>(bl + (uint32_t)g * 16) = pack4<kKind>(lo);
             }
             fence_proxy_async();
             mbar_arrive(&full_b[s]);

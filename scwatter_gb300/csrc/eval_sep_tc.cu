@@ -223,9 +223,13 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     unsigned char* sA_hi = smem;
     unsigned char* sA_lo = sA_hi + a_bytes;
     unsigned char* sB0 = sA_lo + a_bytes;                     // slot s, part h: sB0 + (2 s + h) b_bytes
-    float2* sT = reinterpret_cast<float2*>(sB0 + 4 * b_bytes);   // staged T tile [kRows][3][Mk]
-    const int t_tile = kRows * 3 * Mk;                           // float2 per tile (multiple of 2)
-    float* sOut = reinterpret_cast<float*>(sB0 + 4 * b_bytes + ((t_tile * 8 + 127) / 128) * 128);   // [4 warps][192]
+    float2* sT = reinterpret_cast<float2*>(sB0 + 4 * b_bytes);   // staged T tile [kRows * 3][tstr]
+    const int t_tile = kRows * 3 * Mk;                           // float2 of T per tile
+    // fast producer path: Mk a multiple of the elements per core row; T rows padded in shared
+    // memory to an odd number of 16-byte chunks so a warp's 16-byte reads spread over the banks
+    const bool fast = (Mk % EPC) == 0 && (Mk % 2) == 0;
+    const int tstr = fast ? ((Mk / 2) % 2 == 0 ? Mk + 2 : Mk + 4) : Mk;
+    float* sOut = reinterpret_cast<float*>(sB0 + 4 * b_bytes + ((kRows * 3 * (Mk + 4) * 8 + 127) / 128) * 128);   // [4 warps][192]
     uint64_t* bar = reinterpret_cast<uint64_t*>(sOut + kEpiWarps * 192);
     uint64_t* full_b = bar;          // [2] producers -> MMA
     uint64_t* empty_b = bar + 2;     // [2] MMA completion -> producers
@@ -296,11 +300,10 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             unsigned char* bl = sB0 + (2 * s + 1) * b_bytes;
             // stage the tile's rows of T (one contiguous block; the buffer has slack past the
             // last row, whose values are masked below) with coalesced 16-byte loads, all issued
-            // before the first shared-memory store
+            // before the first shared-memory store; row (r, c) lands at sT + (3 r + c) * tstr
             {
                 const float4* src = reinterpret_cast<const float4*>(T + (long long)r0 * 3 * Mk);
-                float4* dst = reinterpret_cast<float4*>(sT);
-                const int n4 = t_tile / 2;
+                const int n4 = t_tile / 2;                    // Mk even on the fast path
                 constexpr int kPer = (kRows * 3 * 64 / 2 + kProdWarps * 32 - 1) / (kProdWarps * 32);
                 float4 buf[kPer];
 #pragma unroll
@@ -308,16 +311,74 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                     const int e = pt + u * kProdWarps * 32;
                     if (e < n4) buf[u] = __ldg(src + e);
                 }
+                if (fast) {
+                    const int h = Mk / 2;                      // float4 per T row
 #pragma unroll
-                for (int u = 0; u < kPer; u++) {
-                    const int e = pt + u * kProdWarps * 32;
-                    if (e < n4) dst[e] = buf[u];
+                    for (int u = 0; u < kPer; u++) {
+                        const int e = pt + u * kProdWarps * 32;
+                        if (e < n4) {
+                            const int row = e / h;
+                            reinterpret_cast<float4*>(sT + row * tstr)[e - row * h] = buf[u];
+                        }
+                    }
+                } else {
+                    // generic path (odd Mk): element-wise copy through the float2 view
+                    for (int e = pt; e < t_tile; e += kProdWarps * 32) sT[e] = T[(long long)r0 * 3 * Mk + e];
                 }
                 asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");
             }
-            // groups g = pt + t * (threads): q = g / 8 advances by threads / 8 per step, so the
-            // core column kc = q % KC and the 8-row block nb = q / KC update without division
-            {
+            if (fast) {
+                // task = (8-row block nb, row pair nq, core column kc); lanes: nq fastest, then kc.
+                // One task reads 16 bytes x EPC/2 of T row (4 nb + nq) once and writes the Re (n even)
+                // and Im (n odd) rows of B, hi and lo; the two stores per part are issued in an
+                // order that alternates with kc so each warp store covers all 8 bank groups.
+                const int ntask = (kN / 8) * KC * 4;
+                for (int tsk = pt; tsk < ntask; tsk += kProdWarps * 32) {
+                    const int nq = tsk & 3;
+                    const int q = tsk >> 2;
+                    const int nb = q / KC, kc = q - nb * KC;
+                    const int trow = 4 * nb + nq;             // = (r, c) row of T: n >> 1
+                    const int r = trow / 3;
+                    const bool live = (r0 + r) < nrows;
+                    const int k0 = kc * EPC;
+                    E h0[EPC], l0[EPC], h1[EPC], l1[EPC];
+                    if (live && k0 < 2 * Mk) {
+                        const bool first = k0 < Mk;
+                        const float4* tp = reinterpret_cast<const float4*>(sT + trow * tstr + (first ? k0 : k0 - Mk));
+#pragma unroll
+                        for (int e2 = 0; e2 < EPC / 2; e2++) {
+                            const float4 t = tp[e2];
+                            // s = 0 (Re E): [Re T | -Im T];  s = 1 (Im E): [Im T | Re T]
+                            const float a0 = first ? t.x : -t.y, a1 = first ? t.z : -t.w;
+                            const float b0 = first ? t.y : t.x, b1 = first ? t.w : t.z;
+                            Split<kKind>::split(a0, h0[2 * e2], l0[2 * e2]);
+                            Split<kKind>::split(a1, h0[2 * e2 + 1], l0[2 * e2 + 1]);
+                            Split<kKind>::split(b0, h1[2 * e2], l1[2 * e2]);
+                            Split<kKind>::split(b1, h1[2 * e2 + 1], l1[2 * e2 + 1]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < EPC; e++) Split<kKind>::split(0.f, h0[e], l0[e]);
+#pragma unroll
+                        for (int e = 0; e < EPC; e++) Split<kKind>::split(0.f, h1[e], l1[e]);
+                    }
+                    const uint32_t base = (uint32_t)nb * sbo + (uint32_t)kc * 128u + (uint32_t)(2 * nq) * 16u;
+                    const uint4 vh0 = pack4<kKind>(h0), vh1 = pack4<kKind>(h1);
+                    const uint4 vl0 = pack4<kKind>(l0), vl1 = pack4<kKind>(l1);
+                    if ((kc & 1) == 0) {
+                        *reinterpret_cast<uint4*>(bh + base) = vh0;
+                        *reinterpret_cast<uint4*>(bh + base + 16) = vh1;
+                        *reinterpret_cast<uint4*>(bl + base) = vl0;
+                        *reinterpret_cast<uint4*>(bl + base + 16) = vl1;
+                    } else {
+                        *reinterpret_cast<uint4*>(bh + base + 16) = vh1;
+                        *reinterpret_cast<uint4*>(bh + base) = vh0;
+                        *reinterpret_cast<uint4*>(bl + base + 16) = vl1;
+                        *reinterpret_cast<uint4*>(bl + base) = vl0;
+                    }
+                }
+            } else {
+                // generic path: one 16-byte core row per group, groups in address order
                 int q = pt >> 3;
                 int nb = q / KC, kc = q - nb * KC;
                 const int nlo = pt & 7;
@@ -326,7 +387,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                     const int n = (nb << 3) | nlo;
                     const int r = n / 6, c = (n - 6 * r) >> 1, sri = n & 1;
                     const bool live = (r0 + r) < nrows;
-                    const float2* trow = sT + (r * 3 + c) * Mk;
+                    const float2* trow = sT + (r * 3 + c) * tstr;
                     E hi[EPC], lo[EPC];
 #pragma unroll
                     for (int e = 0; e < EPC; e++) {
@@ -335,7 +396,6 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                         if (live && k < 2 * Mk) {
                             const bool first = k < Mk;
                             const float2 t = trow[first ? k : k - Mk];
-                            // s = 0 (Re E): [Re T | -Im T];  s = 1 (Im E): [Im T | Re T]
                             v = sri == 0 ? (first ? t.x : -t.y) : (first ? t.y : t.x);
                         }
                         Split<kKind>::split(v, hi[e], lo[e]);
@@ -449,7 +509,7 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int kalign = kind == 0 ? 8 : 16;                  // K per MMA instruction
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
-    const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * Mk * 8 + 127) / 128 * 128;
+    const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * (Mk + 4) * 8 + 127) / 128 * 128;   // padded rows
     const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + t_tile_bytes + tc::kEpiWarps * 192 * 4 + 128;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     if (!ctx->tc_err) {

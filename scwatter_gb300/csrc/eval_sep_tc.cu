@@ -152,9 +152,11 @@ template <>
 struct Split<0> {           // tf32 in fp32 containers
     using T = float;
     static constexpr int kBytes = 4;
+    // hi: x with the low 13 mantissa bits cleared; lo = x - hi is exact, and the tensor core
+    // reads its top 19 bits, so x = hi + lo to within 2^-20 |x|
     __device__ static void split(float x, float& hi, float& lo) {
-        hi = tf32_rn(x);
-        lo = tf32_rn(x - hi);
+        hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+        lo = x - hi;
     }
 };
 
@@ -286,7 +288,18 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
 
     if (warp >= kEpiWarps && warp < kEpiWarps + kProdWarps) {
         // ---------------- producers ----------------
-        const int pt = tid - kEpiWarps * 32;                  // 0 .. 127
+        const int pt = tid - kEpiWarps * 32;                  // 0 .. kProdWarps * 32 - 1
+        constexpr int kPer = (kRows * 3 * 64 / 2 + kProdWarps * 32 - 1) / (kProdWarps * 32);
+        const int n4 = t_tile / 2;
+        float4 tbuf[kPer];
+        auto load_t = [&](int rr0, float4 (&buf)[kPer]) {
+            const float4* src = reinterpret_cast<const float4*>(T + (long long)rr0 * 3 * Mk);
+#pragma unroll
+            for (int u = 0; u < kPer; u++) {
+                const int e = pt + u * kProdWarps * 32;
+                if (e < n4) buf[u] = __ldg(src + e);
+            }
+        };
         for (int i = 0; i < n_my; i++) {
             const int s = i & 1;
             int stop = *abort_flag;
@@ -298,35 +311,25 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
             unsigned char* bh = sB0 + (2 * s + 0) * b_bytes;
             unsigned char* bl = sB0 + (2 * s + 1) * b_bytes;
-            // stage the tile's rows of T (one contiguous block; the buffer has slack past the
-            // last row, whose values are masked below) with coalesced 16-byte loads, all issued
-            // before the first shared-memory store; row (r, c) lands at sT + (3 r + c) * tstr
-            {
-                const float4* src = reinterpret_cast<const float4*>(T + (long long)r0 * 3 * Mk);
-                const int n4 = t_tile / 2;                    // Mk even on the fast path
-                constexpr int kPer = (kRows * 3 * 64 / 2 + kProdWarps * 32 - 1) / (kProdWarps * 32);
-                float4 buf[kPer];
+            // stage the tile's rows of T: the coalesced 16-byte loads of tile i were issued while
+            // tile i-1 was being built (or just now for the first tile); the buffer has slack past
+            // the last row, whose values are masked below; row (r, c) lands at sT + (3 r + c) * tstr
+            if (i == 0) load_t(r0, tbuf);
+            if (fast) {
+                const int h = Mk / 2;                          // float4 per T row
 #pragma unroll
                 for (int u = 0; u < kPer; u++) {
                     const int e = pt + u * kProdWarps * 32;
-                    if (e < n4) buf[u] = __ldg(src + e);
-                }
-                if (fast) {
-                    const int h = Mk / 2;                      // float4 per T row
-#pragma unroll
-                    for (int u = 0; u < kPer; u++) {
-                        const int e = pt + u * kProdWarps * 32;
-                        if (e < n4) {
-                            const int row = e / h;
-                            reinterpret_cast<float4*>(sT + row * tstr)[e - row * h] = buf[u];
-                        }
+                    if (e < n4) {
+                        const int row = e / h;
+                        reinterpret_cast<float4*>(sT + row * tstr)[e - row * h] = tbuf[u];
                     }
-                } else {
-                    // generic path (odd Mk): element-wise copy through the float2 view
-                    for (int e = pt; e < t_tile; e += kProdWarps * 32) sT[e] = T[(long long)r0 * 3 * Mk + e];
                 }
-                asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");
+            } else {
+                for (int e = pt; e < t_tile; e += kProdWarps * 32) sT[e] = T[(long long)r0 * 3 * Mk + e];
             }
+            asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");
+            if (i + 1 < n_my) load_t(r0 + (int)gridDim.y * kRows, tbuf);    // prefetch the next tile
             if (fast) {
                 // task = (8-row block nb, row pair nq, core column kc); lanes: nq fastest, then kc.
                 // One task reads 16 bytes x EPC/2 of T row (4 nb + nq) once and writes the Re (n even)

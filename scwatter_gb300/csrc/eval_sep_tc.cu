@@ -231,7 +231,8 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     // memory to an odd number of 16-byte chunks so a warp's 16-byte reads spread over the banks
     const bool fast = (Mk % EPC) == 0 && (Mk % 2) == 0;
     const int tstr = fast ? ((Mk / 2) % 2 == 0 ? Mk + 2 : Mk + 4) : Mk;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sB0 + 4 * b_bytes + ((kRows * 3 * (Mk + 4) * 8 + 127) / 128) * 128);
+    float* sOut = reinterpret_cast<float*>(sB0 + 4 * b_bytes + ((kRows * 3 * (Mk + 4) * 8 + 127) / 128) * 128);   // [4 warps][192]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sOut + kEpiWarps * 192);
     uint64_t* full_b = bar;          // [2] producers -> MMA
     uint64_t* empty_b = bar + 2;     // [2] MMA completion -> producers
     uint64_t* acc_full = bar + 4;    // [2] MMA completion -> epilogue
@@ -468,50 +469,32 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             tc_fence_after();
             const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
             const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * 128);
-            // TMEM -> registers: 16 rows x 6 floats of E(row, x) per lane (x = x0 + 32 w + lane).
-            // A lane pair (x even, x + 1) owns 48 contiguous bytes per row = 3 float4:
-            //   even lane writes (e0..e3 of x) and (e4, e5 of x, e0, e1 of x + 1),
-            //   odd lane writes (e2..e5 of x + 1)
-            // so each row of the warp goes out as two 16-byte store instructions.
+            // TMEM -> registers (16 rows x 6 floats per lane) -> per-row staging in shared memory
+            // (lane l at float offset 6 l) -> 768 contiguous bytes per row with 16-byte stores
             uint32_t v[kN];
             tmem_ld32(tbase + 0u, *reinterpret_cast<uint32_t(*)[32]>(&v[0]));
             tmem_ld32(tbase + 32u, *reinterpret_cast<uint32_t(*)[32]>(&v[32]));
             tmem_ld32(tbase + 64u, *reinterpret_cast<uint32_t(*)[32]>(&v[64]));
             tmem_ld_wait();
-            const int xg = x0 + warp * 32 + lane;
-            const int x_even = xg & ~1;
-            const bool odd = (lane & 1) != 0;
-            const bool vec = (ncols % 2) == 0;                 // 16-byte aligned pair records
+            float* stage = sOut + warp * 192;
+            const int xw = x0 + warp * 32;                     // first x of this warp
+            const int nx = min(32, ncols - xw);               // valid x of this warp
 #pragma unroll
             for (int r = 0; r < kRows; r++) {
                 const int row = r0 + r;
-                if (row >= nrows) break;                        // warp-uniform
-                const float f0 = __uint_as_float(v[6 * r + 0]), f1 = __uint_as_float(v[6 * r + 1]);
-                const float f2 = __uint_as_float(v[6 * r + 2]), f3 = __uint_as_float(v[6 * r + 3]);
-                const float f4 = __uint_as_float(v[6 * r + 4]), f5 = __uint_as_float(v[6 * r + 5]);
-                const float n0 = __shfl_down_sync(0xffffffffu, f0, 1);
-                const float n1 = __shfl_down_sync(0xffffffffu, f1, 1);
-                if (vec) {
-                    float* pair = out + ((long long)row * ncols + x_even) * 6;
-                    if (x_even + 1 < ncols || !odd) {
-                        if (!odd) {
-                            if (x_even + 1 < ncols) {
-                                reinterpret_cast<float4*>(pair)[0] = make_float4(f0, f1, f2, f3);
-                                reinterpret_cast<float4*>(pair)[1] = make_float4(f4, f5, n0, n1);
-                            } else if (xg < ncols) {
-                                reinterpret_cast<float4*>(pair)[0] = make_float4(f0, f1, f2, f3);
-                                reinterpret_cast<float2*>(pair)[2] = make_float2(f4, f5);
-                            }
-                        } else if (xg < ncols) {
-                            reinterpret_cast<float4*>(pair)[2] = make_float4(f2, f3, f4, f5);
-                        }
-                    }
-                } else if (xg < ncols) {
-                    float2* p = reinterpret_cast<float2*>(out + ((long long)row * ncols + xg) * 6);
-                    p[0] = make_float2(f0, f1);
-                    p[1] = make_float2(f2, f3);
-                    p[2] = make_float2(f4, f5);
+                if (row >= nrows || nx <= 0) break;           // warp-uniform
+                reinterpret_cast<float2*>(stage)[3 * lane + 0] = make_float2(__uint_as_float(v[6 * r + 0]), __uint_as_float(v[6 * r + 1]));
+                reinterpret_cast<float2*>(stage)[3 * lane + 1] = make_float2(__uint_as_float(v[6 * r + 2]), __uint_as_float(v[6 * r + 3]));
+                reinterpret_cast<float2*>(stage)[3 * lane + 2] = make_float2(__uint_as_float(v[6 * r + 4]), __uint_as_float(v[6 * r + 5]));
+                __syncwarp();
+                float* dst = out + ((long long)row * ncols + xw) * 6;
+                if (nx == 32 && ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0)) {
+                    reinterpret_cast<float4*>(dst)[lane] = reinterpret_cast<const float4*>(stage)[lane];
+                    if (lane < 16) reinterpret_cast<float4*>(dst)[32 + lane] = reinterpret_cast<const float4*>(stage)[32 + lane];
+                } else {
+                    for (int f = lane; f < nx * 6; f += 32) dst[f] = stage[f];
                 }
+                __syncwarp();
             }
             tc_fence_before();
             mbar_arrive(&acc_empty[a]);
@@ -535,7 +518,7 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
     const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * (Mk + 4) * 8 + 127) / 128 * 128;   // padded rows
-    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + t_tile_bytes + 128;
+    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + t_tile_bytes + tc::kEpiWarps * 192 * 4 + 128;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     if (!ctx->tc_err) {
         if (cudaMalloc(&ctx->tc_err, sizeof(int)) != cudaSuccess) return fail(SCW_ERR_NOMEM, "cudaMalloc error flag");

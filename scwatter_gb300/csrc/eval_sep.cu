@@ -71,7 +71,7 @@ template <int NK, int RW>
 __global__ void __launch_bounds__(kCtrWarps * 32, 2)
 sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict__ Phi,
                     const float2* __restrict__ Q, int MF, int J, float2* __restrict__ C) {
-    __shared__ float4 ph[kCtrChunk / 2][NK];    // (phi[j][kk], phi[j+1][kk]) pairs
+    __shared__ float4 ph[NK][kCtrChunk / 2];    // (phi[j][kk], phi[j+1][kk]) pairs; lanes read consecutive pairs
     const PGroup g = groups[blockIdx.y];
     const int l = g.region - 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -97,7 +97,7 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
                 const int jp = e / NK, kk = e % NK;
                 const float2 a = Pg[((long long)half * J + j0 + 2 * jp) * NK + kk];
                 const float2 b = Pg[((long long)half * J + j0 + 2 * jp + 1) * NK + kk];
-                ph[jp][kk] = make_float4(a.x, a.y, b.x, b.y);
+                ph[kk][jp] = make_float4(a.x, a.y, b.x, b.y);
             }
             __syncthreads();
             // each lane keeps one phase pair in registers and applies it to the warp's RW rows
@@ -105,7 +105,7 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
             for (int jp = lane; jp < nj / 2; jp += 32) {
                 float4 f[NK];
 #pragma unroll
-                for (int kk = 0; kk < NK; kk++) f[kk] = ph[jp][kk];
+                for (int kk = 0; kk < NK; kk++) f[kk] = ph[kk][jp];
                 float4 q[RW];
 #pragma unroll
                 for (int r = 0; r < RW; r++) q[r] = __ldcs(qrow[r] + j0 / 2 + jp);     // streamed once: evict-first

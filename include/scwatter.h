@@ -166,6 +166,22 @@ SCW_API scw_status scw_sep_gpu_cw_evaluate(scw_sep s, float* E_xy, float* E_xz, 
                                            float x_start, float y_start, float z_start,
                                            float x, float y, float z, float d, int N, int device, int method);
 
+/* ---------------------------------------------------------------------------------- */
+/* FP64 complex dense linear algebra on DEVICE buffers (row-major, batched back to     */
+/* back) -- GPU replacements of the reference's LAPACK wrappers                         */
+/* MKL_multiply / MKL_linearsolve / MKL_eigensolve (third_Lapack.h:38-87).              */
+/* Complex values are (re, im) doubles.                                                 */
+/* ---------------------------------------------------------------------------------- */
+/* C = alpha A B + beta C; A: M x K, B: K x N, C: M x N per batch entry. */
+SCW_API scw_status scw_zgemm(scw_ctx ctx, int M, int N, int K, const double* alpha, const void* A, const void* B,
+                             const double* beta, void* C, int batch);
+/* B := A^-1 B (A n x n overwritten by its LU factors, B n x nrhs); SCW_ERR_NUMERIC if singular;
+ * info_host (optional, batch ints) receives the first zero pivot + 1 per matrix. */
+SCW_API scw_status scw_zgesv(scw_ctx ctx, int n, int nrhs, void* A, void* B, int batch, int* info_host);
+/* eigenvalues W (n) and right eigenvectors V (n x n, column k = eigenvector k) of A (n x n,
+ * overwritten); SCW_ERR_NUMERIC if the QR iteration does not converge. */
+SCW_API scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* status_host);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,6 +73,9 @@ _SIGS = {
     "scw_sep_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
     "scw_sep_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P, I32],
     "scw_sep_gpu_cw_evaluate": [P, P, P, P, F32, F32, F32, F32, F32, F32, F32, I32, I32, I32],
+    "scw_zgemm": [P, I32, I32, I32, P, P, P, P, P, I32],
+    "scw_zgesv": [P, I32, I32, P, P, I32, P],
+    "scw_zgeev": [P, I32, P, P, P, I32, P],
 }
 
 

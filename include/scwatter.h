@@ -131,6 +131,22 @@ SCW_API scw_status scw_eval_plane_device(scw_waves waves, int axis, float a_star
  * and sum rounded to float separately. */
 SCW_API scw_status scw_eval_volume_device(scw_waves waves, float x_start, float y_start, float z_start,
                                           float dx, float dy, float dz, int Nx, int Ny, int Nz, float* dE);
+/* Allocation-free variant of scw_eval_plane_device (no counterpart in the reference).
+ * Same arguments, output and stream behaviour, for callers that must not allocate GPU memory
+ * while they run: applications that pre-size one device pool and count any other cudaMalloc
+ * as a leak, frame loops that may not stall on the allocator, plug-in hosts that forbid device
+ * allocation.  It calls no cudaMalloc, cudaMallocHost, cudaFree or allocating library routine:
+ * its split-K partial sums live in a 12 MiB array compiled into the library (held on every
+ * GPU that loads it until exit) and its region table travels as kernel parameters.
+ * Limits: N <= 16384 and at most 160 layers (SCW_ERR_ARG beyond either); planes of more
+ * than 1024 tiles of 16 x 32 points run without the split.
+ * The first call on a device looks up the array's device address (and may load the library's
+ * GPU module there); make that first call before any stream capture on that device.
+ * All calls share the one array per device: calls that overlap on the GPU (other streams,
+ * other contexts on the same device) race.  Calls on one stream are ordered and safe; each
+ * call writes every scratch element it reads, so nothing needs clearing between calls. */
+SCW_API scw_status scw_eval_plane_device_static(scw_waves waves, int axis, float a_start, float b_start,
+                                                float c, float d, int N, float* dE);
 
 /* ---------------------------------------------------------------------------------- */
 /* Separable ("GEMM form") evaluator -- no reference counterpart; evaluates the same    */

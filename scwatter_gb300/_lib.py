@@ -62,6 +62,7 @@ _SIGS = {
     "scw_gpu_cw_evaluate": [P, P, P, P, F32, F32, F32, F32, F32, F32, F32, I32, I32],
     "scw_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P],
     "scw_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P],
+    "scw_eval_plane_device_static": [P, I32, F32, F32, F32, F32, I32, P],
     "scw_sep_create": [P, I32, I32, I32, I32, P, P, P, PP],
     "scw_sep_destroy": [P],
     "scw_sep_set_exterior": [P, P, P, P, P, P, P],

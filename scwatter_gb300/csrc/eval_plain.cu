@@ -649,3 +649,293 @@ scw_status scw_gpu_cw_evaluate(scw_waves w, float* E_xy, float* E_xz, float* E_y
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------
+// Allocation-free plane evaluation
+//
+// For callers that must not allocate GPU memory while they run: a host application that
+// sub-allocates one pre-sized pool for everything and treats any other cudaMalloc as a
+// leak, a real-time viewer that may not stall on the allocator in its frame loop, or a
+// plug-in host that forbids its plug-ins from allocating device memory.  The entry point
+// below evaluates one plane like scw_eval_plane_device but takes its split-K scratch from
+// a fixed array compiled into this library, passes its tiny descriptor tables as kernel
+// parameters, and calls no cudaMalloc, cudaMallocHost, cudaFree or allocating library
+// routine.
+// ------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace scw {
+
+constexpr int kStaticMaxLayers = 160;   // layer thresholds carried as kernel parameters
+constexpr int kStaticMaxN = 16384;      // plane edge
+constexpr int kStaticMaxSplit = 64;
+constexpr int kStaticSlots = 1024;      // partial-sum tiles held by the scratch array
+constexpr size_t kStaticScratchFloats = (size_t)kStaticSlots * kTilePts * 6;   // 12 MiB
+
+// Split-K partial sums of the allocation-free path.  Every GPU that loads this library holds
+// this array until the process exits.  Host code must not use its name as a pointer: on the
+// host it is only a stand-in for the symbol, and its device address comes from
+// cudaGetSymbolAddress (static_scratch below).
+static __device__ __align__(256) float g_static_partials[kStaticScratchFloats];
+
+struct StaticRegions {
+    long long begin[kStaticMaxLayers + 1];
+    long long end[kStaticMaxLayers + 1];
+    float z[kStaticMaxLayers];
+    int layers;
+    int rule;
+};
+
+__device__ __forceinline__ int static_region_of(const StaticRegions& R, float z) {
+    // same rule as region_of on the host: the last satisfied threshold wins
+    int l = 0;
+    const double zd = (double)z;
+    for (int li = 0; li < R.layers; li++) {
+        const double thr = (R.rule == 0) ? (double)R.z[li] - 0.001 : (double)R.z[li];
+        if (zd >= thr) l = li + 1;
+    }
+    return l;
+}
+
+// One CTA = one 16 x 32 tile and one of `split` parts of the wave list of every region its
+// rows fall in.  split == 1: the CTA writes the output; otherwise partial slot
+// (tile * split + part) of `partials`, every float of it, so nothing has to start at zero.
+__global__ void __launch_bounds__(kThreads, 4)
+plain_eval_static_kernel(const __grid_constant__ StaticRegions R, PlaneGeom g, int tiles_i, int split, WaveSoA W,
+                         float* __restrict__ partials) {
+    __shared__ StagedWave sw[kBatch];
+    __shared__ double tot[12][kThreads];
+    __shared__ int row_region[kTJ];
+    const int tile = blockIdx.x;
+    const int part = blockIdx.y;
+    const int ti0 = (tile % tiles_i) * kTI, tj0 = (tile / tiles_i) * kTJ;
+    const int t = threadIdx.x;
+    const int li = t & 15;
+    const int lj = t >> 4;
+    const int i = ti0 + li;
+    const int j0 = tj0 + lj;
+    const int j1 = j0 + 16;
+
+    const float ac = grid_coord(g.a0, g.da, ti0 + 8), bc = grid_coord(g.b0, g.db, tj0 + 16);
+    const float dA = (float)((double)grid_coord(g.a0, g.da, i) - (double)ac);
+    const float dB0 = (float)((double)grid_coord(g.b0, g.db, j0) - (double)bc);
+    const float dB1 = (float)((double)grid_coord(g.b0, g.db, j1) - (double)bc);
+    float xc, yc, zc;
+    to_xyz(g.mode, ac, bc, g.c, xc, yc, zc);
+    const int cA = (g.mode == 1) ? 1 : 0;
+    const int cB = (g.mode == 0) ? 1 : 2;
+
+    if (t < kTJ) {
+        const int j = tj0 + t;
+        row_region[t] = (j < g.Nj) ? static_region_of(R, g.mode == 0 ? g.c : grid_coord(g.b0, g.db, j)) : -1;
+    }
+#pragma unroll
+    for (int c = 0; c < 12; c++) tot[c][t] = 0.0;
+    __syncthreads();
+
+    const double two_pi_hi = 6.283185307179586232;
+    const double two_pi_lo = 2.4492935982947064e-16;
+    const double inv_two_pi = 0.15915494309189533577;
+    const float log2e = 1.44269504088896341f;
+
+    // runs of consecutive rows in one region; the loop bounds come from shared memory, so
+    // every thread of the CTA takes the same path
+    int row = 0;
+    while (row < kTJ && row_region[row] >= 0) {
+        const int r = row_region[row];
+        int re = row + 1;
+        while (re < kTJ && row_region[re] == r) re++;
+        const bool in0 = lj >= row && lj < re;
+        const bool in1 = lj + 16 >= row && lj + 16 < re;
+        const long long b = R.begin[r], e = R.end[r];
+        long long chunk = (e - b + split - 1) / split;
+        chunk = (chunk + kBatch - 1) / kBatch * kBatch;
+        const long long w0 = min(e, b + (long long)part * chunk), w1 = min(e, w0 + chunk);
+        for (long long wb = w0; wb < w1; wb += kBatch) {
+            const int nw = (int)min((long long)kBatch, w1 - wb);
+            int cplx = 0;
+            if (t < nw) {
+                const long long w = wb + t;
+                const long long n = W.n;
+                const double krx = W.kre[w], kry = W.kre[n + w], krz = W.kre[2 * n + w];
+                const double kix = W.kim[w], kiy = W.kim[n + w], kiz = W.kim[2 * n + w];
+                const double rx = (double)xc, ry = (double)yc, rz = (double)zc - W.zref[w];
+                double th = fma(krz, rz, fma(kry, ry, krx * rx));
+                const double q = rint(th * inv_two_pi);
+                th = fma(-q, two_pi_lo, fma(-q, two_pi_hi, th));
+                const double ach = -fma(kiz, rz, fma(kiy, ry, kix * rx));
+                const float m = exp2f((float)(ach * 1.4426950408889634074));
+                const float2 ax = W.amp[w], ay = W.amp[n + w], az = W.amp[2 * n + w];
+                const double krA = cA == 0 ? krx : kry, krB = cB == 1 ? kry : krz;
+                const double kiA = cA == 0 ? kix : kiy, kiB = cB == 1 ? kiy : kiz;
+                StagedWave s;
+                s.a = make_float4((float)th, (float)krA, (float)krB, -(float)kiA * log2e);
+                s.x = make_float4(ax.x * m, ax.x * m, ax.y * m, ax.y * m);
+                s.y = make_float4(ay.x * m, ay.x * m, ay.y * m, ay.y * m);
+                s.z = make_float4(az.x * m, az.x * m, az.y * m, az.y * m);
+                s.b = make_float4(-(float)kiB * log2e, 0.f, 0.f, 0.f);
+                sw[t] = s;
+                cplx = (kiA != 0.0) | (kiB != 0.0);
+            }
+            cplx = __syncthreads_or(cplx);
+            PointAcc a0, a1;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                a0.p[c] = a0.q[c] = a1.p[c] = a1.q[c] = make_float2(0.f, 0.f);
+            }
+            if (cplx)
+                accumulate_batch<true>(sw, nw, dA, dB0, dB1, a0, a1);
+            else
+                accumulate_batch<false>(sw, nw, dA, dB0, dB1, a0, a1);
+            if (in0) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    tot[2 * c][t] += (double)(a0.p[c].x - a0.q[c].y);
+                    tot[2 * c + 1][t] += (double)(a0.p[c].y + a0.q[c].x);
+                }
+            }
+            if (in1) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    tot[6 + 2 * c][t] += (double)(a1.p[c].x - a1.q[c].y);
+                    tot[7 + 2 * c][t] += (double)(a1.p[c].y + a1.q[c].x);
+                }
+            }
+            __syncthreads();
+        }
+        row = re;
+    }
+
+    if (split == 1) {
+        if (i < g.Ni) {
+            if (j0 < g.Nj) {
+                float* o = g.out + 6 * ((long long)j0 * g.Ni + i);
+#pragma unroll
+                for (int c = 0; c < 6; c++) o[c] = (float)tot[c][t];
+            }
+            if (j1 < g.Nj) {
+                float* o = g.out + 6 * ((long long)j1 * g.Ni + i);
+#pragma unroll
+                for (int c = 0; c < 6; c++) o[c] = (float)tot[6 + c][t];
+            }
+        }
+    } else {
+        float* p = partials + ((long long)tile * split + part) * kTilePts * 6;
+        float* p0 = p + 6 * (lj * kTI + li);
+        float* p1 = p + 6 * ((lj + 16) * kTI + li);
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            p0[c] = (float)tot[c][t];
+            p1[c] = (float)tot[6 + c][t];
+        }
+    }
+}
+
+// adds the `split` partial slots of each tile in a fixed order, in FP64
+__global__ void __launch_bounds__(kThreads)
+plain_reduce_static_kernel(PlaneGeom g, int tiles_i, int split, const float* __restrict__ partials) {
+    const int tile = blockIdx.x;
+    const int ti0 = (tile % tiles_i) * kTI, tj0 = (tile / tiles_i) * kTJ;
+    for (int q = threadIdx.x; q < kTilePts; q += blockDim.x) {
+        const int i = ti0 + q % kTI, j = tj0 + q / kTI;
+        double s[6] = {0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < split; k++) {
+            const float* p = partials + (((long long)tile * split + k) * kTilePts + q) * 6;
+#pragma unroll
+            for (int c = 0; c < 6; c++) s[c] += (double)p[c];
+        }
+        if (i < g.Ni && j < g.Nj) {
+            float* o = g.out + 6 * ((long long)j * g.Ni + i);
+#pragma unroll
+            for (int c = 0; c < 6; c++) o[c] = (float)s[c];
+        }
+    }
+}
+
+// Device address of g_static_partials, looked up once per device with that device current.
+// The first lookup on a device may load this library's GPU module there.
+constexpr int kStaticMaxDevices = 64;
+static std::mutex g_static_mu;
+static float* g_static_ptr[kStaticMaxDevices] = {};
+
+static scw_status static_scratch(int device, float** out) {
+    if (device < 0 || device >= kStaticMaxDevices)
+        return fail(SCW_ERR_ARG, "scw_eval_plane_device_static: device ordinal beyond " +
+                                     std::to_string(kStaticMaxDevices - 1));
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_partials);
+        if (e != cudaSuccess || !p)
+            return fail(SCW_ERR_CUDA, std::string("cudaGetSymbolAddress of the static scratch array: ") +
+                                          cudaGetErrorString(e));
+        g_static_ptr[device] = (float*)p;
+    }
+    *out = g_static_ptr[device];
+    return SCW_OK;
+}
+
+}  // namespace scw
+
+extern "C" {
+
+scw_status scw_eval_plane_device_static(scw_waves w, int axis, float a_start, float b_start, float c, float d, int N,
+                                        float* dE) {
+    using namespace scw;
+    if (!w || !dE || N <= 0 || axis < 0 || axis > 2)
+        return fail(SCW_ERR_ARG, "scw_eval_plane_device_static: bad arguments");
+    if (N > kStaticMaxN)
+        return fail(SCW_ERR_ARG, "scw_eval_plane_device_static: N = " + std::to_string(N) +
+                                     " exceeds the maximum plane edge " + std::to_string(kStaticMaxN));
+    if (w->layers > kStaticMaxLayers)
+        return fail(SCW_ERR_ARG, "scw_eval_plane_device_static: " + std::to_string(w->layers) +
+                                     " layers exceed the maximum of " + std::to_string(kStaticMaxLayers));
+    scw_ctx ctx = w->ctx;
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    float* scratch = nullptr;
+    scw_status st = static_scratch(ctx->device, &scratch);
+    if (st != SCW_OK) return st;
+
+    StaticRegions R;
+    R.layers = w->layers;
+    R.rule = w->rule;
+    for (int l = 0; l < kStaticMaxLayers; l++) R.z[l] = l < w->layers ? w->z_layers[l] : 0.f;
+    for (int l = 0; l <= kStaticMaxLayers; l++) {
+        R.begin[l] = l <= w->layers ? (long long)w->begin[l] : 0;
+        R.end[l] = l <= w->layers ? (long long)w->end[l] : 0;
+    }
+    long long longest = 0;
+    for (int l = 0; l <= w->layers; l++) longest = std::max<long long>(longest, w->end[l] - w->begin[l]);
+
+    PlaneGeom g{};
+    g.a0 = a_start;
+    g.b0 = b_start;
+    g.c = c;
+    g.da = d;
+    g.db = d;
+    g.Ni = N;
+    g.Nj = N;
+    g.mode = axis;
+    g.out = dE;
+    const int tiles_i = (N + kTI - 1) / kTI, tiles_j = (N + kTJ - 1) / kTJ;
+    const int tiles = tiles_i * tiles_j;
+    // split the wave lists so about 24 CTAs per SM run, at least 4 batches per part, and the
+    // partial sums fit the scratch array (planes of more than kStaticSlots tiles run unsplit)
+    int split = (int)std::min<long long>(kStaticMaxSplit, (24LL * ctx->sm_count + tiles - 1) / tiles);
+    split = (int)std::min<long long>(split, std::max<long long>(1, (longest + 4 * kBatch - 1) / (4 * kBatch)));
+    split = std::min(split, std::max(1, kStaticSlots / tiles));
+    split = std::max(split, 1);
+
+    plain_eval_static_kernel<<<dim3((unsigned)tiles, (unsigned)split), kThreads, 0, ctx->stream>>>(
+        R, g, tiles_i, split, WaveSoA{w->kre, w->kim, w->zref, w->amp, (long long)w->n}, scratch);
+    SCW_CUDA_TRY(cudaGetLastError());
+    ctx->launches++;
+    if (split > 1) {
+        plain_reduce_static_kernel<<<(unsigned)tiles, kThreads, 0, ctx->stream>>>(g, tiles_i, split, scratch);
+        SCW_CUDA_TRY(cudaGetLastError());
+        ctx->launches++;
+    }
+    return SCW_OK;
+}
+
+}  // extern "C"

@@ -47,6 +47,7 @@ typedef struct scw_ctx_s* scw_ctx;       /* one CUDA device + one stream + cache
 typedef struct scw_cw_s* scw_cw;         /* host CoupledWaveStructure<double> */
 typedef struct scw_waves_s* scw_waves;   /* device-resident unpacked wave set */
 typedef struct scw_sep_s* scw_sep;       /* device-resident separable (factored) coefficient set */
+typedef struct scw_solution_s* scw_solution; /* result of the per-layer coupled-wave solve */
 
 /* Output-GEMM methods of the separable evaluator */
 #define SCW_SEP_FP32 1      /* FP32 SIMT */
@@ -197,6 +198,41 @@ SCW_API scw_status scw_zgesv(scw_ctx ctx, int n, int nrhs, void* A, void* B, int
 /* eigenvalues W (n) and right eigenvectors V (n x n, column k = eigenvector k) of A (n x n,
  * overwritten); SCW_ERR_NUMERIC if the QR iteration does not converge. */
 SCW_API scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* status_host);
+
+/* ---------------------------------------------------------------------------------- */
+/* Per-layer coupled-wave solve (FP64, on the GPU) -- the computation of the reference  */
+/* program sCWatter (sCWatter.cpp:569-956; its options sCWatter.cpp:506-527).           */
+/* ---------------------------------------------------------------------------------- */
+typedef struct scw_solve_params {
+    double lambda;        /* --lambda: vacuum wavelength */
+    double direction[3];  /* --direction: incident direction (normalised here) */
+    double ex[2], ey[2], ez[2]; /* --ex/--ey/--ez: incident field components (re, im) */
+    double n[2];          /* --n: real refractive index of the upper and lower media */
+    double kappa;         /* --kappa: absorbance of the lower medium */
+    double size[3];       /* --size: sample extent x, y, z */
+    double z;             /* --z: sample centre along z */
+    int coef[2];          /* --coef: harmonics along x, y (<= 0: the sample's X, Y) */
+    int external;         /* --external: keep only the exterior waves */
+    int pz;               /* 1 = compute Ez of the modes; 0 = the reference's --npz */
+} scw_solve_params;
+
+/* sample: [Z][Y][X] complex128 refractive index in HOST memory (the .npy volume).  Runs the
+ * whole solve on the context's device and blocks until it is done.  SCW_ERR_NUMERIC when an
+ * eigen-solve does not converge or a mode / boundary matrix is singular. */
+SCW_API scw_status scw_solve(scw_ctx ctx, const double* sample, int Z, int Y, int X, const scw_solve_params* prm,
+                             scw_solution* out);
+SCW_API scw_status scw_solution_destroy(scw_solution s);
+SCW_API scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_slices, double* k);
+/* gamma: Z x 2MF complex downward roots (the reference's even-slot eigenvalues); x: 6MF
+ * complex reflected / transmitted amplitudes (sCWatter.cpp:722); ef: 3MF incident Fourier
+ * amplitudes; z_boundaries: Z + 1.  Any pointer may be NULL. */
+SCW_API scw_status scw_solution_get(scw_solution s, double* gamma, double* x, double* ef, double* z_boundaries);
+/* Q_check / Q_hat of slice l: 3MF x 2MF complex each (row-major; rows Ex, Ey, Ez blocks). */
+SCW_API scw_status scw_solution_get_modes(scw_solution s, int l, double* Q_check, double* Q_hat);
+/* Separable coefficient set for the evaluators, on the solution's device. */
+SCW_API scw_status scw_solution_to_sep(scw_solution s, scw_sep* out);
+/* The .cw structure that sCWatter writes (sCWatter.cpp:890-956). */
+SCW_API scw_status scw_solution_to_cw(scw_solution s, scw_cw* out);
 
 #ifdef __cplusplus
 }

@@ -63,6 +63,13 @@ _SIGS = {
     "scw_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P],
     "scw_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P],
     "scw_eval_plane_device_static": [P, I32, F32, F32, F32, F32, I32, P],
+    "scw_solve": [P, P, I32, I32, I32, P, PP],
+    "scw_solution_destroy": [P],
+    "scw_solution_info": [P, P, P, P, P],
+    "scw_solution_get": [P, P, P, P, P],
+    "scw_solution_get_modes": [P, I32, P, P],
+    "scw_solution_to_sep": [P, PP],
+    "scw_solution_to_cw": [P, PP],
     "scw_sep_create": [P, I32, I32, I32, I32, P, P, P, PP],
     "scw_sep_destroy": [P],
     "scw_sep_set_exterior": [P, P, P, P, P, P, P],

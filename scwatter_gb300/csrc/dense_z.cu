@@ -403,6 +403,14 @@ hqr_kernel(double2* __restrict__ H, double2* __restrict__ Z, int n, long long sA
                         l = k;
                         break;
                     }
+                    // coincident diagonal entries (bb = 0 above): zeroing the subdiagonal moves
+                    // the two eigenvalues by at most sqrt(|h(k,k-1) h(k-1,k)|), below rounding
+                    // of h(k,k) when this holds (a diagonal matrix with repeated eigenvalues
+                    // and rounding-level couplings would otherwise never deflate)
+                    if (ba * ab <= (ulp * cabs1(hkk)) * (ulp * cabs1(hkk))) {
+                        l = k;
+                        break;
+                    }
                 }
             }
             s_l = l;
@@ -425,15 +433,16 @@ hqr_kernel(double2* __restrict__ H, double2* __restrict__ Z, int n, long long sA
         }
         its++;
         total++;
+        // exceptional shifts every 10 iterations without a deflation (zlahqr's KEXSH rule)
         // shift
         if (threadIdx.x == 0) {
             double2 t;
             const double2 hii = H[(long long)ihi * n + ihi];
-            if (its == 10) {
+            if (its % 20 == 0) {
+                t = make_double2(0.75 * fabs(H[(long long)ihi * n + ihi - 1].x) + hii.x, hii.y);
+            } else if (its % 10 == 0) {
                 t = make_double2(0.75 * fabs(H[(long long)(l + 1) * n + l].x) + H[(long long)l * n + l].x,
                                  H[(long long)l * n + l].y);
-            } else if (its == 20) {
-                t = make_double2(0.75 * fabs(H[(long long)ihi * n + ihi - 1].x) + hii.x, hii.y);
             } else {
                 // Wilkinson shift from the trailing 2x2 block
                 const double2 a = H[(long long)(ihi - 1) * n + ihi - 1];
@@ -444,11 +453,7 @@ hqr_kernel(double2* __restrict__ H, double2* __restrict__ Z, int n, long long sA
                 const double2 bc = cmul(b, c);
                 const double2 disc = cfma(half, half, bc);
                 // complex sqrt
-                const double r = sqrt(cabs2(disc));
-                double sr = sqrt(fmax(0.0, 0.5 * (r + disc.x)));
-                double si = sqrt(fmax(0.0, 0.5 * (r - disc.x)));
-                if (disc.y < 0) si = -si;
-                double2 sq = make_double2(sr, si);
+                const double2 sq = zsqrt(disc);
                 // choose the root that makes the shift closer to d
                 double2 e1 = cadd(half, sq), e2 = csub(half, sq);
                 const double2 den = cabs2(e1) >= cabs2(e2) ? e1 : e2;

@@ -8,6 +8,17 @@
 
 namespace scw {
 
+#ifdef __CUDACC__
+// principal square root without cancellation: the larger of |Re|, |Im| of the root comes from
+// sqrt((|Re a| + |a|) / 2), the other from Im a / (2 x)
+__device__ __forceinline__ double2 zsqrt(double2 a) {
+    if (a.x == 0.0 && a.y == 0.0) return make_double2(0.0, 0.0);
+    const double t = sqrt(0.5 * (fabs(a.x) + hypot(a.x, a.y)));
+    if (a.x >= 0.0) return make_double2(t, a.y / (2.0 * t));
+    return make_double2(fabs(a.y) / (2.0 * t), copysign(t, a.y));
+}
+#endif
+
 // C = alpha A B + beta C (row-major, batched by strides in elements)
 scw_status zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2* A, int lda, long long sA,
                  const double2* B, int ldb, long long sB, double2 beta, double2* C, int ldc, long long sC, int batch);

@@ -1,0 +1,897 @@
+// Per-layer coupled-wave solve on the GPU in FP64: the computation of the reference program
+// sCWatter (sCWatter.cpp:569-885, FourierWave.h:152-397), producing the reflected and
+// transmitted amplitudes and the per-slice mode amplitudes that the evaluators consume.
+//
+// Reduced eigenproblem.  Per slice the reference builds the 4MF x 4MF matrix
+// Phi = [[0, P], [Q, 0]] (FourierWave.h:336-397) and runs zgeev on it.  Phi^2 = diag(PQ, QP),
+// so here the 2MF x 2MF matrix PQ is decomposed instead: PQ u = lambda u gives the two Phi
+// modes gamma = +-sqrt(lambda) with eigenvectors [u; +-Q u / gamma].  The member the
+// reference files in its even ("downward") slots, i.e. the larger imaginary part
+// (sCWatter.cpp:185-225), is the root with Im > 0 (Re > 0 when Im == 0).  With U = [u_j],
+// W = [Q u_j / gamma_j], E = diag(exp(i k gamma dz)) and V = [[U, U], [W, -W]]:
+//   Gd = V diag(I, E),  Gc = V diag(E, I)                         (sCWatter.cpp:281-316)
+//   V^-1 = 1/2 [[U^-1, W^-1], [U^-1, -W^-1]]
+// so every product with Gd, Gc or their inverses is two 2MF GEMMs plus an elementwise mix.
+//
+// Boundary system.  The reference forms Gc_static = Gc_{Z-1} Gd_{Z-1}^-1 ... Gc_1 Gd_1^-1 Gc_0
+// (sCWatter.cpp:321-330) and then needs Gd_0 Gc_static^-1 f3 (:393-461).  That product equals
+//   prod_{l = 0 .. Z-1} [V_l diag(E_l^-1, E_l) V_l^-1]  f3
+// which is applied here from the right to the 4MF x 3MF matrix f3: no 4MF x 4MF matrix is
+// formed or inverted.  The 6MF system (:722), the beta recursion (:743-777), Q_check / Q_hat
+// and the Ez rows from the magnetic field (:781-871) follow the reference, including its index
+// conventions (column-major flattening of the Sx / Sy meshes, wrapped harmonic differences,
+// the column-major read of the 1/n^2 coefficients in the Ez step).
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include "scw_dense.h"
+#include "scw_sep.h"
+
+using cd = std::complex<double>;
+
+struct scw_solution_s {
+    scw_ctx ctx = nullptr;
+    int M0 = 0, M1 = 0, MF = 0, Z = 0;
+    double k = 0, n0 = 1, n1 = 1;
+    bool external = false;
+    std::vector<double> zb;                // Z + 1 boundaries
+    std::vector<double> Sx, Sy;            // direction components of the flattened meshes
+    std::vector<cd> Sz0, Sz1, EF, x;       // MF, MF, 3MF incident, 6MF boundary solution
+    std::vector<cd> gam;                   // Z x 2MF downward roots
+    double2* dQ = nullptr;                 // device [Z][2][3MF][2MF]: Q_check, Q_hat (FP64)
+    ~scw_solution_s() {
+        if (dQ) {
+            cudaSetDevice(ctx->device);
+            cudaFree(dQ);
+        }
+    }
+};
+
+namespace scw {
+namespace sv {
+
+constexpr double kPiRef = 3.141592653;     // the reference's PI (FourierWave.h:18)
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cinv(double2 a) {
+    const double d = a.x * a.x + a.y * a.y;
+    return make_double2(a.x / d, -a.y / d);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 chalf(double2 a) { return make_double2(0.5 * a.x, 0.5 * a.y); }
+
+// n^2 and n^-2 of every sample value, two planes per slice
+__global__ void n2_kernel(const double2* __restrict__ data, long long per, int Z, double2* __restrict__ F) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= per * Z) return;
+    const int l = (int)(e / per);
+    const long long i = e % per;
+    const double2 n = data[e];
+    const double2 n2 = cmul(n, n);
+    F[(2LL * l) * per + i] = n2;
+    F[(2LL * l + 1) * per + i] = cinv(n2);
+}
+
+// P (rows Ex, Ey; columns Hx, Hy) and Q (rows Hx, Hy; columns Ex, Ey) of Phi
+// (FourierWave.h:359-394); harmonic m = q M0 + p.  coef: per slice the M1 x M0 crops of
+// n^2 and n^-2, stored column-major (index a + b M1).
+__global__ void build_pq_kernel(const double2* __restrict__ coef, const double* __restrict__ up,
+                                const double* __restrict__ wq, const int* __restrict__ qs, const int* __restrict__ ps,
+                                int M0, int M1, double k, double2* __restrict__ P, double2* __restrict__ Qm) {
+    const int l = blockIdx.z;
+    const int MF = M0 * M1, n = 2 * MF;
+    const int i = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double2* Nf = coef + (long long)l * 2 * MF;
+    const double2* Ni = Nf + MF;
+    const int mi = i % MF, mj = j % MF;
+    const int qi = mi / M0, pi_ = mi % M0, qj = mj / M0, pj = mj % M0;
+    // wrapped index differences with C++ remainders (FourierWave.h:366-372)
+    const int R = ((((qs[qi] % M1) - (qs[qj] % M1) + M1) % M1) + M1 / 2) % M1;
+    const int C = ((((ps[pi_] % M0) - (ps[pj] % M0) + M0) % M0) + M0 / 2) % M0;
+    const double2 nf = Nf[R + C * M1], ni = Ni[R + C * M1];
+    const double kin = 1.0 / (k * k);
+    const double upi = up[pi_], wqi = wq[qi], upj = up[pj], wqj = wq[qj];
+    const bool bi = i >= MF, bj = j >= MF;
+    const double d = (mi == mj) ? 1.0 : 0.0;
+    double2 p, q;
+    if (!bi && !bj) p = make_double2(upi * kin * wqj * ni.x, upi * kin * wqj * ni.y);
+    else if (!bi && bj) p = make_double2(-upi * kin * upj * ni.x + d, -upi * kin * upj * ni.y);
+    else if (bi && !bj) p = make_double2(wqi * kin * wqj * ni.x - d, wqi * kin * wqj * ni.y);
+    else p = make_double2(-wqi * kin * upj * ni.x, -wqi * kin * upj * ni.y);
+    if (!bi && !bj) q = make_double2(-upi * wqi * kin * d, 0.0);
+    else if (!bi && bj) q = make_double2(-nf.x + upi * upi * kin * d, -nf.y);
+    else if (bi && !bj) q = make_double2(nf.x - wqi * wqi * kin * d, nf.y);
+    else q = make_double2(upi * wqi * kin * d, 0.0);
+    const long long o = ((long long)l * n + i) * n + j;
+    P[o] = p;
+    Qm[o] = q;
+}
+
+// gamma = sqrt(lambda) with Im > 0 (Re > 0 when Im == 0);  E = exp(i k gamma dz)
+__global__ void roots_kernel(const double2* __restrict__ lam, int n, int Z, const double* __restrict__ dz, double k,
+                             double2* __restrict__ gam, double2* __restrict__ E) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)n * Z) return;
+    const int l = (int)(e / n);
+    const double2 root = zsqrt(lam[e]);
+    double gr = root.x, gi = root.y;
+    if (gi < 0 || (gi == 0 && gr < 0)) {
+        gr = -gr;
+        gi = -gi;
+    }
+    gam[e] = make_double2(gr, gi);
+    const double m = exp(-k * gi * dz[l]);
+    double s, c;
+    sincos(k * gr * dz[l], &s, &c);
+    E[e] = make_double2(m * c, m * s);
+}
+
+// X[b][:, j] /= f[b][j]
+__global__ void coldiv_kernel(double2* __restrict__ X, int n, const double2* __restrict__ f, int batch) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)n * n;
+    if (e >= per * batch) return;
+    const int b = (int)(e / per), j = (int)(e % n);
+    X[e] = cmul(X[e], cinv(f[(long long)b * n + j]));
+}
+
+__global__ void identity_kernel(double2* __restrict__ X, int n, int batch) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)n * n;
+    if (e >= per * batch) return;
+    const long long r = e % per;
+    X[e] = make_double2((r / n) == (r % n) ? 1.0 : 0.0, 0.0);
+}
+
+// [Yt; Yb] from A1 = U^-1 Xt, A2 = W^-1 Xb (rows i scaled by E_i):
+//   mode 0 (Gd Gc^-1 step):  Yt = E^-1 (A1 + A2)/2,  Yb = E (A1 - A2)/2,
+//                            then St = Yt + Yb,  Sb = Yt - Yb   (written over A1, A2)
+//   mode 1 (Gd^-1):          A1 <- (A1 + A2)/2,  A2 <- E^-1 (A1 - A2)/2
+//   mode 2 (Gc):             A1 <- E A1 + A2,    A2 <- E A1 - A2
+__global__ void mix_kernel(double2* __restrict__ A1, double2* __restrict__ A2, const double2* __restrict__ E, int n,
+                           int ncol, int mode) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)n * ncol) return;
+    const int i = (int)(e / ncol);
+    const double2 a1 = A1[e], a2 = A2[e], Ei = E[i];
+    if (mode == 0) {
+        const double2 yt = cmul(cinv(Ei), chalf(cadd(a1, a2)));
+        const double2 yb = cmul(Ei, chalf(csub(a1, a2)));
+        A1[e] = cadd(yt, yb);
+        A2[e] = csub(yt, yb);
+    } else if (mode == 1) {
+        A1[e] = chalf(cadd(a1, a2));
+        A2[e] = cmul(cinv(Ei), chalf(csub(a1, a2)));
+    } else {
+        const double2 ea = cmul(Ei, a1);
+        A1[e] = cadd(ea, a2);
+        A2[e] = csub(ea, a2);
+    }
+}
+
+// f3 (4MF x 3MF, sCWatter.cpp:372-389)
+__global__ void f3_kernel(const double* __restrict__ Sx, const double* __restrict__ Sy, const double2* __restrict__ Sz1,
+                          int MF, double2* __restrict__ F) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ncol = 3 * MF;
+    if (e >= 4LL * MF * ncol) return;
+    const int r = (int)(e / ncol), c = (int)(e % ncol);
+    const int blk = r / MF, m = r % MF;
+    double2 v = make_double2(0, 0);
+    if (blk == 0 && c == m) v = make_double2(-1, 0);
+    else if (blk == 1 && c == MF + m) v = make_double2(-1, 0);
+    else if (blk == 2 && c == MF + m) v = Sz1[m];
+    else if (blk == 2 && c == 2 * MF + m) v = make_double2(-Sy[m], 0);
+    else if (blk == 3 && c == m) v = make_double2(-Sz1[m].x, -Sz1[m].y);
+    else if (blk == 3 && c == 2 * MF + m) v = make_double2(Sx[m], 0);
+    F[e] = v;
+}
+
+// the 6MF x 6MF boundary matrix (sCWatter.cpp:143-146, 393-461): divergence constraints,
+// then [f2 | T3] with T3 = Gd_0 Gc_static^-1 f3 (4MF x 3MF)
+__global__ void bc_matrix_kernel(const double* __restrict__ Sx, const double* __restrict__ Sy,
+                                 const double2* __restrict__ Sz0, const double2* __restrict__ Sz1,
+                                 const double2* __restrict__ T3, int MF, double2* __restrict__ A) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int N6 = 6 * MF;
+    if (e >= (long long)N6 * N6) return;
+    const int r = (int)(e / N6), c = (int)(e % N6);
+    double2 v = make_double2(0, 0);
+    if (r < MF) {
+        const int m = r;
+        if (c == m) v = make_double2(Sx[m], 0);
+        else if (c == MF + m) v = make_double2(Sy[m], 0);
+        else if (c == 2 * MF + m) v = make_double2(-Sz0[m].x, -Sz0[m].y);
+    } else if (r < 2 * MF) {
+        const int m = r - MF;
+        if (c == 3 * MF + m) v = make_double2(Sx[m], 0);
+        else if (c == 4 * MF + m) v = make_double2(Sy[m], 0);
+        else if (c == 5 * MF + m) v = Sz1[m];
+    } else {
+        const int rr = r - 2 * MF;
+        if (c >= 3 * MF) {
+            v = T3[(long long)rr * 3 * MF + (c - 3 * MF)];
+        } else {
+            const int blk = rr / MF, m = rr % MF;
+            if (blk == 0 && c == m) v = make_double2(1, 0);
+            else if (blk == 1 && c == MF + m) v = make_double2(1, 0);
+            else if (blk == 2 && c == MF + m) v = Sz0[m];
+            else if (blk == 2 && c == 2 * MF + m) v = make_double2(Sy[m], 0);
+            else if (blk == 3 && c == m) v = make_double2(-Sz0[m].x, -Sz0[m].y);
+            else if (blk == 3 && c == 2 * MF + m) v = make_double2(-Sx[m], 0);
+        }
+    }
+    A[e] = v;
+}
+
+// Kn[m_i][m_j] = scale * NIf[lin] with lin the wrapped difference index read column-major
+// (sCWatter.cpp:839-871 reads NIf(lin) on a column-major Eigen matrix)
+__global__ void kn_kernel(const double2* __restrict__ NiF, int M0, int M1, double scale, double2* __restrict__ Kn) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int MF = M0 * M1;
+    if (e >= (long long)MF * MF) return;
+    const int mi = (int)(e / MF), mj = (int)(e % MF);
+    const int qi = mi / M0, pi_ = mi % M0, qj = mj / M0, pj = mj % M0;
+    const int lin = (((qi - qj + M1) % M1 + M1 / 2) % M1) * M0 + ((pi_ - pj + M0) % M0 + M0 / 2) % M0;
+    const double2 v = NiF[lin];
+    Kn[e] = make_double2(v.x * scale, v.y * scale);
+}
+
+// rows Ex, Ey of Q_check / Q_hat: U diag(beta);  Hm = sign (up_m Hy - wq_m Hx) for the Ez step,
+// with Hx, Hy = rows of W diag(beta) (sign -1 for the upward modes, whose H rows are -W)
+__global__ void q_rows_kernel(const double2* __restrict__ U, const double2* __restrict__ Wm,
+                              const double2* __restrict__ beta, int MF, double sign, const double* __restrict__ up_pz,
+                              const double* __restrict__ wq_pz, double2* __restrict__ Qout, double2* __restrict__ Hm) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = 2 * MF;
+    if (e >= (long long)n * n) return;
+    const int r = (int)(e / n), j = (int)(e % n);
+    const double2 b = beta[j];
+    Qout[e] = cmul(U[e], b);
+    if (Hm && r < MF) {
+        const double2 hx = cmul(Wm[e], b);
+        const double2 hy = cmul(Wm[(long long)(MF + r) * n + j], b);
+        Hm[e] = make_double2(sign * (up_pz[r] * hy.x - wq_pz[r] * hx.x), sign * (up_pz[r] * hy.y - wq_pz[r] * hx.y));
+    }
+}
+
+__global__ void to_c64_kernel(const double2* __restrict__ a, float2* __restrict__ b, long long n) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) b[e] = make_float2((float)a[e].x, (float)a[e].y);
+}
+
+static unsigned nblk(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// FourierWave.h:82-145: the source index of each shifted row / column, including the column
+// index it builds when the row count is even and the column count odd
+static void fft_shift_index(int m, int n, std::vector<int>& indx, std::vector<int>& indy) {
+    int p, q;
+    if (m % 2 == 1) {
+        p = m / 2;
+        q = n / 2;
+    } else {
+        p = (m + 1) / 2;
+        q = (n + 1) / 2;
+    }
+    indx.resize(m);
+    indy.resize(n);
+    for (int i = 0; i < m; i++) {
+        if (m % 2 == 1) indx[i] = i < m - p - 1 ? (m - p) + i : i - (m - p - 1);
+        else indx[i] = i < m - p ? p + i : i - (m - p);
+    }
+    for (int i = 0; i < n; i++) {
+        if (n % 2 == 1) indy[i] = i < n - q - 1 ? (n - q) + i : i - (n - q - 1);
+        else indy[i] = i < n - q ? q + i : i - (n - q);
+    }
+}
+
+struct DevMem {
+    int device;
+    std::vector<void*> ptrs;
+    explicit DevMem(int dev) : device(dev) {}
+    ~DevMem() {
+        cudaSetDevice(device);
+        for (void* p : ptrs) cudaFree(p);
+    }
+    template <typename T>
+    T* get(size_t n) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        ptrs.push_back(p);
+        return (T*)p;
+    }
+    void release(void* p) {
+        auto it = std::find(ptrs.begin(), ptrs.end(), p);
+        if (it != ptrs.end()) {
+            cudaFree(p);
+            ptrs.erase(it);
+        }
+    }
+};
+
+#define SCW_TRY(expr)                          \
+    do {                                       \
+        const scw_status s_ = (expr);          \
+        if (s_ != SCW_OK) return s_;           \
+    } while (0)
+
+#define SCW_NEED(ptr)                                                               \
+    do {                                                                            \
+        if (!(ptr)) return fail(SCW_ERR_NOMEM, "scw_solve: cudaMalloc of " #ptr);  \
+    } while (0)
+
+const double2 kOne = {1.0, 0.0};
+const double2 kZero = {0.0, 0.0};
+
+}  // namespace sv
+}  // namespace scw
+
+using scw::fail;
+
+extern "C" {
+
+scw_status scw_solution_destroy(scw_solution s) {
+    delete s;
+    return SCW_OK;
+}
+
+// sCWatter main (sCWatter.cpp:569-885) on the context's GPU.
+scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, const scw_solve_params* prm,
+                     scw_solution* out) {
+    using namespace scw;
+    using namespace scw::sv;
+    if (!ctx || !sample || !prm || !out || Zs < 1 || Y < 1 || X < 1) return fail(SCW_ERR_ARG, "scw_solve: bad arguments");
+    *out = nullptr;
+    if (!(prm->lambda > 0) || !(prm->size[0] > 0) || !(prm->size[1] > 0) || !(prm->size[2] > 0))
+        return fail(SCW_ERR_ARG, "scw_solve: wavelength and sizes must be positive");
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+
+    // ---- geometry and incident field (sCWatter.cpp:569-680) ----
+    const double dn = std::sqrt(prm->direction[0] * prm->direction[0] + prm->direction[1] * prm->direction[1] +
+                                prm->direction[2] * prm->direction[2]);
+    if (!(dn > 0)) return fail(SCW_ERR_ARG, "scw_solve: zero direction");
+    const double dvec[3] = {prm->direction[0] / dn, prm->direction[1] / dn, prm->direction[2] / dn};
+    cd e[3] = {cd(prm->ex[0], prm->ex[1]), cd(prm->ey[0], prm->ey[1]), cd(prm->ez[0], prm->ez[1])};
+    {   // orthogonalize (FourierWave.h:32-39): |E| is the complex sqrt of sum(E_i^2)
+        const cd mag = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+        for (auto& c : e) c /= mag;
+        const cd d[3] = {dvec[0], dvec[1], dvec[2]};
+        const cd s[3] = {e[1] * d[2] - e[2] * d[1], e[2] * d[0] - e[0] * d[2], e[0] * d[1] - e[1] * d[0]};
+        e[0] = d[1] * s[2] - d[2] * s[1];
+        e[1] = d[2] * s[0] - d[0] * s[2];
+        e[2] = d[0] * s[1] - d[1] * s[0];
+    }
+    const double n0 = prm->n[0], n1r = prm->n[1];
+    const double dir[3] = {dvec[0] * n0, dvec[1] * n0, dvec[2] * n0};
+    const double k = 2 * kPiRef / prm->lambda;
+    const cd ni0(n0, 0.0), ni1(n1r, prm->kappa);
+    const int ZL = Zs + 1;
+    std::vector<double> zb(ZL);
+    zb[0] = prm->z - prm->size[2] / 2.0;
+    for (int i = 1; i < ZL; i++) zb[i] = zb[i - 1] + prm->size[2] / Zs;
+    int M0 = prm->coef[0] > 0 ? prm->coef[0] : X, M1 = prm->coef[1] > 0 ? prm->coef[1] : Y;
+    {   // harmonic count clamping (sCWatter.cpp:607-645)
+        const double lam = prm->lambda;
+        auto sq = [](double v) { return v * v; };
+        if (sq(double(M0 / 2) / prm->size[0] * lam + dir[0]) + sq(double(M1 / 2) / prm->size[1] * lam + dir[1]) >=
+            n0 * n0) {
+            if (M0 != 1 && M1 != 1) {
+                if ((double(M0 / 2) / prm->size[0] * lam + dir[0]) > 0.71 * n0)
+                    M0 = int(0.707 * n0 * 2 * prm->size[0] / lam) - 1;
+                if ((double(M1 / 2) / prm->size[1] * lam + dir[1]) > 0.71 * n0)
+                    M1 = int(0.707 * n1r * 2 * prm->size[1] / lam) - 1;
+            }
+            if (M0 == 1 && (double(M1 / 2) / prm->size[1] * lam + std::fabs(dir[1])) >= n0) {
+                M1 = int(n1r * 2 * prm->size[1] / lam - 1e-10);
+                if (M1 % 2 == 0) M1 -= 1;
+            }
+            if (M1 == 1 && (double(M0 / 2) / prm->size[1] * lam + std::fabs(dir[0])) >= n0) {
+                M0 = int(n0 * 2 * prm->size[0] / lam - 1e-10);
+                if (M0 % 2 == 0) M0 -= 1;
+            }
+        }
+        M0 = std::min(M0, X);
+        M1 = std::min(M1, Y);
+        if (M0 < 1 || M1 < 1) return fail(SCW_ERR_ARG, "scw_solve: no Fourier coefficients left after clamping");
+    }
+    const int MF = M0 * M1, n = 2 * MF, N4 = 4 * MF, M3 = 3 * MF, M6 = 6 * MF;
+    if ((long long)M6 * M6 > (1LL << 31) * 4) return fail(SCW_ERR_ARG, "scw_solve: too many Fourier coefficients");
+    // k grids (FourierWave.h:319-334): integer series -(M/2) .. (M-1)/2
+    std::vector<int> ps(M0), qs(M1);
+    std::vector<double> up(M0), wq(M1);
+    for (int i = 0; i < M0; i++) {
+        ps[i] = -(M0 / 2) + i;
+        up[i] = 2 * kPiRef * ps[i] / prm->size[0] + dir[0] * k;
+    }
+    for (int i = 0; i < M1; i++) {
+        qs[i] = -(M1 / 2) + i;
+        wq[i] = 2 * kPiRef * qs[i] / prm->size[1] + dir[1] * k;
+    }
+    std::unique_ptr<scw_solution_s> sol(new (std::nothrow) scw_solution_s());
+    if (!sol) return fail(SCW_ERR_NOMEM, "host allocation");
+    sol->ctx = ctx;
+    sol->M0 = M0;
+    sol->M1 = M1;
+    sol->MF = MF;
+    sol->Z = Zs;
+    sol->k = k;
+    sol->zb = zb;
+    sol->external = prm->external != 0;
+    sol->n0 = n0;
+    sol->n1 = n1r;
+    sol->Sx.resize(MF);
+    sol->Sy.resize(MF);
+    sol->Sz0.resize(MF);
+    sol->Sz1.resize(MF);
+    for (int f = 0; f < MF; f++) {      // column-major flattening of the M1 x M0 meshes (sCWatter.cpp:677-680)
+        const double sx = up[f / M1] / k, sy = wq[f % M1] / k;
+        sol->Sx[f] = sx;
+        sol->Sy[f] = sy;
+        sol->Sz0[f] = std::sqrt(ni0 * ni0 - cd(sx * sx) - cd(sy * sy));
+        sol->Sz1[f] = std::sqrt(ni1 * ni1 - cd(sx * sx) - cd(sy * sy));
+    }
+    // the DFT rows / columns that land in the centred crop after the shift
+    std::vector<int> ix, iy;
+    fft_shift_index(Y, X, ix, iy);
+    const int r0 = Y / 2 - M1 / 2, c0 = X / 2 - M0 / 2;
+    std::vector<int> du(M1), dv(M0);
+    for (int a = 0; a < M1; a++) du[a] = ix[r0 + a];
+    for (int b = 0; b < M0; b++) dv[b] = iy[c0 + b];
+    // incident field: the transform of a constant lands on the DC bin (sCWatter.cpp:656-674)
+    sol->EF.assign(3 * MF, cd(0, 0));
+    for (int c = 0; c < 3; c++)
+        for (int a = 0; a < M1; a++)
+            for (int b = 0; b < M0; b++)
+                if (du[a] == 0 && dv[b] == 0) sol->EF[c * MF + a + b * M1] = e[c];
+
+    DevMem mem(ctx->device);
+    const long long nn = (long long)n * n;
+    const long long YX = (long long)Y * X;
+
+    // ---- Fourier coefficients of n^2 and n^-2 (FourierWave.h:152-195, 283-301) ----
+    // Slice memory read as the X x Y row-major matrix F^T (F[r][c] = data[r + c Y]); the 2-D
+    // DFT crop is tw2^T (M0 x X) . (F^T (X x Y) . tw1^T (Y x M1)), which comes out as the
+    // M1 x M0 crop stored column-major.
+    double2* d_coef = mem.get<double2>((size_t)Zs * 2 * MF);
+    SCW_NEED(d_coef);
+    {
+        std::vector<double2> tw1((size_t)Y * M1), tw2((size_t)M0 * X);
+        for (int r = 0; r < Y; r++)
+            for (int a = 0; a < M1; a++) {
+                const double t = (double)(((long long)du[a] * r) % Y) / Y;
+                tw1[(size_t)r * M1 + a] = make_double2(std::cos(2 * M_PI * t), -std::sin(2 * M_PI * t));
+            }
+        for (int b = 0; b < M0; b++)
+            for (int c = 0; c < X; c++) {
+                const double t = (double)(((long long)dv[b] * c) % X) / X;
+                tw2[(size_t)b * X + c] = make_double2(std::cos(2 * M_PI * t), -std::sin(2 * M_PI * t));
+            }
+        double2* d_data = mem.get<double2>((size_t)Zs * YX);
+        double2* d_F = mem.get<double2>((size_t)Zs * 2 * YX);
+        double2* d_tw1 = mem.get<double2>(tw1.size());
+        double2* d_tw2 = mem.get<double2>(tw2.size());
+        double2* d_T = mem.get<double2>((size_t)Zs * 2 * X * M1);
+        SCW_NEED(d_data);
+        SCW_NEED(d_F);
+        SCW_NEED(d_tw1);
+        SCW_NEED(d_tw2);
+        SCW_NEED(d_T);
+        SCW_CUDA_TRY(cudaMemcpyAsync(d_data, sample, sizeof(double2) * Zs * YX, cudaMemcpyHostToDevice, st));
+        SCW_CUDA_TRY(cudaMemcpyAsync(d_tw1, tw1.data(), sizeof(double2) * tw1.size(), cudaMemcpyHostToDevice, st));
+        SCW_CUDA_TRY(cudaMemcpyAsync(d_tw2, tw2.data(), sizeof(double2) * tw2.size(), cudaMemcpyHostToDevice, st));
+        n2_kernel<<<nblk(Zs * YX), 256, 0, st>>>(d_data, YX, Zs, d_F);
+        SCW_CUDA_TRY(cudaGetLastError());
+        SCW_TRY(zgemm(st, X, M1, Y, kOne, d_F, Y, YX, d_tw1, M1, 0, kZero, d_T, M1, (long long)X * M1, 2 * Zs));
+        SCW_TRY(zgemm(st, M0, M1, X, make_double2(1.0 / (double)YX, 0.0), d_tw2, X, 0, d_T, M1, (long long)X * M1, kZero,
+                      d_coef, M1, MF, 2 * Zs));
+        SCW_CUDA_TRY(cudaStreamSynchronize(st));
+        mem.release(d_data);
+        mem.release(d_F);
+        mem.release(d_T);
+        mem.release(d_tw1);
+        mem.release(d_tw2);
+    }
+
+    // ---- P, Q and the reduced eigenproblem (FourierWave.h:336-397, sCWatter.cpp:248-272) ----
+    int* d_qs = mem.get<int>(M1);
+    int* d_ps = mem.get<int>(M0);
+    double* d_up = mem.get<double>(M0);
+    double* d_wq = mem.get<double>(M1);
+    double* d_dz = mem.get<double>(Zs);
+    double2* d_P = mem.get<double2>((size_t)Zs * (nn + 3 * n));   // P, then eigen work, then U^-1
+    double2* d_Q = mem.get<double2>((size_t)Zs * nn);             // Q, then LU factors
+    double2* d_PQ = mem.get<double2>((size_t)Zs * nn);            // PQ, then W^-1
+    double2* d_U = mem.get<double2>((size_t)Zs * nn);
+    double2* d_W = mem.get<double2>((size_t)Zs * nn);
+    double2* d_lam = mem.get<double2>((size_t)Zs * n);
+    double2* d_gam = mem.get<double2>((size_t)Zs * n);
+    double2* d_E = mem.get<double2>((size_t)Zs * n);
+    int* d_status = mem.get<int>(Zs);
+    int* d_piv = mem.get<int>((size_t)Zs * n + M6);
+    SCW_NEED(d_qs);
+    SCW_NEED(d_ps);
+    SCW_NEED(d_up);
+    SCW_NEED(d_wq);
+    SCW_NEED(d_dz);
+    SCW_NEED(d_P);
+    SCW_NEED(d_Q);
+    SCW_NEED(d_PQ);
+    SCW_NEED(d_U);
+    SCW_NEED(d_W);
+    SCW_NEED(d_lam);
+    SCW_NEED(d_gam);
+    SCW_NEED(d_E);
+    SCW_NEED(d_status);
+    SCW_NEED(d_piv);
+    std::vector<double> dz(Zs);
+    for (int l = 0; l < Zs; l++) dz[l] = (Zs == 1) ? zb[ZL - 1] - zb[0] : zb[l + 1] - zb[l];
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_qs, qs.data(), sizeof(int) * M1, cudaMemcpyHostToDevice, st));
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_ps, ps.data(), sizeof(int) * M0, cudaMemcpyHostToDevice, st));
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_up, up.data(), sizeof(double) * M0, cudaMemcpyHostToDevice, st));
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_wq, wq.data(), sizeof(double) * M1, cudaMemcpyHostToDevice, st));
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_dz, dz.data(), sizeof(double) * Zs, cudaMemcpyHostToDevice, st));
+    build_pq_kernel<<<dim3(nblk(n), n, Zs), 256, 0, st>>>(d_coef, d_up, d_wq, d_qs, d_ps, M0, M1, k, d_P, d_Q);
+    SCW_CUDA_TRY(cudaGetLastError());
+    SCW_TRY(zgemm(st, n, n, n, kOne, d_P, n, nn, d_Q, n, nn, kZero, d_PQ, n, nn, Zs));
+    SCW_TRY(zgeev(st, d_PQ, d_lam, d_U, n, Zs, d_P, d_status));
+    std::vector<int> status(Zs);
+    SCW_CUDA_TRY(cudaMemcpyAsync(status.data(), d_status, sizeof(int) * Zs, cudaMemcpyDeviceToHost, st));
+    SCW_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int l = 0; l < Zs; l++)
+        if (status[l]) return fail(SCW_ERR_NUMERIC, "scw_solve: eigen-solver did not converge for slice " + std::to_string(l));
+    roots_kernel<<<nblk((long long)n * Zs), 256, 0, st>>>(d_lam, n, Zs, d_dz, k, d_gam, d_E);
+    SCW_CUDA_TRY(cudaGetLastError());
+    // W = Q U Gamma^-1
+    SCW_TRY(zgemm(st, n, n, n, kOne, d_Q, n, nn, d_U, n, nn, kZero, d_W, n, nn, Zs));
+    coldiv_kernel<<<nblk(nn * Zs), 256, 0, st>>>(d_W, n, d_gam, Zs);
+    SCW_CUDA_TRY(cudaGetLastError());
+    // U^-1 into P, W^-1 into PQ (LU factors in Q)
+    double2* d_Uinv = d_P;
+    double2* d_Winv = d_PQ;
+    for (int which = 0; which < 2; which++) {
+        double2* inv = which == 0 ? d_Uinv : d_Winv;
+        identity_kernel<<<nblk(nn * Zs), 256, 0, st>>>(inv, n, Zs);
+        SCW_CUDA_TRY(cudaGetLastError());
+        SCW_CUDA_TRY(cudaMemcpyAsync(d_Q, which == 0 ? d_U : d_W, sizeof(double2) * nn * Zs, cudaMemcpyDeviceToDevice, st));
+        SCW_TRY(zgetrf(st, d_Q, n, nn, d_piv, n, d_status, Zs, nullptr));
+        SCW_TRY(zgetrs(st, d_Q, n, nn, d_piv, n, inv, n, nn, Zs));
+        SCW_CUDA_TRY(cudaMemcpyAsync(status.data(), d_status, sizeof(int) * Zs, cudaMemcpyDeviceToHost, st));
+        SCW_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int l = 0; l < Zs; l++)
+            if (status[l])
+                return fail(SCW_ERR_NUMERIC, std::string("scw_solve: singular ") + (which ? "W" : "U") +
+                                                 " mode matrix in slice " + std::to_string(l));
+    }
+    mem.release(d_Q);
+    d_Q = nullptr;
+
+    // ---- T3 = Gd_0 Gc_static^-1 f3 = prod_l V_l diag(E_l^-1, E_l) V_l^-1 f3 ----
+    double* d_Sx = mem.get<double>(MF);
+    double* d_Sy = mem.get<double>(MF);
+    double2* d_Sz0 = mem.get<double2>(MF);
+    double2* d_Sz1 = mem.get<double2>(MF);
+    double2* d_X = mem.get<double2>((size_t)N4 * M3);
+    double2* d_A1 = mem.get<double2>((size_t)n * M3);
+    double2* d_A2 = mem.get<double2>((size_t)n * M3);
+    SCW_NEED(d_Sx);
+    SCW_NEED(d_Sy);
+    SCW_NEED(d_Sz0);
+    SCW_NEED(d_Sz1);
+    SCW_NEED(d_X);
+    SCW_NEED(d_A1);
+    SCW_NEED(d_A2);
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_Sx, sol->Sx.data(), sizeof(double) * MF, cudaMemcpyHostToDevice, st));
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_Sy, sol->Sy.data(), sizeof(double) * MF, cudaMemcpyHostToDevice, st));
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_Sz0, sol->Sz0.data(), sizeof(double2) * MF, cudaMemcpyHostToDevice, st));
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_Sz1, sol->Sz1.data(), sizeof(double2) * MF, cudaMemcpyHostToDevice, st));
+    f3_kernel<<<nblk((long long)N4 * M3), 256, 0, st>>>(d_Sx, d_Sy, d_Sz1, MF, d_X);
+    SCW_CUDA_TRY(cudaGetLastError());
+    for (int l = Zs - 1; l >= 0; l--) {
+        const long long o = (long long)l * nn;
+        SCW_TRY(zgemm(st, n, M3, n, kOne, d_Uinv + o, n, 0, d_X, M3, 0, kZero, d_A1, M3, 0, 1));
+        SCW_TRY(zgemm(st, n, M3, n, kOne, d_Winv + o, n, 0, d_X + (size_t)n * M3, M3, 0, kZero, d_A2, M3, 0, 1));
+        mix_kernel<<<nblk((long long)n * M3), 256, 0, st>>>(d_A1, d_A2, d_E + (size_t)l * n, n, M3, 0);
+        SCW_CUDA_TRY(cudaGetLastError());
+        SCW_TRY(zgemm(st, n, M3, n, kOne, d_U + o, n, 0, d_A1, M3, 0, kZero, d_X, M3, 0, 1));
+        SCW_TRY(zgemm(st, n, M3, n, kOne, d_W + o, n, 0, d_A2, M3, 0, kZero, d_X + (size_t)n * M3, M3, 0, 1));
+    }
+
+    // ---- boundary system and its solve (sCWatter.cpp:393-461, 722) ----
+    double2* d_A = mem.get<double2>((size_t)M6 * M6);
+    double2* d_b = mem.get<double2>(M6);
+    SCW_NEED(d_A);
+    SCW_NEED(d_b);
+    bc_matrix_kernel<<<nblk((long long)M6 * M6), 256, 0, st>>>(d_Sx, d_Sy, d_Sz0, d_Sz1, d_X, MF, d_A);
+    SCW_CUDA_TRY(cudaGetLastError());
+    std::vector<cd> f1EF(N4);
+    for (int m = 0; m < MF; m++) {      // f1 EF (sCWatter.cpp:334-357)
+        const cd ph = std::exp(cd(0, 1) * k * zb[0] * sol->Sz0[m]);
+        const cd ex = sol->EF[m], ey = sol->EF[MF + m], ez = sol->EF[2 * MF + m];
+        f1EF[m] = ph * ex;
+        f1EF[MF + m] = ph * ey;
+        f1EF[2 * MF + m] = -ph * sol->Sz0[m] * ey + ph * sol->Sy[m] * ez;
+        f1EF[3 * MF + m] = ph * sol->Sz0[m] * ex - ph * sol->Sx[m] * ez;
+    }
+    {
+        std::vector<cd> bh(M6, cd(0, 0));
+        for (int r = 0; r < N4; r++) bh[2 * MF + r] = -f1EF[r];
+        SCW_CUDA_TRY(cudaMemcpyAsync(d_b, bh.data(), sizeof(double2) * M6, cudaMemcpyHostToDevice, st));
+        SCW_TRY(zgetrf(st, d_A, M6, 0, d_piv, 0, d_status, 1, nullptr));
+        SCW_TRY(zgetrs(st, d_A, M6, 0, d_piv, 0, d_b, 1, 0, 1));
+        sol->x.resize(M6);
+        SCW_CUDA_TRY(cudaMemcpyAsync(sol->x.data(), d_b, sizeof(double2) * M6, cudaMemcpyDeviceToHost, st));
+        SCW_CUDA_TRY(cudaMemcpyAsync(status.data(), d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SCW_CUDA_TRY(cudaStreamSynchronize(st));
+        if (status[0]) return fail(SCW_ERR_NUMERIC, "scw_solve: singular boundary system");
+    }
+    mem.release(d_A);
+    sol->gam.resize((size_t)Zs * n);
+    SCW_CUDA_TRY(cudaMemcpyAsync(sol->gam.data(), d_gam, sizeof(double2) * Zs * n, cudaMemcpyDeviceToHost, st));
+    SCW_CUDA_TRY(cudaStreamSynchronize(st));
+    if (sol->external) {
+        ctx->launches += 16 + 4 * Zs;
+        *out = sol.release();
+        return SCW_OK;
+    }
+
+    // ---- beta: beta_0 = Gd_0^-1 (f1 EF + f2 R),  beta_l = Gd_l^-1 Gc_{l-1} beta_{l-1} (sCWatter.cpp:743-777) ----
+    double2* d_beta = mem.get<double2>((size_t)Zs * N4);
+    double2* d_v = mem.get<double2>(N4);
+    SCW_NEED(d_beta);
+    SCW_NEED(d_v);
+    {
+        std::vector<cd> v4(N4);
+        for (int m = 0; m < MF; m++) {
+            const cd rx = sol->x[m], ry = sol->x[MF + m], rz = sol->x[2 * MF + m];
+            v4[m] = f1EF[m] + rx;
+            v4[MF + m] = f1EF[MF + m] + ry;
+            v4[2 * MF + m] = f1EF[2 * MF + m] + sol->Sz0[m] * ry + sol->Sy[m] * rz;
+            v4[3 * MF + m] = f1EF[3 * MF + m] - sol->Sz0[m] * rx - sol->Sx[m] * rz;
+        }
+        SCW_CUDA_TRY(cudaMemcpyAsync(d_v, v4.data(), sizeof(double2) * N4, cudaMemcpyHostToDevice, st));
+        SCW_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    for (int l = 0; l < Zs; l++) {
+        const long long o = (long long)l * nn;
+        double2* bl = d_beta + (size_t)l * N4;
+        if (l > 0) {   // v = Gc_{l-1} beta_{l-1} = [U (E bt + bb); W (E bt - bb)]
+            const double2* bp = d_beta + (size_t)(l - 1) * N4;
+            SCW_CUDA_TRY(cudaMemcpyAsync(d_A1, bp, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+            SCW_CUDA_TRY(cudaMemcpyAsync(d_A2, bp + n, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+            mix_kernel<<<nblk(n), 256, 0, st>>>(d_A1, d_A2, d_E + (size_t)(l - 1) * n, n, 1, 2);
+            SCW_CUDA_TRY(cudaGetLastError());
+            SCW_TRY(zgemm(st, n, 1, n, kOne, d_U + o - nn, n, 0, d_A1, 1, 0, kZero, d_v, 1, 0, 1));
+            SCW_TRY(zgemm(st, n, 1, n, kOne, d_W + o - nn, n, 0, d_A2, 1, 0, kZero, d_v + n, 1, 0, 1));
+        }
+        SCW_TRY(zgemm(st, n, 1, n, kOne, d_Uinv + o, n, 0, d_v, 1, 0, kZero, bl, 1, 0, 1));
+        SCW_TRY(zgemm(st, n, 1, n, kOne, d_Winv + o, n, 0, d_v + n, 1, 0, kZero, bl + n, 1, 0, 1));
+        mix_kernel<<<nblk(n), 256, 0, st>>>(bl, bl + n, d_E + (size_t)l * n, n, 1, 1);
+        SCW_CUDA_TRY(cudaGetLastError());
+    }
+    mem.release(d_P);
+    mem.release(d_PQ);
+
+    // ---- Q_check / Q_hat with Ez from the magnetic field (sCWatter.cpp:781-871) ----
+    std::vector<double> up_pz(MF), wq_pz(MF);
+    for (int m = 0; m < MF; m++) {      // built with M_PI here, as in the reference
+        up_pz[m] = 2.0 * ps[m % M0] * M_PI / prm->size[0] + dir[0] * k;
+        wq_pz[m] = 2.0 * qs[m / M0] * M_PI / prm->size[1] + dir[1] * k;
+    }
+    double* d_uppz = mem.get<double>(MF);
+    double* d_wqpz = mem.get<double>(MF);
+    double2* d_Kn = mem.get<double2>((size_t)MF * MF);
+    double2* d_Hm = mem.get<double2>((size_t)MF * n);
+    double2* d_Qall = nullptr;
+    if (cudaMalloc(&d_Qall, sizeof(double2) * (size_t)Zs * 2 * M3 * n) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SCW_ERR_NOMEM, "scw_solve: cudaMalloc of the mode amplitudes");
+    }
+    sol->dQ = d_Qall;
+    SCW_NEED(d_uppz);
+    SCW_NEED(d_wqpz);
+    SCW_NEED(d_Kn);
+    SCW_NEED(d_Hm);
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_uppz, up_pz.data(), sizeof(double) * MF, cudaMemcpyHostToDevice, st));
+    SCW_CUDA_TRY(cudaMemcpyAsync(d_wqpz, wq_pz.data(), sizeof(double) * MF, cudaMemcpyHostToDevice, st));
+    for (int l = 0; l < Zs; l++) {
+        const long long o = (long long)l * nn;
+        if (prm->pz) {
+            kn_kernel<<<nblk((long long)MF * MF), 256, 0, st>>>(d_coef + (size_t)l * 2 * MF + MF, M0, M1, -1.0 / k, d_Kn);
+            SCW_CUDA_TRY(cudaGetLastError());
+        }
+        for (int h = 0; h < 2; h++) {
+            double2* Qo = d_Qall + ((size_t)l * 2 + h) * M3 * n;
+            const double2* beta = d_beta + (size_t)l * N4 + (h ? n : 0);
+            q_rows_kernel<<<nblk(nn), 256, 0, st>>>(d_U + o, d_W + o, beta, MF, h ? -1.0 : 1.0, d_uppz, d_wqpz, Qo,
+                                                   prm->pz ? d_Hm : nullptr);
+            SCW_CUDA_TRY(cudaGetLastError());
+            if (prm->pz) {
+                SCW_TRY(zgemm(st, MF, n, MF, kOne, d_Kn, MF, 0, d_Hm, n, 0, kZero, Qo + (size_t)n * n, n, 0, 1));
+            } else {
+                SCW_CUDA_TRY(cudaMemsetAsync(Qo + (size_t)n * n, 0, sizeof(double2) * MF * n, st));
+            }
+        }
+    }
+    SCW_CUDA_TRY(cudaStreamSynchronize(st));
+    ctx->launches += 16 + 14 * Zs;
+    *out = sol.release();
+    return SCW_OK;
+}
+
+scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_slices, double* k) {
+    if (!s) return fail(SCW_ERR_ARG, "null solution");
+    if (M0) *M0 = s->M0;
+    if (M1) *M1 = s->M1;
+    if (n_slices) *n_slices = s->Z;
+    if (k) *k = s->k;
+    return SCW_OK;
+}
+
+scw_status scw_solution_get(scw_solution s, double* gamma, double* x, double* ef, double* z_boundaries) {
+    if (!s) return fail(SCW_ERR_ARG, "null solution");
+    if (gamma) std::memcpy(gamma, s->gam.data(), sizeof(cd) * s->gam.size());
+    if (x) std::memcpy(x, s->x.data(), sizeof(cd) * s->x.size());
+    if (ef) std::memcpy(ef, s->EF.data(), sizeof(cd) * s->EF.size());
+    if (z_boundaries) std::memcpy(z_boundaries, s->zb.data(), sizeof(double) * s->zb.size());
+    return SCW_OK;
+}
+
+scw_status scw_solution_get_modes(scw_solution s, int l, double* Q_check, double* Q_hat) {
+    if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_solution_get_modes: slice out of range");
+    if (!s->dQ) return fail(SCW_ERR_STATE, "scw_solution_get_modes: no mode amplitudes (external solve)");
+    const size_t blk = (size_t)3 * s->MF * 2 * s->MF;
+    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    if (Q_check)
+        SCW_CUDA_TRY(cudaMemcpy(Q_check, s->dQ + (size_t)l * 2 * blk, sizeof(double2) * blk, cudaMemcpyDeviceToHost));
+    if (Q_hat)
+        SCW_CUDA_TRY(cudaMemcpy(Q_hat, s->dQ + ((size_t)l * 2 + 1) * blk, sizeof(double2) * blk, cudaMemcpyDeviceToHost));
+    return SCW_OK;
+}
+
+// The separable coefficient set of a solution, on the solution's device.
+scw_status scw_solution_to_sep(scw_solution s, scw_sep* out) {
+    if (!s || !out) return fail(SCW_ERR_ARG, "null argument");
+    *out = nullptr;
+    scw_ctx ctx = s->ctx;
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int MF = s->MF, n = 2 * MF, M0 = s->M0, M1 = s->M1, Z = s->Z;
+    const double k = s->k;
+    std::vector<double> kx(M0), ky(M1);
+    for (int a = 0; a < M0; a++) kx[a] = s->Sx[(size_t)a * M1] * k;
+    for (int b = 0; b < M1; b++) ky[b] = s->Sy[(size_t)b] * k;
+    std::vector<double> zb = s->zb;
+    if (s->external)      // interior layers of an external-only structure sit at z = 0 with no waves
+        for (int l = 1; l < Z; l++) zb[l] = 0.0;
+    scw_sep sp = nullptr;
+    scw_status st = scw_sep_create(ctx, M0, M1, Z, s->external ? 0 : n, kx.data(), ky.data(), zb.data(), &sp);
+    if (st != SCW_OK) return st;
+    std::unique_ptr<scw_sep_s, scw_status (*)(scw_sep)> guard(sp, scw_sep_destroy);
+    std::vector<cd> inc(3 * MF), refl(3 * MF), trans(3 * MF), kzi(MF), kzr(MF), kzt(MF);
+    for (int p = 0; p < MF; p++) {
+        for (int c = 0; c < 3; c++) {
+            inc[c * MF + p] = s->EF[c * MF + p];
+            refl[c * MF + p] = s->x[c * MF + p];
+            trans[c * MF + p] = s->x[3 * MF + c * MF + p];
+        }
+        kzi[p] = s->Sz0[p] * k;
+        kzr[p] = -s->Sz0[p] * k * s->n0;     // sCWatter.cpp:471-475 multiplies by n0 once more
+        kzt[p] = s->Sz1[p] * k * s->n1;
+    }
+    st = scw_sep_set_exterior(sp, (const double*)inc.data(), (const double*)kzi.data(), (const double*)refl.data(),
+                              (const double*)kzr.data(), (const double*)trans.data(), (const double*)kzt.data());
+    if (st != SCW_OK) return st;
+    if (!s->external) {
+        const size_t blk = (size_t)3 * MF * n;
+        float2* tmp = nullptr;
+        if (cudaMalloc(&tmp, sizeof(float2) * 2 * blk) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SCW_ERR_NOMEM, "scw_solution_to_sep: cudaMalloc");
+        }
+        std::vector<cd> kzd(n), kzu(n);
+        for (int l = 0; l < Z && st == SCW_OK; l++) {
+            for (int j = 0; j < n; j++) {
+                kzd[j] = s->gam[(size_t)l * n + j] * k;
+                kzu[j] = -s->gam[(size_t)l * n + j] * k;
+            }
+            scw::sv::to_c64_kernel<<<scw::sv::nblk(2 * blk), 256, 0, ctx->stream>>>(s->dQ + (size_t)l * 2 * blk, tmp,
+                                                                                   (long long)(2 * blk));
+            st = scw_sep_set_slice_device(sp, l, (const double*)kzd.data(), tmp, (const double*)kzu.data(), tmp + blk);
+            if (st == SCW_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+                st = fail(SCW_ERR_CUDA, "scw_solution_to_sep: stream error");
+        }
+        cudaFree(tmp);
+        if (st != SCW_OK) return st;
+    }
+    *out = guard.release();
+    return SCW_OK;
+}
+
+// The .cw structure written by sCWatter (sCWatter.cpp:890-956): per harmonic p the incident
+// wave, the reflected wave (wound to z_0), the transmitted wave (wound to z_Z) and, unless
+// external, the 2MF downward / upward modes of each slice wound to their boundary.
+scw_status scw_solution_to_cw(scw_solution s, scw_cw* out) {
+    if (!s || !out) return fail(SCW_ERR_ARG, "null argument");
+    *out = nullptr;
+    const int MF = s->MF, n = 2 * MF, Z = s->Z, ZL = Z + 1;
+    const double k = s->k;
+    const size_t blk = (size_t)3 * MF * n;
+    std::vector<cd> Qh;
+    try {
+        if (!s->external) Qh.resize((size_t)Z * 2 * blk);
+    } catch (const std::bad_alloc&) {
+        return fail(SCW_ERR_NOMEM, "host allocation of the mode amplitudes");
+    }
+    if (!s->external) {
+        SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+        SCW_CUDA_TRY(cudaMemcpy(Qh.data(), s->dQ, sizeof(double2) * Qh.size(), cudaMemcpyDeviceToHost));
+    }
+    std::unique_ptr<scw_cw_s> cw(new (std::nothrow) scw_cw_s());
+    if (!cw) return fail(SCW_ERR_NOMEM, "host allocation");
+    try {
+        cw->layers.resize(ZL);
+        for (int l = 0; l < ZL; l++) cw->layers[l].z = 0.0;
+        auto rec = [](std::vector<double>& v, cd ex, cd ey, cd ez, cd kx, cd ky, cd kz, double zw) {
+            const cd f = std::exp(cd(0, -1) * kz * zw);     // wind(0, 0, -z): E0 exp(-i kz z)
+            const cd E[3] = {ex * f, ey * f, ez * f};
+            const cd K[3] = {kx, ky, kz};
+            for (int c = 0; c < 3; c++) {
+                v.push_back(E[c].real());
+                v.push_back(E[c].imag());
+            }
+            for (int c = 0; c < 3; c++) {
+                v.push_back(K[c].real());
+                v.push_back(K[c].imag());
+            }
+        };
+        auto modes = [&](std::vector<double>& v, const cd* Q, int p, cd kx, cd ky, const cd* gam, double sgn, double zw) {
+            for (int j = 0; j < n; j++)
+                rec(v, Q[(size_t)p * n + j], Q[(size_t)(MF + p) * n + j], Q[(size_t)(2 * MF + p) * n + j], kx, ky,
+                    sgn * gam[j] * k, zw);
+        };
+        for (int p = 0; p < MF; p++) {
+            const cd kx = s->Sx[p] * k, ky = s->Sy[p] * k;
+            rec(cw->Pi, s->EF[p], s->EF[MF + p], s->EF[2 * MF + p], kx, ky, s->Sz0[p] * k, 0.0);
+            for (int l = 0; l < ZL; l++) {
+                auto& L = cw->layers[l];
+                if (l == 0) {
+                    L.z = s->zb[0];
+                    rec(L.Pr, s->x[p], s->x[MF + p], s->x[2 * MF + p], kx, ky, -s->Sz0[p] * k * s->n0, s->zb[0]);
+                    if (!s->external) modes(L.Pt, Qh.data(), p, kx, ky, s->gam.data(), 1.0, s->zb[0]);
+                } else if (l == ZL - 1) {
+                    L.z = s->zb[l];
+                    rec(L.Pt, s->x[3 * MF + p], s->x[4 * MF + p], s->x[5 * MF + p], kx, ky, s->Sz1[p] * k * s->n1,
+                        s->zb[l]);
+                    if (!s->external)
+                        modes(L.Pr, Qh.data() + ((size_t)(l - 1) * 2 + 1) * blk, p, kx, ky,
+                              s->gam.data() + (size_t)(l - 1) * n, -1.0, s->zb[l]);
+                } else if (!s->external) {
+                    L.z = s->zb[l];
+                    modes(L.Pr, Qh.data() + ((size_t)(l - 1) * 2 + 1) * blk, p, kx, ky,
+                          s->gam.data() + (size_t)(l - 1) * n, -1.0, s->zb[l]);
+                    modes(L.Pt, Qh.data() + (size_t)l * 2 * blk, p, kx, ky, s->gam.data() + (size_t)l * n, 1.0,
+                          s->zb[l]);
+                }
+            }
+        }
+    } catch (const std::bad_alloc&) {
+        return fail(SCW_ERR_NOMEM, "host allocation of the wave lists");
+    }
+    *out = cw.release();
+    return SCW_OK;
+}
+
+}  // extern "C"

@@ -118,3 +118,27 @@ def test_zgeev_degenerate(ctx):
     assert res < 1e-10
     s = np.linalg.svd(V / np.linalg.norm(V, axis=0), compute_uv=False)
     assert s[-1] / s[0] > 1e-8
+
+
+def test_zgeev_diagonal_with_rounding_couplings(ctx):
+    """A homogeneous slice's PQ: diagonal with repeated eigenvalues and 1e-18 couplings
+    between equal entries.  The QR iteration must deflate them instead of cycling."""
+    from scwatter_gb300 import _lib
+    import torch
+    rng = np.random.default_rng(5)
+    n = 30
+    lam = np.repeat(rng.uniform(0.9, 1.0, 6), 5).astype(np.complex128)
+    A = np.diag(lam)
+    for i in range(0, n - 1, 2):
+        if lam[i] == lam[i + 1]:
+            A[i, i + 1] = A[i + 1, i] = 4.3e-18
+    dA = _dev(A[None])
+    dW = torch.zeros((1, n), dtype=torch.complex128, device="cuda")
+    dV = torch.zeros((1, n, n), dtype=torch.complex128, device="cuda")
+    torch.cuda.synchronize()
+    _lib.call("scw_zgeev", ctx.handle, n, _p(dA), _p(dW), _p(dV), 1, None)
+    W, V = dW.cpu().numpy()[0], dV.cpu().numpy()[0]
+    res = np.linalg.norm(A @ V - V * W[None, :]) / (np.linalg.norm(A) * np.linalg.norm(V))
+    assert res < 1e-14
+    assert np.linalg.cond(V / np.linalg.norm(V, axis=0)) < 10
+    np.testing.assert_allclose(np.sort(W.real), np.sort(lam.real), atol=1e-15)

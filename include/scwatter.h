@@ -214,6 +214,7 @@ typedef struct scw_solve_params {
     int coef[2];          /* --coef: harmonics along x, y (<= 0: the sample's X, Y) */
     int external;         /* --external: keep only the exterior waves */
     int pz;               /* 1 = compute Ez of the modes; 0 = the reference's --npz */
+    int psf;              /* --psf: every harmonic carries the incident field (sCWatter.cpp:665-669) */
 } scw_solve_params;
 
 /* sample: [Z][Y][X] complex128 refractive index in HOST memory (the .npy volume).  Runs the

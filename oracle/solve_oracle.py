@@ -142,6 +142,7 @@ class SolveParams:
     coef: tuple | None = None
     external: bool = False
     pz: bool = True          # False == the reference's --npz flag
+    psf: bool = False        # the reference's --psf flag (sCWatter.cpp:665-669)
 
 
 @dataclass
@@ -307,6 +308,8 @@ def solve(sample, prm: SolveParams, keep_phi: bool = False) -> SolveResult:
 
     # incident field (sCWatter.cpp:656-674)
     EF = np.concatenate([fft2_crop(e[c] * np.ones((Y, X)), M1, M0).flatten(order="F") for c in range(3)])
+    if prm.psf:     # sCWatter.cpp:665-669: every harmonic carries E0
+        EF = np.concatenate([np.full(MF, e[c]) for c in range(3)])
 
     # CalculateD + EigenDecompositionD
     evals, evecs, NIfs, Phis = [], [], [], []

@@ -456,7 +456,7 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
     for (int c = 0; c < 3; c++)
         for (int a = 0; a < M1; a++)
             for (int b = 0; b < M0; b++)
-                if (du[a] == 0 && dv[b] == 0) sol->EF[c * MF + a + b * M1] = e[c];
+                if (prm->psf || (du[a] == 0 && dv[b] == 0)) sol->EF[c * MF + a + b * M1] = e[c];
 
     DevMem mem(ctx->device);
     const long long nn = (long long)n * n;

@@ -14,6 +14,7 @@ sCWatter flag   keyword                meaning
 --coef          ``coef``               harmonics along x, y (None: the sample's X, Y)
 --external      ``external``           keep only the exterior waves
 --npz           ``pz=False``           skip the Ez rows of the modes
+--psf           ``psf``                every harmonic carries the incident field
 ==============  =====================  ====================================
 
 The whole solve runs in the native library on the GPU (FP64); there is no CPU path.
@@ -35,10 +36,10 @@ class _Params(ctypes.Structure):
     _fields_ = [("lam", ctypes.c_double), ("direction", ctypes.c_double * 3), ("ex", ctypes.c_double * 2),
                 ("ey", ctypes.c_double * 2), ("ez", ctypes.c_double * 2), ("n", ctypes.c_double * 2),
                 ("kappa", ctypes.c_double), ("size", ctypes.c_double * 3), ("z", ctypes.c_double),
-                ("coef", ctypes.c_int * 2), ("external", ctypes.c_int), ("pz", ctypes.c_int)]
+                ("coef", ctypes.c_int * 2), ("external", ctypes.c_int), ("pz", ctypes.c_int), ("psf", ctypes.c_int)]
 
 
-def _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz) -> _Params:
+def _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz, psf=False) -> _Params:
     p = _Params()
     p.lam = float(lam)
     p.direction[:] = [float(v) for v in direction]
@@ -60,6 +61,7 @@ def _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz) -
         p.coef[:] = [int(coef[0]), int(coef[1])]
     p.external = 1 if external else 0
     p.pz = 1 if pz else 0
+    p.psf = 1 if psf else 0
     return p
 
 
@@ -126,7 +128,7 @@ class Solution:
 
 
 def solve(sample, lam=1.0, direction=(0.0, 0.0, 1.0), ex=(0.0, 0.0), ey=(1.0, 0.0), ez=(0.0, 0.0), n=(1.0, 1.0),
-          kappa=0.0, size=(10.0, 10.0, 2.0), z=0.0, coef=None, external=False, pz=True,
+          kappa=0.0, size=(10.0, 10.0, 2.0), z=0.0, coef=None, external=False, pz=True, psf=False,
           ctx: Context | None = None) -> Solution:
     """Solves the sample (``[Z, Y, X]`` or ``[Y, X]`` complex refractive index) on the GPU."""
     vol = np.ascontiguousarray(sample, dtype=np.complex128)
@@ -135,7 +137,7 @@ def solve(sample, lam=1.0, direction=(0.0, 0.0, 1.0), ex=(0.0, 0.0), ey=(1.0, 0.
     if vol.ndim != 3:
         raise ValueError("sample must be [Z, Y, X] or [Y, X]")
     ctx = ctx or Context(0)
-    prm = _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz)
+    prm = _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz, psf)
     h = ctypes.c_void_p()
     Z, Y, X = vol.shape
     _lib.call("scw_solve", ctx.handle, ctypes.c_void_p(vol.ctypes.data), Z, Y, X, ctypes.byref(prm), ctypes.byref(h))

@@ -29,6 +29,7 @@ CASES = {
                                                 n=(1.0, 1.3), kappa=0.05, z=0.4)),
     "one_slice_even_rows_odd_cols": dict(shape=(1, 10, 9), coef=(3, 3), seed=3, kw=dict()),
     "no_pz_rectangular": dict(shape=(4, 9, 8), coef=(5, 3), seed=4, kw=dict(pz=False, ex=(0.5, 0.2), ey=(1, 0))),
+    "psf_default_polarisation": dict(shape=(2, 8, 8), coef=(3, 3), seed=8, kw=dict(psf=True)),
 }
 
 
@@ -154,3 +155,21 @@ def test_save_roundtrip(ctx, tmp_path):
     for a, b in zip(S.Layers, T.Layers):
         np.testing.assert_array_equal(a.Pr, b.Pr)
         np.testing.assert_array_equal(a.Pt, b.Pt)
+
+
+def test_command_line(tmp_path):
+    """python -m scwatter_gb300.scwatter writes the structure the oracle packs."""
+    from scwatter_gb300 import scwatter
+    from scwatter_gb300.cw import CoupledWaveStructure
+    sample = samples.spheres((2, 8, 8), n_spheres=1, radius=(2, 3), seed=9)
+    np.save(tmp_path / "s.npy", sample)
+    out = tmp_path / "c.cw"
+    rc = scwatter.main(["--sample", str(tmp_path / "s.npy"), "--size", "8", "8", "2", "--coef", "3", "3",
+                        "--ex", "1", "0", "--ey", "0", "0", "--direction", "0.2", "-0.1", "1", "--output", str(out)])
+    assert rc == 0
+    S = CoupledWaveStructure()
+    assert S.load(str(out))
+    prm = so.SolveParams(size=(8.0, 8.0, 2.0), coef=(3, 3), ex=(1, 0), ey=(0, 0), direction=(0.2, -0.1, 1.0))
+    cw_ref = so.pack(so.solve(sample, prm), prm)
+    pts = _points(-3, 3, 4, 4)
+    assert max(rel_l2(_field(_cw_of(S), pts), _field(cw_ref, pts))) < TOL_FIELD

@@ -29,8 +29,11 @@
 #include <new>
 #include <vector>
 
+#include <string>
+
 #include "scw_dense.h"
 #include "scw_sep.h"
+#include "solve_plan.h"
 
 using cd = std::complex<double>;
 
@@ -270,6 +273,54 @@ __global__ void to_c64_kernel(const double2* __restrict__ a, float2* __restrict_
     if (e < n) b[e] = make_float2((float)a[e].x, (float)a[e].y);
 }
 
+// b = [0 (2MF); -f1 EF (4MF)]  (sCWatter.cpp:459-460)
+__global__ void bc_rhs_kernel(const double2* __restrict__ f1EF, int MF, double2* __restrict__ b) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 6 * MF) return;
+    b[e] = e < 2 * MF ? make_double2(0.0, 0.0) : make_double2(-f1EF[e - 2 * MF].x, -f1EF[e - 2 * MF].y);
+}
+
+// v = f1 EF + f2 R with R = x[0, 3MF)  (sCWatter.cpp:745-747)
+__global__ void beta_init_kernel(const double2* __restrict__ f1EF, const double2* __restrict__ x,
+                                 const double* __restrict__ Sx, const double* __restrict__ Sy,
+                                 const double2* __restrict__ Sz0, int MF, double2* __restrict__ v) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= MF) return;
+    const double2 rx = x[m], ry = x[MF + m], rz = x[2 * MF + m], s0 = Sz0[m];
+    v[m] = cadd(f1EF[m], rx);
+    v[MF + m] = cadd(f1EF[MF + m], ry);
+    v[2 * MF + m] = cadd(cadd(f1EF[2 * MF + m], cmul(s0, ry)), make_double2(Sy[m] * rz.x, Sy[m] * rz.y));
+    v[3 * MF + m] = csub(csub(f1EF[3 * MF + m], cmul(s0, rx)), make_double2(Sx[m] * rz.x, Sx[m] * rz.y));
+}
+
+// kz of the separable set: [l][0][j] = gamma k, [l][1][j] = -gamma k
+__global__ void sep_kz_kernel(const double2* __restrict__ gam, int Z, int n, double k, double2* __restrict__ kz) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)Z * n) return;
+    const int l = (int)(e / n), j = (int)(e % n);
+    const double2 g = gam[e];
+    kz[((long long)l * 2) * n + j] = make_double2(g.x * k, g.y * k);
+    kz[((long long)l * 2 + 1) * n + j] = make_double2(-g.x * k, -g.y * k);
+}
+
+// exterior blocks of the separable set: incident, reflected, transmitted amplitudes [3][MF]
+// each, then kz of the three (reflected -Sz0 k n0, transmitted Sz1 k n1: sCWatter.cpp:471-475)
+__global__ void sep_ext_kernel(const double2* __restrict__ EF, const double2* __restrict__ x,
+                               const double2* __restrict__ Sz0, const double2* __restrict__ Sz1, int MF, double k,
+                               double n0, double n1, double2* __restrict__ ext) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 3 * MF) return;
+    ext[e] = EF[e];
+    ext[3 * MF + e] = x[e];
+    ext[6 * MF + e] = x[3 * MF + e];
+    if (e < MF) {
+        const double2 a = Sz0[e], b = Sz1[e];
+        ext[9 * MF + e] = make_double2(a.x * k, a.y * k);
+        ext[10 * MF + e] = make_double2(-a.x * k * n0, -a.y * k * n0);
+        ext[11 * MF + e] = make_double2(b.x * k * n1, b.y * k * n1);
+    }
+}
+
 static unsigned nblk(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
 // FourierWave.h:82-145: the source index of each shifted row / column, including the column
@@ -295,72 +346,22 @@ static void fft_shift_index(int m, int n, std::vector<int>& indx, std::vector<in
     }
 }
 
-struct DevMem {
-    int device;
-    std::vector<void*> ptrs;
-    explicit DevMem(int dev) : device(dev) {}
-    ~DevMem() {
-        cudaSetDevice(device);
-        for (void* p : ptrs) cudaFree(p);
-    }
-    template <typename T>
-    T* get(size_t n) {
-        void* p = nullptr;
-        if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
-            cudaGetLastError();
-            return nullptr;
-        }
-        ptrs.push_back(p);
-        return (T*)p;
-    }
-    void release(void* p) {
-        auto it = std::find(ptrs.begin(), ptrs.end(), p);
-        if (it != ptrs.end()) {
-            cudaFree(p);
-            ptrs.erase(it);
-        }
-    }
-};
-
 #define SCW_TRY(expr)                          \
     do {                                       \
         const scw_status s_ = (expr);          \
         if (s_ != SCW_OK) return s_;           \
     } while (0)
 
-#define SCW_NEED(ptr)                                                               \
-    do {                                                                            \
-        if (!(ptr)) return fail(SCW_ERR_NOMEM, "scw_solve: cudaMalloc of " #ptr);  \
-    } while (0)
-
 const double2 kOne = {1.0, 0.0};
 const double2 kZero = {0.0, 0.0};
 
-}  // namespace sv
-}  // namespace scw
-
-using scw::fail;
-
-extern "C" {
-
-scw_status scw_solution_destroy(scw_solution s) {
-    delete s;
-    return SCW_OK;
-}
-
-// sCWatter main (sCWatter.cpp:569-885) on the context's GPU.
-scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, const scw_solve_params* prm,
-                     scw_solution* out) {
-    using namespace scw;
-    using namespace scw::sv;
-    if (!ctx || !sample || !prm || !out || Zs < 1 || Y < 1 || X < 1) return fail(SCW_ERR_ARG, "scw_solve: bad arguments");
-    *out = nullptr;
+// ---------------------------------------------------------------------------------------
+// Planning (host): sCWatter.cpp:569-680
+// ---------------------------------------------------------------------------------------
+scw_status plan_solve(const scw_solve_params* prm, int Zs, int Y, int X, SolvePlan& p) {
+    if (!prm || Zs < 1 || Y < 1 || X < 1) return fail(SCW_ERR_ARG, "scw_solve: bad arguments");
     if (!(prm->lambda > 0) || !(prm->size[0] > 0) || !(prm->size[1] > 0) || !(prm->size[2] > 0))
         return fail(SCW_ERR_ARG, "scw_solve: wavelength and sizes must be positive");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
-    cudaStream_t st = ctx->stream;
-
-    // ---- geometry and incident field (sCWatter.cpp:569-680) ----
     const double dn = std::sqrt(prm->direction[0] * prm->direction[0] + prm->direction[1] * prm->direction[1] +
                                 prm->direction[2] * prm->direction[2]);
     if (!(dn > 0)) return fail(SCW_ERR_ARG, "scw_solve: zero direction");
@@ -380,9 +381,19 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
     const double k = 2 * kPiRef / prm->lambda;
     const cd ni0(n0, 0.0), ni1(n1r, prm->kappa);
     const int ZL = Zs + 1;
-    std::vector<double> zb(ZL);
-    zb[0] = prm->z - prm->size[2] / 2.0;
-    for (int i = 1; i < ZL; i++) zb[i] = zb[i - 1] + prm->size[2] / Zs;
+    p.Z = Zs;
+    p.Y = Y;
+    p.X = X;
+    p.k = k;
+    p.n0 = n0;
+    p.n1 = n1r;
+    p.external = prm->external != 0;
+    p.pz = prm->pz != 0;
+    p.zb.resize(ZL);
+    p.zb[0] = prm->z - prm->size[2] / 2.0;
+    for (int i = 1; i < ZL; i++) p.zb[i] = p.zb[i - 1] + prm->size[2] / Zs;
+    p.dz.resize(Zs);
+    for (int l = 0; l < Zs; l++) p.dz[l] = (Zs == 1) ? p.zb[ZL - 1] - p.zb[0] : p.zb[l + 1] - p.zb[l];
     int M0 = prm->coef[0] > 0 ? prm->coef[0] : X, M1 = prm->coef[1] > 0 ? prm->coef[1] : Y;
     {   // harmonic count clamping (sCWatter.cpp:607-645)
         const double lam = prm->lambda;
@@ -408,41 +419,41 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
         M1 = std::min(M1, Y);
         if (M0 < 1 || M1 < 1) return fail(SCW_ERR_ARG, "scw_solve: no Fourier coefficients left after clamping");
     }
-    const int MF = M0 * M1, n = 2 * MF, N4 = 4 * MF, M3 = 3 * MF, M6 = 6 * MF;
-    if ((long long)M6 * M6 > (1LL << 31) * 4) return fail(SCW_ERR_ARG, "scw_solve: too many Fourier coefficients");
+    const int MF = M0 * M1;
+    if ((long long)6 * MF * 6 * MF > (1LL << 31)) return fail(SCW_ERR_ARG, "scw_solve: too many Fourier coefficients");
+    p.M0 = M0;
+    p.M1 = M1;
+    p.MF = MF;
+    p.n = 2 * MF;
     // k grids (FourierWave.h:319-334): integer series -(M/2) .. (M-1)/2
-    std::vector<int> ps(M0), qs(M1);
-    std::vector<double> up(M0), wq(M1);
+    p.ps.resize(M0);
+    p.qs.resize(M1);
+    p.up.resize(M0);
+    p.wq.resize(M1);
     for (int i = 0; i < M0; i++) {
-        ps[i] = -(M0 / 2) + i;
-        up[i] = 2 * kPiRef * ps[i] / prm->size[0] + dir[0] * k;
+        p.ps[i] = -(M0 / 2) + i;
+        p.up[i] = 2 * kPiRef * p.ps[i] / prm->size[0] + dir[0] * k;
     }
     for (int i = 0; i < M1; i++) {
-        qs[i] = -(M1 / 2) + i;
-        wq[i] = 2 * kPiRef * qs[i] / prm->size[1] + dir[1] * k;
+        p.qs[i] = -(M1 / 2) + i;
+        p.wq[i] = 2 * kPiRef * p.qs[i] / prm->size[1] + dir[1] * k;
     }
-    std::unique_ptr<scw_solution_s> sol(new (std::nothrow) scw_solution_s());
-    if (!sol) return fail(SCW_ERR_NOMEM, "host allocation");
-    sol->ctx = ctx;
-    sol->M0 = M0;
-    sol->M1 = M1;
-    sol->MF = MF;
-    sol->Z = Zs;
-    sol->k = k;
-    sol->zb = zb;
-    sol->external = prm->external != 0;
-    sol->n0 = n0;
-    sol->n1 = n1r;
-    sol->Sx.resize(MF);
-    sol->Sy.resize(MF);
-    sol->Sz0.resize(MF);
-    sol->Sz1.resize(MF);
-    for (int f = 0; f < MF; f++) {      // column-major flattening of the M1 x M0 meshes (sCWatter.cpp:677-680)
-        const double sx = up[f / M1] / k, sy = wq[f % M1] / k;
-        sol->Sx[f] = sx;
-        sol->Sy[f] = sy;
-        sol->Sz0[f] = std::sqrt(ni0 * ni0 - cd(sx * sx) - cd(sy * sy));
-        sol->Sz1[f] = std::sqrt(ni1 * ni1 - cd(sx * sx) - cd(sy * sy));
+    p.up_pz.resize(MF);
+    p.wq_pz.resize(MF);
+    for (int m = 0; m < MF; m++) {      // the Ez step builds its grids with M_PI (sCWatter.cpp:806-812)
+        p.up_pz[m] = 2.0 * p.ps[m % M0] * M_PI / prm->size[0] + dir[0] * k;
+        p.wq_pz[m] = 2.0 * p.qs[m / M0] * M_PI / prm->size[1] + dir[1] * k;
+    }
+    p.Sx.resize(MF);
+    p.Sy.resize(MF);
+    p.Sz0.resize(MF);
+    p.Sz1.resize(MF);
+    for (int f = 0; f < MF; f++) {      // column-major flattening of the M1 x M0 meshes
+        const double sx = p.up[f / M1] / k, sy = p.wq[f % M1] / k;
+        p.Sx[f] = sx;
+        p.Sy[f] = sy;
+        p.Sz0[f] = std::sqrt(ni0 * ni0 - cd(sx * sx) - cd(sy * sy));
+        p.Sz1[f] = std::sqrt(ni1 * ni1 - cd(sx * sx) - cd(sy * sy));
     }
     // the DFT rows / columns that land in the centred crop after the shift
     std::vector<int> ix, iy;
@@ -451,283 +462,352 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
     std::vector<int> du(M1), dv(M0);
     for (int a = 0; a < M1; a++) du[a] = ix[r0 + a];
     for (int b = 0; b < M0; b++) dv[b] = iy[c0 + b];
-    // incident field: the transform of a constant lands on the DC bin (sCWatter.cpp:656-674)
-    sol->EF.assign(3 * MF, cd(0, 0));
+    // incident field: the transform of a constant lands on the DC bin (sCWatter.cpp:656-674);
+    // --psf puts E0 on every harmonic (:665-669)
+    p.EF.assign(3 * MF, cd(0, 0));
     for (int c = 0; c < 3; c++)
         for (int a = 0; a < M1; a++)
             for (int b = 0; b < M0; b++)
-                if (prm->psf || (du[a] == 0 && dv[b] == 0)) sol->EF[c * MF + a + b * M1] = e[c];
-
-    DevMem mem(ctx->device);
-    const long long nn = (long long)n * n;
-    const long long YX = (long long)Y * X;
-
-    // ---- Fourier coefficients of n^2 and n^-2 (FourierWave.h:152-195, 283-301) ----
-    // Slice memory read as the X x Y row-major matrix F^T (F[r][c] = data[r + c Y]); the 2-D
-    // DFT crop is tw2^T (M0 x X) . (F^T (X x Y) . tw1^T (Y x M1)), which comes out as the
-    // M1 x M0 crop stored column-major.
-    double2* d_coef = mem.get<double2>((size_t)Zs * 2 * MF);
-    SCW_NEED(d_coef);
-    {
-        std::vector<double2> tw1((size_t)Y * M1), tw2((size_t)M0 * X);
-        for (int r = 0; r < Y; r++)
-            for (int a = 0; a < M1; a++) {
-                const double t = (double)(((long long)du[a] * r) % Y) / Y;
-                tw1[(size_t)r * M1 + a] = make_double2(std::cos(2 * M_PI * t), -std::sin(2 * M_PI * t));
-            }
-        for (int b = 0; b < M0; b++)
-            for (int c = 0; c < X; c++) {
-                const double t = (double)(((long long)dv[b] * c) % X) / X;
-                tw2[(size_t)b * X + c] = make_double2(std::cos(2 * M_PI * t), -std::sin(2 * M_PI * t));
-            }
-        double2* d_data = mem.get<double2>((size_t)Zs * YX);
-        double2* d_F = mem.get<double2>((size_t)Zs * 2 * YX);
-        double2* d_tw1 = mem.get<double2>(tw1.size());
-        double2* d_tw2 = mem.get<double2>(tw2.size());
-        double2* d_T = mem.get<double2>((size_t)Zs * 2 * X * M1);
-        SCW_NEED(d_data);
-        SCW_NEED(d_F);
-        SCW_NEED(d_tw1);
-        SCW_NEED(d_tw2);
-        SCW_NEED(d_T);
-        SCW_CUDA_TRY(cudaMemcpyAsync(d_data, sample, sizeof(double2) * Zs * YX, cudaMemcpyHostToDevice, st));
-        SCW_CUDA_TRY(cudaMemcpyAsync(d_tw1, tw1.data(), sizeof(double2) * tw1.size(), cudaMemcpyHostToDevice, st));
-        SCW_CUDA_TRY(cudaMemcpyAsync(d_tw2, tw2.data(), sizeof(double2) * tw2.size(), cudaMemcpyHostToDevice, st));
-        n2_kernel<<<nblk(Zs * YX), 256, 0, st>>>(d_data, YX, Zs, d_F);
-        SCW_CUDA_TRY(cudaGetLastError());
-        SCW_TRY(zgemm(st, X, M1, Y, kOne, d_F, Y, YX, d_tw1, M1, 0, kZero, d_T, M1, (long long)X * M1, 2 * Zs));
-        SCW_TRY(zgemm(st, M0, M1, X, make_double2(1.0 / (double)YX, 0.0), d_tw2, X, 0, d_T, M1, (long long)X * M1, kZero,
-                      d_coef, M1, MF, 2 * Zs));
-        SCW_CUDA_TRY(cudaStreamSynchronize(st));
-        mem.release(d_data);
-        mem.release(d_F);
-        mem.release(d_T);
-        mem.release(d_tw1);
-        mem.release(d_tw2);
+                if (prm->psf || (du[a] == 0 && dv[b] == 0)) p.EF[c * MF + a + b * M1] = e[c];
+    p.f1EF.resize(4 * MF);
+    for (int m = 0; m < MF; m++) {      // f1 EF (sCWatter.cpp:334-357)
+        const cd ph = std::exp(cd(0, 1) * k * p.zb[0] * p.Sz0[m]);
+        const cd ex = p.EF[m], ey = p.EF[MF + m], ez = p.EF[2 * MF + m];
+        p.f1EF[m] = ph * ex;
+        p.f1EF[MF + m] = ph * ey;
+        p.f1EF[2 * MF + m] = -ph * p.Sz0[m] * ey + ph * p.Sy[m] * ez;
+        p.f1EF[3 * MF + m] = ph * p.Sz0[m] * ex - ph * p.Sx[m] * ez;
     }
+    // twiddles of the cropped DFT bins, phases reduced with integers
+    p.tw1.resize((size_t)Y * M1);
+    p.tw2.resize((size_t)M0 * X);
+    for (int r = 0; r < Y; r++)
+        for (int a = 0; a < M1; a++) {
+            const double t = (double)(((long long)du[a] * r) % Y) / Y;
+            p.tw1[(size_t)r * M1 + a] = cd(std::cos(2 * M_PI * t), -std::sin(2 * M_PI * t));
+        }
+    for (int b = 0; b < M0; b++)
+        for (int c = 0; c < X; c++) {
+            const double t = (double)(((long long)dv[b] * c) % X) / X;
+            p.tw2[(size_t)b * X + c] = cd(std::cos(2 * M_PI * t), -std::sin(2 * M_PI * t));
+        }
+    return SCW_OK;
+}
 
-    // ---- P, Q and the reduced eigenproblem (FourierWave.h:336-397, sCWatter.cpp:248-272) ----
-    int* d_qs = mem.get<int>(M1);
-    int* d_ps = mem.get<int>(M0);
-    double* d_up = mem.get<double>(M0);
-    double* d_wq = mem.get<double>(M1);
-    double* d_dz = mem.get<double>(Zs);
-    double2* d_P = mem.get<double2>((size_t)Zs * (nn + 3 * n));   // P, then eigen work, then U^-1
-    double2* d_Q = mem.get<double2>((size_t)Zs * nn);             // Q, then LU factors
-    double2* d_PQ = mem.get<double2>((size_t)Zs * nn);            // PQ, then W^-1
-    double2* d_U = mem.get<double2>((size_t)Zs * nn);
-    double2* d_W = mem.get<double2>((size_t)Zs * nn);
-    double2* d_lam = mem.get<double2>((size_t)Zs * n);
-    double2* d_gam = mem.get<double2>((size_t)Zs * n);
-    double2* d_E = mem.get<double2>((size_t)Zs * n);
-    int* d_status = mem.get<int>(Zs);
-    int* d_piv = mem.get<int>((size_t)Zs * n + M6);
-    SCW_NEED(d_qs);
-    SCW_NEED(d_ps);
-    SCW_NEED(d_up);
-    SCW_NEED(d_wq);
-    SCW_NEED(d_dz);
-    SCW_NEED(d_P);
-    SCW_NEED(d_Q);
-    SCW_NEED(d_PQ);
-    SCW_NEED(d_U);
-    SCW_NEED(d_W);
-    SCW_NEED(d_lam);
-    SCW_NEED(d_gam);
-    SCW_NEED(d_E);
-    SCW_NEED(d_status);
-    SCW_NEED(d_piv);
-    std::vector<double> dz(Zs);
-    for (int l = 0; l < Zs; l++) dz[l] = (Zs == 1) ? zb[ZL - 1] - zb[0] : zb[l + 1] - zb[l];
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_qs, qs.data(), sizeof(int) * M1, cudaMemcpyHostToDevice, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_ps, ps.data(), sizeof(int) * M0, cudaMemcpyHostToDevice, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_up, up.data(), sizeof(double) * M0, cudaMemcpyHostToDevice, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_wq, wq.data(), sizeof(double) * M1, cudaMemcpyHostToDevice, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_dz, dz.data(), sizeof(double) * Zs, cudaMemcpyHostToDevice, st));
-    build_pq_kernel<<<dim3(nblk(n), n, Zs), 256, 0, st>>>(d_coef, d_up, d_wq, d_qs, d_ps, M0, M1, k, d_P, d_Q);
+void carve_in(const SolvePlan& p, Carver& c, SolveIn& in) {
+    const int MF = p.MF;
+    in.data = c.take<double2>((size_t)p.Z * p.Y * p.X);
+    in.tw1 = c.take<double2>(p.tw1.size());
+    in.tw2 = c.take<double2>(p.tw2.size());
+    in.Sz0 = c.take<double2>(MF);
+    in.Sz1 = c.take<double2>(MF);
+    in.f1EF = c.take<double2>(4 * MF);
+    in.EF = c.take<double2>(3 * MF);
+    in.qs = c.take<int>(p.M1);
+    in.ps = c.take<int>(p.M0);
+    in.up = c.take<double>(p.M0);
+    in.wq = c.take<double>(p.M1);
+    in.dz = c.take<double>(p.Z);
+    in.Sx = c.take<double>(MF);
+    in.Sy = c.take<double>(MF);
+    in.uppz = c.take<double>(MF);
+    in.wqpz = c.take<double>(MF);
+}
+
+void carve_ws(const SolvePlan& p, Carver& c, SolveWs& ws) {
+    const size_t Z = p.Z, MF = p.MF, n = p.n, nn = n * n, N4 = 4 * MF, M3 = 3 * MF, M6 = 6 * MF;
+    ws.coef = c.take<double2>(Z * 2 * MF);
+    ws.P = c.take<double2>(Z * (nn + 3 * n));     // P, then eigen-solver work, then U^-1
+    ws.Q = c.take<double2>(Z * nn);               // Q, then LU factors
+    ws.PQ = c.take<double2>(Z * nn);              // PQ, then W^-1
+    ws.U = c.take<double2>(Z * nn);
+    ws.W = c.take<double2>(Z * nn);
+    ws.lam = c.take<double2>(Z * n);
+    ws.E = c.take<double2>(Z * n);
+    ws.beta = c.take<double2>(Z * N4);
+    ws.v = c.take<double2>(N4);
+    ws.piv = c.take<int>(std::max(Z * n, M6));
+    // temporary region, three overlays
+    const size_t t0 = (c.off + 255) / 256 * 256;
+    Carver ca{c.base, t0};
+    ws.F = ca.take<double2>(2 * Z * (size_t)p.Y * p.X);
+    ws.T = ca.take<double2>(2 * Z * (size_t)p.X * p.M1);
+    Carver cc{c.base, t0};
+    ws.X = cc.take<double2>(N4 * M3);
+    ws.A1 = cc.take<double2>(n * M3);
+    ws.A2 = cc.take<double2>(n * M3);
+    const size_t tA = (cc.off + 255) / 256 * 256;
+    ws.A = cc.take<double2>(M6 * M6);
+    ws.b = cc.take<double2>(M6);
+    Carver cm{c.base, tA};
+    ws.Kn = cm.take<double2>(MF * MF);
+    ws.Hm = cm.take<double2>(MF * n);
+    ws.Qtmp = cm.take<double2>(M3 * n);
+    c.off = std::max(ca.off, std::max(cc.off, cm.off));
+}
+
+void carve_out(const SolvePlan& p, Carver& c, SolveOut& out, bool q64, bool sep) {
+    const size_t Z = p.Z, MF = p.MF, n = p.n;
+    out.x = c.take<double2>(6 * MF);
+    out.gam = c.take<double2>(Z * n);
+    out.status = c.take<int>(3 * Z + 1);
+    out.Q64 = (q64 && !p.external) ? c.take<double2>(Z * 2 * 3 * MF * n) : nullptr;
+    out.Qsep = (sep && !p.external) ? c.take<float2>(Z * 2 * 3 * MF * n) : nullptr;
+    out.sepKz = (sep && !p.external) ? c.take<double2>(Z * 2 * n) : nullptr;
+    out.sepExt = sep ? c.take<double2>(12 * MF) : nullptr;
+}
+
+scw_status upload_inputs(const SolvePlan& p, const double* sample, const SolveIn& in, cudaStream_t st) {
+    auto up = [&](void* dst, const void* src, size_t bytes) -> scw_status {
+        SCW_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+        return SCW_OK;
+    };
+    const size_t MF = p.MF;
+    SCW_TRY(up(in.data, sample, sizeof(double2) * p.Z * p.Y * p.X));
+    SCW_TRY(up(in.tw1, p.tw1.data(), sizeof(double2) * p.tw1.size()));
+    SCW_TRY(up(in.tw2, p.tw2.data(), sizeof(double2) * p.tw2.size()));
+    SCW_TRY(up(in.Sz0, p.Sz0.data(), sizeof(double2) * MF));
+    SCW_TRY(up(in.Sz1, p.Sz1.data(), sizeof(double2) * MF));
+    SCW_TRY(up(in.f1EF, p.f1EF.data(), sizeof(double2) * 4 * MF));
+    SCW_TRY(up(in.EF, p.EF.data(), sizeof(double2) * 3 * MF));
+    SCW_TRY(up(in.qs, p.qs.data(), sizeof(int) * p.M1));
+    SCW_TRY(up(in.ps, p.ps.data(), sizeof(int) * p.M0));
+    SCW_TRY(up(in.up, p.up.data(), sizeof(double) * p.M0));
+    SCW_TRY(up(in.wq, p.wq.data(), sizeof(double) * p.M1));
+    SCW_TRY(up(in.dz, p.dz.data(), sizeof(double) * p.Z));
+    SCW_TRY(up(in.Sx, p.Sx.data(), sizeof(double) * MF));
+    SCW_TRY(up(in.Sy, p.Sy.data(), sizeof(double) * MF));
+    SCW_TRY(up(in.uppz, p.up_pz.data(), sizeof(double) * MF));
+    SCW_TRY(up(in.wqpz, p.wq_pz.data(), sizeof(double) * MF));
+    return SCW_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Recording (launches only): sCWatter.cpp:248-871 restated on the reduced problem
+// ---------------------------------------------------------------------------------------
+scw_status record_solve(const SolvePlan& p, const SolveIn& in, const SolveWs& ws, const SolveOut& out,
+                        cudaStream_t st, long long* launches) {
+    const int Zs = p.Z, Y = p.Y, X = p.X, M0 = p.M0, M1 = p.M1, MF = p.MF, n = p.n;
+    const int N4 = 4 * MF, M3 = 3 * MF, M6 = 6 * MF;
+    const long long nn = (long long)n * n, YX = (long long)Y * X;
+    const double k = p.k;
+    long long L = 0;
+    // Fourier coefficients of n^2 and n^-2 (FourierWave.h:152-195, 283-301): the slice read as
+    // the X x Y row-major matrix F^T (F[r][c] = data[r + c Y]); the 2-D DFT crop is
+    // tw2^T (M0 x X) . (F^T (X x Y) . tw1^T (Y x M1)), the M1 x M0 crop stored column-major
+    n2_kernel<<<nblk(Zs * YX), 256, 0, st>>>(in.data, YX, Zs, ws.F);
     SCW_CUDA_TRY(cudaGetLastError());
-    SCW_TRY(zgemm(st, n, n, n, kOne, d_P, n, nn, d_Q, n, nn, kZero, d_PQ, n, nn, Zs));
-    SCW_TRY(zgeev(st, d_PQ, d_lam, d_U, n, Zs, d_P, d_status));
-    std::vector<int> status(Zs);
-    SCW_CUDA_TRY(cudaMemcpyAsync(status.data(), d_status, sizeof(int) * Zs, cudaMemcpyDeviceToHost, st));
-    SCW_CUDA_TRY(cudaStreamSynchronize(st));
-    for (int l = 0; l < Zs; l++)
-        if (status[l]) return fail(SCW_ERR_NUMERIC, "scw_solve: eigen-solver did not converge for slice " + std::to_string(l));
-    roots_kernel<<<nblk((long long)n * Zs), 256, 0, st>>>(d_lam, n, Zs, d_dz, k, d_gam, d_E);
+    SCW_TRY(zgemm(st, X, M1, Y, kOne, ws.F, Y, YX, in.tw1, M1, 0, kZero, ws.T, M1, (long long)X * M1, 2 * Zs));
+    SCW_TRY(zgemm(st, M0, M1, X, make_double2(1.0 / (double)YX, 0.0), in.tw2, X, 0, ws.T, M1, (long long)X * M1, kZero,
+                  ws.coef, M1, MF, 2 * Zs));
+    // P, Q and the reduced eigenproblem
+    build_pq_kernel<<<dim3(nblk(n), n, Zs), 256, 0, st>>>(ws.coef, in.up, in.wq, in.qs, in.ps, M0, M1, k, ws.P, ws.Q);
+    SCW_CUDA_TRY(cudaGetLastError());
+    SCW_TRY(zgemm(st, n, n, n, kOne, ws.P, n, nn, ws.Q, n, nn, kZero, ws.PQ, n, nn, Zs));
+    SCW_TRY(zgeev(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.P, out.status));
+    roots_kernel<<<nblk((long long)n * Zs), 256, 0, st>>>(ws.lam, n, Zs, in.dz, k, out.gam, ws.E);
     SCW_CUDA_TRY(cudaGetLastError());
     // W = Q U Gamma^-1
-    SCW_TRY(zgemm(st, n, n, n, kOne, d_Q, n, nn, d_U, n, nn, kZero, d_W, n, nn, Zs));
-    coldiv_kernel<<<nblk(nn * Zs), 256, 0, st>>>(d_W, n, d_gam, Zs);
+    SCW_TRY(zgemm(st, n, n, n, kOne, ws.Q, n, nn, ws.U, n, nn, kZero, ws.W, n, nn, Zs));
+    coldiv_kernel<<<nblk(nn * Zs), 256, 0, st>>>(ws.W, n, out.gam, Zs);
     SCW_CUDA_TRY(cudaGetLastError());
+    L += 12;
     // U^-1 into P, W^-1 into PQ (LU factors in Q)
-    double2* d_Uinv = d_P;
-    double2* d_Winv = d_PQ;
+    double2* Uinv = ws.P;
+    double2* Winv = ws.PQ;
     for (int which = 0; which < 2; which++) {
-        double2* inv = which == 0 ? d_Uinv : d_Winv;
+        double2* inv = which == 0 ? Uinv : Winv;
         identity_kernel<<<nblk(nn * Zs), 256, 0, st>>>(inv, n, Zs);
         SCW_CUDA_TRY(cudaGetLastError());
-        SCW_CUDA_TRY(cudaMemcpyAsync(d_Q, which == 0 ? d_U : d_W, sizeof(double2) * nn * Zs, cudaMemcpyDeviceToDevice, st));
-        SCW_TRY(zgetrf(st, d_Q, n, nn, d_piv, n, d_status, Zs, nullptr));
-        SCW_TRY(zgetrs(st, d_Q, n, nn, d_piv, n, inv, n, nn, Zs));
-        SCW_CUDA_TRY(cudaMemcpyAsync(status.data(), d_status, sizeof(int) * Zs, cudaMemcpyDeviceToHost, st));
-        SCW_CUDA_TRY(cudaStreamSynchronize(st));
-        for (int l = 0; l < Zs; l++)
-            if (status[l])
-                return fail(SCW_ERR_NUMERIC, std::string("scw_solve: singular ") + (which ? "W" : "U") +
-                                                 " mode matrix in slice " + std::to_string(l));
+        SCW_CUDA_TRY(cudaMemcpyAsync(ws.Q, which == 0 ? ws.U : ws.W, sizeof(double2) * nn * Zs,
+                                     cudaMemcpyDeviceToDevice, st));
+        SCW_TRY(zgetrf(st, ws.Q, n, nn, ws.piv, n, out.status + (1 + which) * Zs, Zs, nullptr));
+        SCW_TRY(zgetrs(st, ws.Q, n, nn, ws.piv, n, inv, n, nn, Zs));
+        L += 2 + 3 * ((n + 31) / 32);
     }
-    mem.release(d_Q);
-    d_Q = nullptr;
-
-    // ---- T3 = Gd_0 Gc_static^-1 f3 = prod_l V_l diag(E_l^-1, E_l) V_l^-1 f3 ----
-    double* d_Sx = mem.get<double>(MF);
-    double* d_Sy = mem.get<double>(MF);
-    double2* d_Sz0 = mem.get<double2>(MF);
-    double2* d_Sz1 = mem.get<double2>(MF);
-    double2* d_X = mem.get<double2>((size_t)N4 * M3);
-    double2* d_A1 = mem.get<double2>((size_t)n * M3);
-    double2* d_A2 = mem.get<double2>((size_t)n * M3);
-    SCW_NEED(d_Sx);
-    SCW_NEED(d_Sy);
-    SCW_NEED(d_Sz0);
-    SCW_NEED(d_Sz1);
-    SCW_NEED(d_X);
-    SCW_NEED(d_A1);
-    SCW_NEED(d_A2);
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_Sx, sol->Sx.data(), sizeof(double) * MF, cudaMemcpyHostToDevice, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_Sy, sol->Sy.data(), sizeof(double) * MF, cudaMemcpyHostToDevice, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_Sz0, sol->Sz0.data(), sizeof(double2) * MF, cudaMemcpyHostToDevice, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_Sz1, sol->Sz1.data(), sizeof(double2) * MF, cudaMemcpyHostToDevice, st));
-    f3_kernel<<<nblk((long long)N4 * M3), 256, 0, st>>>(d_Sx, d_Sy, d_Sz1, MF, d_X);
+    // T3 = Gd_0 Gc_static^-1 f3 = prod_l V_l diag(E_l^-1, E_l) V_l^-1 f3
+    f3_kernel<<<nblk((long long)N4 * M3), 256, 0, st>>>(in.Sx, in.Sy, in.Sz1, MF, ws.X);
     SCW_CUDA_TRY(cudaGetLastError());
     for (int l = Zs - 1; l >= 0; l--) {
         const long long o = (long long)l * nn;
-        SCW_TRY(zgemm(st, n, M3, n, kOne, d_Uinv + o, n, 0, d_X, M3, 0, kZero, d_A1, M3, 0, 1));
-        SCW_TRY(zgemm(st, n, M3, n, kOne, d_Winv + o, n, 0, d_X + (size_t)n * M3, M3, 0, kZero, d_A2, M3, 0, 1));
-        mix_kernel<<<nblk((long long)n * M3), 256, 0, st>>>(d_A1, d_A2, d_E + (size_t)l * n, n, M3, 0);
+        SCW_TRY(zgemm(st, n, M3, n, kOne, Uinv + o, n, 0, ws.X, M3, 0, kZero, ws.A1, M3, 0, 1));
+        SCW_TRY(zgemm(st, n, M3, n, kOne, Winv + o, n, 0, ws.X + (size_t)n * M3, M3, 0, kZero, ws.A2, M3, 0, 1));
+        mix_kernel<<<nblk((long long)n * M3), 256, 0, st>>>(ws.A1, ws.A2, ws.E + (size_t)l * n, n, M3, 0);
         SCW_CUDA_TRY(cudaGetLastError());
-        SCW_TRY(zgemm(st, n, M3, n, kOne, d_U + o, n, 0, d_A1, M3, 0, kZero, d_X, M3, 0, 1));
-        SCW_TRY(zgemm(st, n, M3, n, kOne, d_W + o, n, 0, d_A2, M3, 0, kZero, d_X + (size_t)n * M3, M3, 0, 1));
+        SCW_TRY(zgemm(st, n, M3, n, kOne, ws.U + o, n, 0, ws.A1, M3, 0, kZero, ws.X, M3, 0, 1));
+        SCW_TRY(zgemm(st, n, M3, n, kOne, ws.W + o, n, 0, ws.A2, M3, 0, kZero, ws.X + (size_t)n * M3, M3, 0, 1));
+        L += 5;
     }
-
-    // ---- boundary system and its solve (sCWatter.cpp:393-461, 722) ----
-    double2* d_A = mem.get<double2>((size_t)M6 * M6);
-    double2* d_b = mem.get<double2>(M6);
-    SCW_NEED(d_A);
-    SCW_NEED(d_b);
-    bc_matrix_kernel<<<nblk((long long)M6 * M6), 256, 0, st>>>(d_Sx, d_Sy, d_Sz0, d_Sz1, d_X, MF, d_A);
+    // boundary system and its solve (sCWatter.cpp:393-461, 722)
+    bc_matrix_kernel<<<nblk((long long)M6 * M6), 256, 0, st>>>(in.Sx, in.Sy, in.Sz0, in.Sz1, ws.X, MF, ws.A);
     SCW_CUDA_TRY(cudaGetLastError());
-    std::vector<cd> f1EF(N4);
-    for (int m = 0; m < MF; m++) {      // f1 EF (sCWatter.cpp:334-357)
-        const cd ph = std::exp(cd(0, 1) * k * zb[0] * sol->Sz0[m]);
-        const cd ex = sol->EF[m], ey = sol->EF[MF + m], ez = sol->EF[2 * MF + m];
-        f1EF[m] = ph * ex;
-        f1EF[MF + m] = ph * ey;
-        f1EF[2 * MF + m] = -ph * sol->Sz0[m] * ey + ph * sol->Sy[m] * ez;
-        f1EF[3 * MF + m] = ph * sol->Sz0[m] * ex - ph * sol->Sx[m] * ez;
+    bc_rhs_kernel<<<nblk(M6), 256, 0, st>>>(in.f1EF, MF, ws.b);
+    SCW_CUDA_TRY(cudaGetLastError());
+    SCW_TRY(zgetrf(st, ws.A, M6, 0, ws.piv, 0, out.status + 3 * Zs, 1, nullptr));
+    SCW_TRY(zgetrs(st, ws.A, M6, 0, ws.piv, 0, ws.b, 1, 0, 1));
+    SCW_CUDA_TRY(cudaMemcpyAsync(out.x, ws.b, sizeof(double2) * M6, cudaMemcpyDeviceToDevice, st));
+    L += 4 + 3 * ((M6 + 31) / 32);
+    if (out.sepExt) {
+        sep_ext_kernel<<<nblk(M3), 256, 0, st>>>(in.EF, out.x, in.Sz0, in.Sz1, MF, k, p.n0, p.n1, out.sepExt);
+        SCW_CUDA_TRY(cudaGetLastError());
+        L++;
     }
-    {
-        std::vector<cd> bh(M6, cd(0, 0));
-        for (int r = 0; r < N4; r++) bh[2 * MF + r] = -f1EF[r];
-        SCW_CUDA_TRY(cudaMemcpyAsync(d_b, bh.data(), sizeof(double2) * M6, cudaMemcpyHostToDevice, st));
-        SCW_TRY(zgetrf(st, d_A, M6, 0, d_piv, 0, d_status, 1, nullptr));
-        SCW_TRY(zgetrs(st, d_A, M6, 0, d_piv, 0, d_b, 1, 0, 1));
-        sol->x.resize(M6);
-        SCW_CUDA_TRY(cudaMemcpyAsync(sol->x.data(), d_b, sizeof(double2) * M6, cudaMemcpyDeviceToHost, st));
-        SCW_CUDA_TRY(cudaMemcpyAsync(status.data(), d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
-        SCW_CUDA_TRY(cudaStreamSynchronize(st));
-        if (status[0]) return fail(SCW_ERR_NUMERIC, "scw_solve: singular boundary system");
-    }
-    mem.release(d_A);
-    sol->gam.resize((size_t)Zs * n);
-    SCW_CUDA_TRY(cudaMemcpyAsync(sol->gam.data(), d_gam, sizeof(double2) * Zs * n, cudaMemcpyDeviceToHost, st));
-    SCW_CUDA_TRY(cudaStreamSynchronize(st));
-    if (sol->external) {
-        ctx->launches += 16 + 4 * Zs;
-        *out = sol.release();
+    if (p.external) {
+        if (launches) *launches += L;
         return SCW_OK;
     }
-
-    // ---- beta: beta_0 = Gd_0^-1 (f1 EF + f2 R),  beta_l = Gd_l^-1 Gc_{l-1} beta_{l-1} (sCWatter.cpp:743-777) ----
-    double2* d_beta = mem.get<double2>((size_t)Zs * N4);
-    double2* d_v = mem.get<double2>(N4);
-    SCW_NEED(d_beta);
-    SCW_NEED(d_v);
-    {
-        std::vector<cd> v4(N4);
-        for (int m = 0; m < MF; m++) {
-            const cd rx = sol->x[m], ry = sol->x[MF + m], rz = sol->x[2 * MF + m];
-            v4[m] = f1EF[m] + rx;
-            v4[MF + m] = f1EF[MF + m] + ry;
-            v4[2 * MF + m] = f1EF[2 * MF + m] + sol->Sz0[m] * ry + sol->Sy[m] * rz;
-            v4[3 * MF + m] = f1EF[3 * MF + m] - sol->Sz0[m] * rx - sol->Sx[m] * rz;
-        }
-        SCW_CUDA_TRY(cudaMemcpyAsync(d_v, v4.data(), sizeof(double2) * N4, cudaMemcpyHostToDevice, st));
-        SCW_CUDA_TRY(cudaStreamSynchronize(st));
-    }
+    // beta: beta_0 = Gd_0^-1 (f1 EF + f2 R),  beta_l = Gd_l^-1 Gc_{l-1} beta_{l-1} (sCWatter.cpp:743-777)
+    beta_init_kernel<<<nblk(MF), 256, 0, st>>>(in.f1EF, out.x, in.Sx, in.Sy, in.Sz0, MF, ws.v);
+    SCW_CUDA_TRY(cudaGetLastError());
     for (int l = 0; l < Zs; l++) {
         const long long o = (long long)l * nn;
-        double2* bl = d_beta + (size_t)l * N4;
+        double2* bl = ws.beta + (size_t)l * N4;
         if (l > 0) {   // v = Gc_{l-1} beta_{l-1} = [U (E bt + bb); W (E bt - bb)]
-            const double2* bp = d_beta + (size_t)(l - 1) * N4;
-            SCW_CUDA_TRY(cudaMemcpyAsync(d_A1, bp, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
-            SCW_CUDA_TRY(cudaMemcpyAsync(d_A2, bp + n, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
-            mix_kernel<<<nblk(n), 256, 0, st>>>(d_A1, d_A2, d_E + (size_t)(l - 1) * n, n, 1, 2);
+            const double2* bp = ws.beta + (size_t)(l - 1) * N4;
+            SCW_CUDA_TRY(cudaMemcpyAsync(ws.A1, bp, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+            SCW_CUDA_TRY(cudaMemcpyAsync(ws.A2, bp + n, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+            mix_kernel<<<nblk(n), 256, 0, st>>>(ws.A1, ws.A2, ws.E + (size_t)(l - 1) * n, n, 1, 2);
             SCW_CUDA_TRY(cudaGetLastError());
-            SCW_TRY(zgemm(st, n, 1, n, kOne, d_U + o - nn, n, 0, d_A1, 1, 0, kZero, d_v, 1, 0, 1));
-            SCW_TRY(zgemm(st, n, 1, n, kOne, d_W + o - nn, n, 0, d_A2, 1, 0, kZero, d_v + n, 1, 0, 1));
+            SCW_TRY(zgemm(st, n, 1, n, kOne, ws.U + o - nn, n, 0, ws.A1, 1, 0, kZero, ws.v, 1, 0, 1));
+            SCW_TRY(zgemm(st, n, 1, n, kOne, ws.W + o - nn, n, 0, ws.A2, 1, 0, kZero, ws.v + n, 1, 0, 1));
+            L += 3;
         }
-        SCW_TRY(zgemm(st, n, 1, n, kOne, d_Uinv + o, n, 0, d_v, 1, 0, kZero, bl, 1, 0, 1));
-        SCW_TRY(zgemm(st, n, 1, n, kOne, d_Winv + o, n, 0, d_v + n, 1, 0, kZero, bl + n, 1, 0, 1));
-        mix_kernel<<<nblk(n), 256, 0, st>>>(bl, bl + n, d_E + (size_t)l * n, n, 1, 1);
+        SCW_TRY(zgemm(st, n, 1, n, kOne, Uinv + o, n, 0, ws.v, 1, 0, kZero, bl, 1, 0, 1));
+        SCW_TRY(zgemm(st, n, 1, n, kOne, Winv + o, n, 0, ws.v + n, 1, 0, kZero, bl + n, 1, 0, 1));
+        mix_kernel<<<nblk(n), 256, 0, st>>>(bl, bl + n, ws.E + (size_t)l * n, n, 1, 1);
         SCW_CUDA_TRY(cudaGetLastError());
+        L += 3;
     }
-    mem.release(d_P);
-    mem.release(d_PQ);
-
-    // ---- Q_check / Q_hat with Ez from the magnetic field (sCWatter.cpp:781-871) ----
-    std::vector<double> up_pz(MF), wq_pz(MF);
-    for (int m = 0; m < MF; m++) {      // built with M_PI here, as in the reference
-        up_pz[m] = 2.0 * ps[m % M0] * M_PI / prm->size[0] + dir[0] * k;
-        wq_pz[m] = 2.0 * qs[m / M0] * M_PI / prm->size[1] + dir[1] * k;
-    }
-    double* d_uppz = mem.get<double>(MF);
-    double* d_wqpz = mem.get<double>(MF);
-    double2* d_Kn = mem.get<double2>((size_t)MF * MF);
-    double2* d_Hm = mem.get<double2>((size_t)MF * n);
-    double2* d_Qall = nullptr;
-    if (cudaMalloc(&d_Qall, sizeof(double2) * (size_t)Zs * 2 * M3 * n) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(SCW_ERR_NOMEM, "scw_solve: cudaMalloc of the mode amplitudes");
-    }
-    sol->dQ = d_Qall;
-    SCW_NEED(d_uppz);
-    SCW_NEED(d_wqpz);
-    SCW_NEED(d_Kn);
-    SCW_NEED(d_Hm);
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_uppz, up_pz.data(), sizeof(double) * MF, cudaMemcpyHostToDevice, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(d_wqpz, wq_pz.data(), sizeof(double) * MF, cudaMemcpyHostToDevice, st));
+    // Q_check / Q_hat with Ez from the magnetic field (sCWatter.cpp:781-871)
     for (int l = 0; l < Zs; l++) {
         const long long o = (long long)l * nn;
-        if (prm->pz) {
-            kn_kernel<<<nblk((long long)MF * MF), 256, 0, st>>>(d_coef + (size_t)l * 2 * MF + MF, M0, M1, -1.0 / k, d_Kn);
+        if (p.pz) {
+            kn_kernel<<<nblk((long long)MF * MF), 256, 0, st>>>(ws.coef + (size_t)l * 2 * MF + MF, M0, M1, -1.0 / k,
+                                                                ws.Kn);
             SCW_CUDA_TRY(cudaGetLastError());
+            L++;
         }
         for (int h = 0; h < 2; h++) {
-            double2* Qo = d_Qall + ((size_t)l * 2 + h) * M3 * n;
-            const double2* beta = d_beta + (size_t)l * N4 + (h ? n : 0);
-            q_rows_kernel<<<nblk(nn), 256, 0, st>>>(d_U + o, d_W + o, beta, MF, h ? -1.0 : 1.0, d_uppz, d_wqpz, Qo,
-                                                   prm->pz ? d_Hm : nullptr);
+            double2* Qo = out.Q64 ? out.Q64 + ((size_t)l * 2 + h) * M3 * n : ws.Qtmp;
+            const double2* beta = ws.beta + (size_t)l * N4 + (h ? n : 0);
+            q_rows_kernel<<<nblk(nn), 256, 0, st>>>(ws.U + o, ws.W + o, beta, MF, h ? -1.0 : 1.0, in.uppz, in.wqpz, Qo,
+                                                   p.pz ? ws.Hm : nullptr);
             SCW_CUDA_TRY(cudaGetLastError());
-            if (prm->pz) {
-                SCW_TRY(zgemm(st, MF, n, MF, kOne, d_Kn, MF, 0, d_Hm, n, 0, kZero, Qo + (size_t)n * n, n, 0, 1));
+            if (p.pz) {
+                SCW_TRY(zgemm(st, MF, n, MF, kOne, ws.Kn, MF, 0, ws.Hm, n, 0, kZero, Qo + (size_t)n * n, n, 0, 1));
             } else {
                 SCW_CUDA_TRY(cudaMemsetAsync(Qo + (size_t)n * n, 0, sizeof(double2) * MF * n, st));
             }
+            if (out.Qsep) {
+                const long long cnt = (long long)M3 * n;
+                to_c64_kernel<<<nblk(cnt), 256, 0, st>>>(Qo, out.Qsep + ((size_t)l * 2 + h) * M3 * n, cnt);
+                SCW_CUDA_TRY(cudaGetLastError());
+                L++;
+            }
+            L += 2;
         }
     }
-    SCW_CUDA_TRY(cudaStreamSynchronize(st));
-    ctx->launches += 16 + 14 * Zs;
+    if (out.sepKz) {
+        sep_kz_kernel<<<nblk((long long)Zs * n), 256, 0, st>>>(out.gam, Zs, n, k, out.sepKz);
+        SCW_CUDA_TRY(cudaGetLastError());
+        L++;
+    }
+    if (launches) *launches += L;
+    return SCW_OK;
+}
+
+}  // namespace sv
+}  // namespace scw
+
+using scw::fail;
+
+static std::string solve_status_message(const std::vector<int>& status, int Z) {
+    for (int l = 0; l < Z; l++)
+        if (status[l]) return "scw_solve: eigen-solver did not converge for slice " + std::to_string(l);
+    for (int l = 0; l < Z; l++)
+        if (status[Z + l]) return "scw_solve: singular U mode matrix in slice " + std::to_string(l);
+    for (int l = 0; l < Z; l++)
+        if (status[2 * Z + l]) return "scw_solve: singular W mode matrix in slice " + std::to_string(l);
+    if (status[3 * Z]) return "scw_solve: singular boundary system";
+    return "";
+}
+
+extern "C" {
+
+scw_status scw_solution_destroy(scw_solution s) {
+    delete s;
+    return SCW_OK;
+}
+
+// sCWatter main (sCWatter.cpp:569-885) on the context's GPU.
+scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, const scw_solve_params* prm,
+                     scw_solution* out) {
+    using namespace scw::sv;
+    if (!ctx || !sample || !prm || !out) return fail(SCW_ERR_ARG, "scw_solve: bad arguments");
+    *out = nullptr;
+    SolvePlan p;
+    scw_status st = plan_solve(prm, Zs, Y, X, p);
+    if (st != SCW_OK) return st;
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    std::unique_ptr<scw_solution_s> sol(new (std::nothrow) scw_solution_s());
+    if (!sol) return fail(SCW_ERR_NOMEM, "host allocation");
+    sol->ctx = ctx;
+    sol->M0 = p.M0;
+    sol->M1 = p.M1;
+    sol->MF = p.MF;
+    sol->Z = Zs;
+    sol->k = p.k;
+    sol->zb = p.zb;
+    sol->external = p.external;
+    sol->n0 = p.n0;
+    sol->n1 = p.n1;
+    sol->Sx = p.Sx;
+    sol->Sy = p.Sy;
+    sol->Sz0 = p.Sz0;
+    sol->Sz1 = p.Sz1;
+    sol->EF = p.EF;
+    // one block for inputs, scratch and the small results; the FP64 mode amplitudes in their own
+    // allocation, owned by the solution
+    SolveIn in{};
+    SolveWs ws{};
+    SolveOut o{};
+    Carver sz;
+    carve_in(p, sz, in);
+    carve_ws(p, sz, ws);
+    carve_out(p, sz, o, false, false);
+    char* blk = nullptr;
+    if (cudaMalloc(&blk, sz.off) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SCW_ERR_NOMEM, "scw_solve: cudaMalloc of " + std::to_string(sz.off >> 20) + " MiB");
+    }
+    std::unique_ptr<char, void (*)(char*)> blk_guard(blk, [](char* q) { cudaFree(q); });
+    Carver c{blk, 0};
+    carve_in(p, c, in);
+    carve_ws(p, c, ws);
+    carve_out(p, c, o, false, false);
+    if (!p.external) {
+        const size_t qbytes = sizeof(double2) * (size_t)Zs * 2 * 3 * p.MF * p.n;
+        if (cudaMalloc(&sol->dQ, qbytes) != cudaSuccess) {
+            cudaGetLastError();
+            sol->dQ = nullptr;
+            return fail(SCW_ERR_NOMEM, "scw_solve: cudaMalloc of the mode amplitudes");
+        }
+        o.Q64 = sol->dQ;
+    }
+    cudaStream_t s = ctx->stream;
+    if ((st = upload_inputs(p, sample, in, s)) != SCW_OK) return st;
+    long long launches = 0;
+    if ((st = record_solve(p, in, ws, o, s, &launches)) != SCW_OK) return st;
+    std::vector<int> status(3 * Zs + 1);
+    sol->x.resize(6 * p.MF);
+    sol->gam.resize((size_t)Zs * p.n);
+    SCW_CUDA_TRY(cudaMemcpyAsync(status.data(), o.status, sizeof(int) * status.size(), cudaMemcpyDeviceToHost, s));
+    SCW_CUDA_TRY(cudaMemcpyAsync(sol->x.data(), o.x, sizeof(double2) * sol->x.size(), cudaMemcpyDeviceToHost, s));
+    SCW_CUDA_TRY(cudaMemcpyAsync(sol->gam.data(), o.gam, sizeof(double2) * sol->gam.size(), cudaMemcpyDeviceToHost, s));
+    SCW_CUDA_TRY(cudaStreamSynchronize(s));
+    ctx->launches += launches;
+    const std::string msg = solve_status_message(status, Zs);
+    if (!msg.empty()) return fail(SCW_ERR_NUMERIC, msg);
     *out = sol.release();
     return SCW_OK;
 }

@@ -48,6 +48,7 @@ typedef struct scw_cw_s* scw_cw;         /* host CoupledWaveStructure<double> */
 typedef struct scw_waves_s* scw_waves;   /* device-resident unpacked wave set */
 typedef struct scw_sep_s* scw_sep;       /* device-resident separable (factored) coefficient set */
 typedef struct scw_solution_s* scw_solution; /* result of the per-layer coupled-wave solve */
+typedef struct scw_batch_s* scw_batch;       /* many samples solved + evaluated by one CUDA graph */
 
 /* Output-GEMM methods of the separable evaluator */
 #define SCW_SEP_FP32 1      /* FP32 SIMT */
@@ -234,6 +235,37 @@ SCW_API scw_status scw_solution_get_modes(scw_solution s, int l, double* Q_check
 SCW_API scw_status scw_solution_to_sep(scw_solution s, scw_sep* out);
 /* The .cw structure that sCWatter writes (sCWatter.cpp:890-956). */
 SCW_API scw_status scw_solution_to_cw(scw_solution s, scw_cw* out);
+
+/* ---------------------------------------------------------------------------------- */
+/* Batched solve + evaluate (no counterpart in the reference, which solves one sample   */
+/* per sCWatter run): every item is solved (FP64) and its field volume evaluated with   */
+/* the separable evaluator; the whole batch is captured once into a CUDA graph.         */
+/* ---------------------------------------------------------------------------------- */
+typedef struct scw_batch_item {
+    const double* sample;  /* [Z][Y][X] complex128 refractive index, host; read during create */
+    int Z, Y, X;
+    scw_solve_params prm;
+    float x0, y0, z0;      /* evaluation grid: point (i, j, k) = (x0 + dx i, y0 + dy j, z0 + dz k) */
+    float dx, dy, dz;
+    int Nx, Ny, Nz;
+} scw_batch_item;
+/* lanes: concurrent streams (0 = autotune); method: SCW_SEP_* output GEMM (0 = autotune).
+ * Plans, uploads, autotunes on a stratified subset, and captures the graph. */
+SCW_API scw_status scw_batch_create(scw_ctx ctx, const scw_batch_item* items, int count, int lanes, int method,
+                                    scw_batch* out);
+/* One cudaGraphLaunch on the context stream (asynchronous). */
+SCW_API scw_status scw_batch_run(scw_batch b);
+/* Waits; item_status (count ints, may be NULL): 0, SCW_ERR_NUMERIC or SCW_ERR_TIMEOUT. */
+SCW_API scw_status scw_batch_wait(scw_batch b, int* item_status);
+/* x: 6MF complex; gamma: Z x 2MF complex; field_host: [Nz][Ny][Nx][3] complex64; any may be NULL. */
+SCW_API scw_status scw_batch_get(scw_batch b, int i, double* x, double* gamma, float* field_host, float** field_device);
+/* harmonics, slices and points x modes of the item's volume */
+SCW_API scw_status scw_batch_item_info(scw_batch b, int i, int* M0, int* M1, int* n_slices, int64_t* points_modes);
+/* chosen lanes / method, graph nodes, kernels per launch, tuning time and its log
+ * (triples lanes, method, ms; n_tune entries). */
+SCW_API scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int64_t* graph_nodes, int64_t* kernels,
+                                  double* tune_ms, double* tune_log, int* n_tune);
+SCW_API scw_status scw_batch_destroy(scw_batch b);
 
 #ifdef __cplusplus
 }

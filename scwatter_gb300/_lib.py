@@ -70,6 +70,13 @@ _SIGS = {
     "scw_solution_get_modes": [P, I32, P, P],
     "scw_solution_to_sep": [P, PP],
     "scw_solution_to_cw": [P, PP],
+    "scw_batch_create": [P, P, I32, I32, I32, PP],
+    "scw_batch_run": [P],
+    "scw_batch_wait": [P, P],
+    "scw_batch_get": [P, I32, P, P, P, PP],
+    "scw_batch_item_info": [P, I32, P, P, P, P],
+    "scw_batch_info": [P, P, P, P, P, P, P, P],
+    "scw_batch_destroy": [P],
     "scw_sep_create": [P, I32, I32, I32, I32, P, P, P, PP],
     "scw_sep_destroy": [P],
     "scw_sep_set_exterior": [P, P, P, P, P, P, P],

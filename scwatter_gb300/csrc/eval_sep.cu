@@ -336,19 +336,18 @@ static float host_coord(float s, float d, int i) {
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
-// Stage 1 for a list of z-values: fills C [nz][3][MF] in the context's scratch.
-static scw_status stage1(scw_sep s, const std::vector<float>& zlist, float2* dC, char*& cursor) {
-    scw_ctx ctx = s->ctx;
-    const int MF = s->MF, J = s->Jp;          // device row stride (even)
-    std::vector<PGroup> groups;
-    std::vector<int2> ext;
+// Stage-1 plan: the z-planes grouped by region (up to kMaxGroup planes of one region share a
+// pass over that region's Q), exterior planes listed apart.
+static void stage1_plan(const scw_sep_s* s, SepEvalPlan& p) {
     std::map<int64_t, std::vector<int>> by_region;
-    for (int i = 0; i < (int)zlist.size(); i++) by_region[sep_region(s, zlist[i])].push_back(i);
-    int max_nk = 1;
+    for (int i = 0; i < (int)p.zlist.size(); i++) by_region[sep_region(s, p.zlist[i])].push_back(i);
+    p.max_nk = 1;
+    p.groups.clear();
+    p.ext.clear();
     for (auto& kv : by_region) {
         const int64_t r = kv.first;
         if (r == 0 || r == s->Z + 1) {
-            for (int zi : kv.second) ext.push_back(make_int2(zi, r == 0 ? 0 : 1));
+            for (int zi : kv.second) p.ext.push_back(make_int2(zi, r == 0 ? 0 : 1));
             continue;
         }
         for (size_t o = 0; o < kv.second.size(); o += kMaxGroup) {
@@ -356,29 +355,33 @@ static scw_status stage1(scw_sep s, const std::vector<float>& zlist, float2* dC,
             g.region = (int)r;
             g.nk = (int)std::min<size_t>(kMaxGroup, kv.second.size() - o);
             for (int kk = 0; kk < g.nk; kk++) g.zi[kk] = kv.second[o + kk];
-            max_nk = std::max(max_nk, g.nk);
-            groups.push_back(g);
+            p.max_nk = std::max(p.max_nk, g.nk);
+            p.groups.push_back(g);
         }
     }
-    // descriptors to the device (pinned staging, guarded by the context's event)
-    const size_t gbytes = groups.size() * sizeof(PGroup), ebytes = ext.size() * sizeof(int2),
-                 zbytes = zlist.size() * sizeof(float);
-    const size_t off_e = align256(gbytes), off_z = off_e + align256(ebytes), total = off_z + align256(zbytes);
-    SCW_CUDA_TRY(cudaEventSynchronize(ctx->desc_done));
-    scw_status st = ctx->host_desc.reserve(total);
-    if (st != SCW_OK) return st;
-    st = ctx->desc.reserve(total);
-    if (st != SCW_OK) return st;
-    char* h = (char*)ctx->host_desc.ptr;
-    if (gbytes) std::memcpy(h, groups.data(), gbytes);
-    if (ebytes) std::memcpy(h + off_e, ext.data(), ebytes);
-    std::memcpy(h + off_z, zlist.data(), zbytes);
-    SCW_CUDA_TRY(cudaMemcpyAsync(ctx->desc.ptr, h, total, cudaMemcpyHostToDevice, ctx->stream));
-    SCW_CUDA_TRY(cudaEventRecord(ctx->desc_done, ctx->stream));
-    const PGroup* dg = (const PGroup*)ctx->desc.ptr;
-    const int2* de = (const int2*)((char*)ctx->desc.ptr + off_e);
-    const float* dz = (const float*)((char*)ctx->desc.ptr + off_z);
+    const size_t gbytes = p.groups.size() * sizeof(PGroup), ebytes = p.ext.size() * sizeof(int2),
+                 zbytes = p.zlist.size() * sizeof(float);
+    p.off_e = align256(gbytes);
+    p.off_z = p.off_e + align256(ebytes);
+    p.desc_bytes = p.off_z + align256(zbytes);
+}
 
+void sep_eval_desc(const SepEvalPlan& p, char* h) {
+    if (!p.groups.empty()) std::memcpy(h, p.groups.data(), p.groups.size() * sizeof(PGroup));
+    if (!p.ext.empty()) std::memcpy(h + p.off_e, p.ext.data(), p.ext.size() * sizeof(int2));
+    std::memcpy(h + p.off_z, p.zlist.data(), p.zlist.size() * sizeof(float));
+}
+
+// Stage 1 for the plan's z-values: fills C [nz][3][MF]; descriptors already on the device.
+static scw_status stage1_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, float2* dC, char* cursor) {
+    scw_ctx ctx = s->ctx;
+    const int MF = s->MF, J = s->Jp;          // device row stride (even)
+    const auto& groups = p.groups;
+    const auto& ext = p.ext;
+    const int max_nk = p.max_nk;
+    const PGroup* dg = (const PGroup*)d_desc;
+    const int2* de = (const int2*)(d_desc + p.off_e);
+    const float* dz = (const float*)(d_desc + p.off_z);
     if (!groups.empty()) {
         if (J > 0) {
             const int nks = max_nk <= 1 ? 1 : max_nk <= 2 ? 2 : max_nk <= 4 ? 4 : 8;
@@ -467,51 +470,68 @@ scw_status sep_synth(scw_ctx ctx, const float2* T, const float2* F, int nrows, i
     return SCW_OK;
 }
 
-// One evaluation "sheet" family: a volume of xy planes, or an xz / yz plane.
-scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, float db, float dz, int Na, int Nb,
-                    int Nz, float* dE, int method) {
-    scw_ctx ctx = s->ctx;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+// One evaluation "sheet" family: a volume of xy planes, or an xz / yz plane.  Host-only plan.
+scw_status sep_eval_plan(const scw_sep_s* s, int kind, float a0, float b0, float c, float da, float db, float dz,
+                         int Na, int Nb, int Nz, int method, SepEvalPlan& p) {
     const int M0 = s->M0, M1 = s->M1, MF = s->MF;
-    // z-values needed
-    std::vector<float> zlist;
+    p.kind = kind;
+    p.a0 = a0;
+    p.b0 = b0;
+    p.c = c;
+    p.da = da;
+    p.db = db;
+    p.dz = dz;
+    p.Na = Na;
+    p.Nb = Nb;
+    p.Nz = Nz;
+    p.method = method;
+    p.zlist.clear();
     if (kind == 0) {            // volume: Nz xy planes at z = c + dz*k; a = x (Na), b = y (Nb)
-        for (int k = 0; k < Nz; k++) zlist.push_back(host_coord(c, dz, k));
+        for (int k = 0; k < Nz; k++) p.zlist.push_back(host_coord(c, dz, k));
     } else {                    // kind 1: xz plane at y = c (a = x, rows = z); kind 2: yz plane at x = c (a = y)
-        for (int k = 0; k < Nb; k++) zlist.push_back(host_coord(b0, db, k));
+        for (int k = 0; k < Nb; k++) p.zlist.push_back(host_coord(b0, db, k));
     }
-    const int nz = (int)zlist.size();
-    // scratch layout
-    int nrows = 0, ncols = 0, Mk = 0;
-    if (kind == 0) { nrows = Nz * Nb; ncols = Na; Mk = M0; }
-    else if (kind == 1) { nrows = Nb; ncols = Na; Mk = M0; }
-    else { nrows = Nb; ncols = Na; Mk = M1; }
-    // phases for the PGroups: at most nz groups
-    const size_t phi_bytes = align256((size_t)nz * 2 * (size_t)s->Jp * kMaxGroup * sizeof(float2));
-    const size_t c_bytes = align256((size_t)nz * 3 * MF * sizeof(float2));
-    // slack past the last row: the tensor-core producer reads whole 16-row tiles of T
-    const size_t t_bytes = align256((size_t)nrows * 3 * Mk * sizeof(float2) + 16 * 3 * 64 * sizeof(float2) + 4096);
-    const size_t tab_bytes = align256((size_t)(M0 + M1) * (Na + Nb + 2) * sizeof(float2));
-    scw_status st = ctx->sep_scratch.reserve(phi_bytes + c_bytes + t_bytes + 2 * tab_bytes);
-    if (st != SCW_OK) return st;
-    char* cursor = (char*)ctx->sep_scratch.ptr;
-    float2* dC = (float2*)cursor;
-    cursor += c_bytes;
-    float2* dT = (float2*)cursor;
-    cursor += t_bytes;
-    float2* tabA = (float2*)cursor;
-    cursor += tab_bytes;
-    float2* tabB = (float2*)cursor;
-    cursor += tab_bytes;
-    st = stage1(s, zlist, dC, cursor);
-    if (st != SCW_OK) return st;
+    const int nz = (int)p.zlist.size();
+    if (kind == 0) { p.nrows = Nz * Nb; p.ncols = Na; p.Mk = M0; }
+    else if (kind == 1) { p.nrows = Nb; p.ncols = Na; p.Mk = M0; }
+    else { p.nrows = Nb; p.ncols = Na; p.Mk = M1; }
     if (kind == 0) {
+        const size_t smem = (size_t)(3 * M0 * M1 + kRowsBlk * M1) * sizeof(float2);
+        if (smem > 200 * 1024) return fail(SCW_ERR_UNSUPPORTED, "harmonic grid too large for the row stage");
+    }
+    // phases for the PGroups: at most nz groups
+    p.phi_bytes = align256((size_t)nz * 2 * (size_t)s->Jp * kMaxGroup * sizeof(float2));
+    p.c_bytes = align256((size_t)nz * 3 * MF * sizeof(float2));
+    // slack past the last row: the tensor-core producer reads whole 16-row tiles of T
+    p.t_bytes = align256((size_t)p.nrows * 3 * p.Mk * sizeof(float2) + 16 * 3 * 64 * sizeof(float2) + 4096);
+    p.tab_bytes = align256((size_t)(M0 + M1) * (Na + Nb + 2) * sizeof(float2));
+    p.scratch_bytes = p.phi_bytes + p.c_bytes + p.t_bytes + 2 * p.tab_bytes;
+    stage1_plan(s, p);
+    return SCW_OK;
+}
+
+// Launches of one planned evaluation (no allocation, no host synchronisation).
+scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, char* scratch, float* dE) {
+    scw_ctx ctx = s->ctx;
+    const int M0 = s->M0, M1 = s->M1;
+    char* cursor = scratch;
+    float2* dC = (float2*)cursor;
+    cursor += p.c_bytes;
+    float2* dT = (float2*)cursor;
+    cursor += p.t_bytes;
+    float2* tabA = (float2*)cursor;
+    cursor += p.tab_bytes;
+    float2* tabB = (float2*)cursor;
+    cursor += p.tab_bytes;
+    scw_status st = stage1_record(s, p, d_desc, dC, cursor);
+    if (st != SCW_OK) return st;
+    const int nrows = p.nrows, ncols = p.ncols, Mk = p.Mk, Na = p.Na, Nb = p.Nb, Nz = p.Nz;
+    if (p.kind == 0) {
         // F = Ex table [a][x]; R = Ey table [b][y]
-        if ((st = launch_table(ctx, s->dkx, M0, a0, da, Na, tabA)) != SCW_OK) return st;
-        if ((st = launch_table(ctx, s->dky, M1, b0, db, Nb, tabB)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dkx, M0, p.a0, p.da, Na, tabA)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dky, M1, p.b0, p.db, Nb, tabB)) != SCW_OK) return st;
         {
             const size_t smem = (size_t)(3 * M0 * M1 + kRowsBlk * M1) * sizeof(float2);
-            if (smem > 200 * 1024) return fail(SCW_ERR_UNSUPPORTED, "harmonic grid too large for the row stage");
             SCW_CUDA_TRY(cudaFuncSetAttribute(sep_rows_volume_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem));
             dim3 grid((Nb + kRowsBlk - 1) / kRowsBlk, Nz);
@@ -520,20 +540,38 @@ scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, 
             SCW_CUDA_TRY(cudaGetLastError());
             ctx->launches++;
         }
-        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, method);
-    } else if (kind == 1) {
+        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, p.method);
+    } else if (p.kind == 1) {
         // xz plane at y = c: R = Ey(c) [b]; F = Ex table [a][x]
-        if ((st = launch_table(ctx, s->dkx, M0, a0, da, Na, tabA)) != SCW_OK) return st;
-        if ((st = launch_table(ctx, s->dky, M1, c, 0.f, 1, tabB)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dkx, M0, p.a0, p.da, Na, tabA)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dky, M1, p.c, 0.f, 1, tabB)) != SCW_OK) return st;
         if ((st = launch_rows(ctx, dC, tabB, 1, 1, 1, 0, nrows, 0, M0, M1, dT)) != SCW_OK) return st;
-        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, method);
+        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, p.method);
     } else {
         // yz plane at x = c: R = Ex(c) [a]; F = Ey table [b][y]
-        if ((st = launch_table(ctx, s->dky, M1, a0, da, Na, tabA)) != SCW_OK) return st;
-        if ((st = launch_table(ctx, s->dkx, M0, c, 0.f, 1, tabB)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dky, M1, p.a0, p.da, Na, tabA)) != SCW_OK) return st;
+        if ((st = launch_table(ctx, s->dkx, M0, p.c, 0.f, 1, tabB)) != SCW_OK) return st;
         if ((st = launch_rows(ctx, dC, tabB, 1, 1, 1, 0, nrows, 1, M0, M1, dT)) != SCW_OK) return st;
-        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, method);
+        return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, p.method);
     }
+}
+
+scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, float db, float dz, int Na, int Nb,
+                    int Nz, float* dE, int method) {
+    scw_ctx ctx = s->ctx;
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SepEvalPlan p;
+    scw_status st = sep_eval_plan(s, kind, a0, b0, c, da, db, dz, Na, Nb, Nz, method, p);
+    if (st != SCW_OK) return st;
+    if ((st = ctx->sep_scratch.reserve(p.scratch_bytes)) != SCW_OK) return st;
+    // descriptors to the device (pinned staging, guarded by the context's event)
+    SCW_CUDA_TRY(cudaEventSynchronize(ctx->desc_done));
+    if ((st = ctx->host_desc.reserve(p.desc_bytes)) != SCW_OK) return st;
+    if ((st = ctx->desc.reserve(p.desc_bytes)) != SCW_OK) return st;
+    sep_eval_desc(p, (char*)ctx->host_desc.ptr);
+    SCW_CUDA_TRY(cudaMemcpyAsync(ctx->desc.ptr, ctx->host_desc.ptr, p.desc_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    SCW_CUDA_TRY(cudaEventRecord(ctx->desc_done, ctx->stream));
+    return sep_eval_record(s, p, (const char*)ctx->desc.ptr, (char*)ctx->sep_scratch.ptr, dE);
 }
 
 }  // namespace scw

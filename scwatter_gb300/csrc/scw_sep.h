@@ -17,6 +17,26 @@ struct PGroup {
     int zi[kMaxGroup];
 };
 
+// A planned evaluation of a separable set: the z-planes, their stage-1 grouping, the device
+// descriptor block (groups, exterior planes, z-values) and the scratch it needs.
+struct SepEvalPlan {
+    int kind = 0, Na = 0, Nb = 0, Nz = 0, method = 0;
+    float a0 = 0, b0 = 0, c = 0, da = 0, db = 0, dz = 0;
+    std::vector<float> zlist;
+    std::vector<PGroup> groups;
+    std::vector<int2> ext;
+    int max_nk = 1;
+    size_t off_e = 0, off_z = 0, desc_bytes = 0;
+    int nrows = 0, ncols = 0, Mk = 0;
+    size_t phi_bytes = 0, c_bytes = 0, t_bytes = 0, tab_bytes = 0, scratch_bytes = 0;
+};
+// kind 0: Nz xy planes (a = x, b = y); 1: xz plane at y = c; 2: yz plane at x = c
+scw_status sep_eval_plan(const scw_sep_s* s, int kind, float a0, float b0, float c, float da, float db, float dz,
+                         int Na, int Nb, int Nz, int method, SepEvalPlan& p);
+void sep_eval_desc(const SepEvalPlan& p, char* host);
+// launches only, on the set's context stream
+scw_status sep_eval_record(scw_sep_s* s, const SepEvalPlan& p, const char* d_desc, char* scratch, float* dE);
+
 // output GEMM of stage 2: E[r][col][c] = sum_m T[r][c][m] F[m][col]
 scw_status sep_synth(scw_ctx ctx, const float2* T, const float2* F, int nrows, int ncols, int Mk, float* out,
                      int method);

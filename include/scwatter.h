@@ -49,6 +49,7 @@ typedef struct scw_waves_s* scw_waves;   /* device-resident unpacked wave set */
 typedef struct scw_sep_s* scw_sep;       /* device-resident separable (factored) coefficient set */
 typedef struct scw_solution_s* scw_solution; /* result of the per-layer coupled-wave solve */
 typedef struct scw_batch_s* scw_batch;       /* many samples solved + evaluated by one CUDA graph */
+typedef struct scw_mlp_s* scw_mlp;           /* small fully connected network (FP32) */
 
 /* Output-GEMM methods of the separable evaluator */
 #define SCW_SEP_FP32 1      /* FP32 SIMT */
@@ -266,6 +267,37 @@ SCW_API scw_status scw_batch_item_info(scw_batch b, int i, int* M0, int* M1, int
 SCW_API scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int64_t* graph_nodes, int64_t* kernels,
                                   double* tune_ms, double* tune_log, int* n_tune);
 SCW_API scw_status scw_batch_destroy(scw_batch b);
+
+/* ---------------------------------------------------------------------------------- */
+/* Learned eigen warm start (no counterpart in the reference, whose eigen-solve is one   */
+/* zgeev per slice, sCWatter.cpp:248-272)                                               */
+/* ---------------------------------------------------------------------------------- */
+/* Layer problems of a sample without the solve: Fourier crops of n^2 and n^-2 per slice
+ * (coef: DEVICE Z x 2 x MF complex, column-major M1 x M0 crops) and the reduced matrices PQ
+ * (DEVICE Z x 2MF x 2MF complex); both may be NULL (harmonic counts only). */
+SCW_API scw_status scw_layer_problem(scw_ctx ctx, const double* sample, int Z, int Y, int X,
+                                     const scw_solve_params* prm, int* M0, int* M1, void* coef, void* PQ);
+/* Network y = W3 relu(W2 relu(W1 x + b1) + b2) + b3 (FP32), He-uniform initialisation. */
+SCW_API scw_status scw_mlp_create(scw_ctx ctx, int n_in, int width, int n_out, uint64_t seed, scw_mlp* out);
+SCW_API scw_status scw_mlp_destroy(scw_mlp m);
+SCW_API scw_status scw_mlp_info(scw_mlp m, int* n_in, int* width, int* n_out, int64_t* n_params);
+/* parameters as one host vector: W1 [width][n_in], b1, W2 [width][width], b2, W3 [n_out][width], b3 */
+SCW_API scw_status scw_mlp_get_params(scw_mlp m, float* host);
+SCW_API scw_status scw_mlp_set_params(scw_mlp m, const float* host);
+/* X: DEVICE [B][n_in] float, Y: DEVICE [B][n_out] float (asynchronous) */
+SCW_API scw_status scw_mlp_forward(scw_mlp m, const float* X, int B, float* Y);
+/* gradient of the mean squared error against T (DEVICE [B][n_out]) into grad_host (n_params) */
+SCW_API scw_status scw_mlp_gradients(scw_mlp m, const float* X, const float* T, int B, float* grad_host, double* loss);
+/* one Adam step (beta 0.9 / 0.999); loss before the step to *loss (may be NULL; synchronises if not) */
+SCW_API scw_status scw_mlp_train_step(scw_mlp m, const float* X, const float* T, int B, float lr, double* loss);
+/* Eigenpairs of a batch of n x n matrices (DEVICE, not modified) from one shift per eigenvalue
+ * (DEVICE batch x n complex): Rayleigh-quotient iteration on the Hessenberg form, one warp per
+ * eigenpair.  A matrix is accepted when every pair has ||A v - lambda v|| <= tol ||A||_F ||v||
+ * and no two pairs share an eigenvector; otherwise the plain eigen-solver replaces it.
+ * W: DEVICE batch x n, V: DEVICE batch x n x n (columns).  accepted_host: batch ints (may be
+ * NULL); stats_host: [mean iterations, largest accepted residual, accepted, fallen back]. */
+SCW_API scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A, int batch, const void* shifts, int max_it,
+                                double tol, void* W, void* V, int* accepted_host, double* stats_host);
 
 #ifdef __cplusplus
 }

@@ -201,11 +201,10 @@ lu_swap_trsm_kernel(double2* __restrict__ A, int n, int lda, long long sA, int k
     }
 }
 
-// solve A X = B with the LU factors (B: n x nrhs, row-major, in place), one CTA column block
+// Row interchanges of B from zgetrf's pivots (LAPACK laswp order), one thread per column.
 __global__ void __launch_bounds__(256)
-lu_solve_kernel(const double2* __restrict__ LU, int n, int lda, long long sA, const int* __restrict__ piv,
-                long long sP, double2* __restrict__ B, int ldb, long long sB, int nrhs) {
-    LU += sA * blockIdx.y;
+laswp_kernel(const int* __restrict__ piv, long long sP, double2* __restrict__ B, int ldb, long long sB, int n,
+             int nrhs) {
     piv += sP * blockIdx.y;
     B += sB * blockIdx.y;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -218,17 +217,32 @@ lu_solve_kernel(const double2* __restrict__ LU, int n, int lda, long long sA, co
             B[(long long)p * ldb + j] = t;
         }
     }
-    for (int i = 0; i < n; i++) {                            // forward: unit L
-        double2 v = B[(long long)i * ldb + j];
-        const double2* row = LU + (long long)i * lda;
-        for (int m = 0; m < i; m++) v = csub(v, cmul(row[m], B[(long long)m * ldb + j]));
-        B[(long long)i * ldb + j] = v;
-    }
-    for (int i = n - 1; i >= 0; i--) {                       // backward: U
-        double2 v = B[(long long)i * ldb + j];
-        const double2* row = LU + (long long)i * lda;
-        for (int m = i + 1; m < n; m++) v = csub(v, cmul(row[m], B[(long long)m * ldb + j]));
-        B[(long long)i * ldb + j] = cdiv(v, row[i]);
+}
+
+// Triangular solve restricted to the diagonal block rows [k0, k0 + nb) of the LU factors, one
+// thread per right-hand-side column: unit lower L (upper == 0) or U (upper == 1).  Rows
+// outside the block were already folded in by the GEMM updates of the blocked solve.
+__global__ void __launch_bounds__(256)
+trsm_block_kernel(const double2* __restrict__ LU, int lda, long long sA, int k0, int nb, double2* __restrict__ B,
+                  int ldb, long long sB, int nrhs, int upper) {
+    LU += sA * blockIdx.y;
+    B += sB * blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nrhs) return;
+    if (!upper) {
+        for (int i = k0; i < k0 + nb; i++) {
+            double2 v = B[(long long)i * ldb + j];
+            const double2* row = LU + (long long)i * lda;
+            for (int m = k0; m < i; m++) v = csub(v, cmul(row[m], B[(long long)m * ldb + j]));
+            B[(long long)i * ldb + j] = v;
+        }
+    } else {
+        for (int i = k0 + nb - 1; i >= k0; i--) {
+            double2 v = B[(long long)i * ldb + j];
+            const double2* row = LU + (long long)i * lda;
+            for (int m = i + 1; m < k0 + nb; m++) v = csub(v, cmul(row[m], B[(long long)m * ldb + j]));
+            B[(long long)i * ldb + j] = cdiv(v, row[i]);
+        }
     }
 }
 
@@ -591,9 +605,40 @@ scw_status zgetrf(cudaStream_t st, double2* A, int n, long long sA, int* piv, lo
 
 scw_status zgetrs(cudaStream_t st, const double2* LU, int n, long long sA, const int* piv, long long sP, double2* B,
                   int nrhs, long long sB, int batch) {
+    // blocked: per diagonal block a small triangular solve, the rest of the rows updated by GEMM
     if (n <= 0 || nrhs <= 0 || batch <= 0) return SCW_OK;
-    dim3 g((nrhs + 255) / 256, batch);
-    z::lu_solve_kernel<<<g, 256, 0, st>>>(LU, n, n, sA, piv, sP, B, nrhs, sB, nrhs);
+    constexpr int kTB = 64;
+    const dim3 g((nrhs + 255) / 256, batch);
+    z::laswp_kernel<<<g, 256, 0, st>>>(piv, sP, B, nrhs, sB, n, nrhs);
+    SCW_CUDA_TRY(cudaGetLastError());
+    for (int k0 = 0; k0 < n; k0 += kTB) {
+        const int nb = std::min(kTB, n - k0);
+        z::trsm_block_kernel<<<g, 256, 0, st>>>(LU, n, sA, k0, nb, B, nrhs, sB, nrhs, 0);
+        SCW_CUDA_TRY(cudaGetLastError());
+        const int rem = n - k0 - nb;
+        if (rem > 0) {
+            scw_status s = zgemm(st, rem, nrhs, nb, make_double2(-1.0, 0.0), LU + (long long)(k0 + nb) * n + k0, n, sA,
+                                 B + (long long)k0 * nrhs, nrhs, sB, make_double2(1.0, 0.0),
+                                 B + (long long)(k0 + nb) * nrhs, nrhs, sB, batch);
+            if (s != SCW_OK) return s;
+        }
+    }
+    for (int k0 = ((n - 1) / kTB) * kTB; k0 >= 0; k0 -= kTB) {
+        const int nb = std::min(kTB, n - k0);
+        z::trsm_block_kernel<<<g, 256, 0, st>>>(LU, n, sA, k0, nb, B, nrhs, sB, nrhs, 1);
+        SCW_CUDA_TRY(cudaGetLastError());
+        if (k0 > 0) {
+            scw_status s = zgemm(st, k0, nrhs, nb, make_double2(-1.0, 0.0), LU + k0, n, sA, B + (long long)k0 * nrhs,
+                                 nrhs, sB, make_double2(1.0, 0.0), B, nrhs, sB, batch);
+            if (s != SCW_OK) return s;
+        }
+    }
+    return SCW_OK;
+}
+
+scw_status zgehrd(cudaStream_t st, double2* A, double2* Q, int n, int batch, double2* work) {
+    if (n <= 0 || batch <= 0) return SCW_OK;
+    z::hessenberg_kernel<<<batch, 1024, 0, st>>>(A, Q, n, (long long)n * n, work);
     SCW_CUDA_TRY(cudaGetLastError());
     return SCW_OK;
 }

@@ -28,6 +28,9 @@ scw_status zgetrf(cudaStream_t st, double2* A, int n, long long sA, int* piv, lo
 // B := A^-1 B using zgetrf's factors (B: n x nrhs, leading dimension nrhs)
 scw_status zgetrs(cudaStream_t st, const double2* LU, int n, long long sA, const int* piv, long long sP, double2* B,
                   int nrhs, long long sB, int batch);
+// Hessenberg form of A (in place, n x n per batch entry) and the unitary Q (A = Q H Q^H);
+// work >= batch * 3 n
+scw_status zgehrd(cudaStream_t st, double2* A, double2* Q, int n, int batch, double2* work);
 // eigenvalues W and right eigenvectors V (columns) of A (overwritten); work >= batch (n^2 + 3 n)
 scw_status zgeev(cudaStream_t st, double2* A, double2* W, double2* V, int n, int batch, double2* work, int* status);
 

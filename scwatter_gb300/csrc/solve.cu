@@ -812,6 +812,61 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
     return SCW_OK;
 }
 
+// The layer problems of a sample without solving them: per slice the M1 x M0 Fourier crops
+// of n^2 and n^-2 (column-major, FourierWave.h:152-195) and the reduced matrix PQ
+// (2MF x 2MF, FourierWave.h:336-397), written to caller-provided DEVICE buffers
+// (coef: Z x 2 x MF complex, PQ: Z x 2MF x 2MF complex).  Either may be NULL (M0 / M1 only).
+scw_status scw_layer_problem(scw_ctx ctx, const double* sample, int Zs, int Y, int X, const scw_solve_params* prm,
+                             int* M0, int* M1, void* coef, void* PQ) {
+    using namespace scw::sv;
+    if (!ctx || !prm) return fail(SCW_ERR_ARG, "scw_layer_problem: bad arguments");
+    SolvePlan p;
+    scw_status st = plan_solve(prm, Zs, Y, X, p);
+    if (st != SCW_OK) return st;
+    if (M0) *M0 = p.M0;
+    if (M1) *M1 = p.M1;
+    if (!coef && !PQ) return SCW_OK;
+    if (!sample) return fail(SCW_ERR_ARG, "scw_layer_problem: null sample");
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SolveIn in{};
+    SolveWs ws{};
+    Carver sz;
+    carve_in(p, sz, in);
+    carve_ws(p, sz, ws);
+    char* blk = nullptr;
+    if (cudaMalloc(&blk, sz.off) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SCW_ERR_NOMEM, "scw_layer_problem: cudaMalloc");
+    }
+    std::unique_ptr<char, void (*)(char*)> guard(blk, [](char* q) { cudaFree(q); });
+    Carver c{blk, 0};
+    carve_in(p, c, in);
+    carve_ws(p, c, ws);
+    cudaStream_t s = ctx->stream;
+    if ((st = upload_inputs(p, sample, in, s)) != SCW_OK) return st;
+    const int MF = p.MF, n = p.n;
+    const long long nn = (long long)n * n, YX = (long long)Y * X;
+    n2_kernel<<<nblk(Zs * YX), 256, 0, s>>>(in.data, YX, Zs, ws.F);
+    SCW_CUDA_TRY(cudaGetLastError());
+    if ((st = scw::zgemm(s, X, p.M1, Y, kOne, ws.F, Y, YX, in.tw1, p.M1, 0, kZero, ws.T, p.M1, (long long)X * p.M1, 2 * Zs)) !=
+        SCW_OK)
+        return st;
+    if ((st = scw::zgemm(s, p.M0, p.M1, X, make_double2(1.0 / (double)YX, 0.0), in.tw2, X, 0, ws.T, p.M1, (long long)X * p.M1,
+                    kZero, ws.coef, p.M1, MF, 2 * Zs)) != SCW_OK)
+        return st;
+    if (PQ) {
+        build_pq_kernel<<<dim3(nblk(n), n, Zs), 256, 0, s>>>(ws.coef, in.up, in.wq, in.qs, in.ps, p.M0, p.M1, p.k, ws.P,
+                                                              ws.Q);
+        SCW_CUDA_TRY(cudaGetLastError());
+        if ((st = scw::zgemm(s, n, n, n, kOne, ws.P, n, nn, ws.Q, n, nn, kZero, (double2*)PQ, n, nn, Zs)) != SCW_OK) return st;
+    }
+    if (coef)
+        SCW_CUDA_TRY(cudaMemcpyAsync(coef, ws.coef, sizeof(double2) * (size_t)Zs * 2 * MF, cudaMemcpyDeviceToDevice, s));
+    SCW_CUDA_TRY(cudaStreamSynchronize(s));
+    ctx->launches += PQ ? 5 : 3;
+    return SCW_OK;
+}
+
 scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_slices, double* k) {
     if (!s) return fail(SCW_ERR_ARG, "null solution");
     if (M0) *M0 = s->M0;

@@ -291,13 +291,17 @@ SCW_API scw_status scw_mlp_gradients(scw_mlp m, const float* X, const float* T, 
 /* one Adam step (beta 0.9 / 0.999); loss before the step to *loss (may be NULL; synchronises if not) */
 SCW_API scw_status scw_mlp_train_step(scw_mlp m, const float* X, const float* T, int B, float lr, double* loss);
 /* Eigenpairs of a batch of n x n matrices (DEVICE, not modified) from one shift per eigenvalue
- * (DEVICE batch x n complex): Rayleigh-quotient iteration on the Hessenberg form, one warp per
- * eigenpair.  A matrix is accepted when every pair has ||A v - lambda v|| <= tol ||A||_F ||v||
- * and no two pairs share an eigenvector; otherwise the plain eigen-solver replaces it.
- * W: DEVICE batch x n, V: DEVICE batch x n x n (columns).  accepted_host: batch ints (may be
- * NULL); stats_host: [mean iterations, largest accepted residual, accepted, fallen back]. */
-SCW_API scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A, int batch, const void* shifts, int max_it,
-                                double tol, void* W, void* V, int* accepted_host, double* stats_host);
+ * (DEVICE batch x n complex) and optionally one proposed mode per eigenvalue (DEVICE batch x n
+ * ints: the start vector is that unit vector of A's basis; NULL or -1: pseudo-random):
+ * Rayleigh-quotient iteration on the Hessenberg form, one warp per eigenpair; tasks that land on
+ * another task's eigenvector restart with it projected out.  A matrix is accepted when every pair
+ * has ||A v - lambda v|| <= tol ||A||_F ||v|| and no two pairs share an eigenvector; otherwise
+ * the plain eigen-solver replaces it.  W: DEVICE batch x n, V: DEVICE batch x n x n (columns).
+ * accepted_host: batch ints (may be NULL); stats_host (5 doubles, may be NULL): mean iterations,
+ * largest accepted residual, accepted, fallen back, repaired tasks. */
+SCW_API scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A, int batch, const void* shifts,
+                                const int* start_index, int max_it, double tol, void* W, void* V,
+                                int* accepted_host, double* stats_host);
 
 #ifdef __cplusplus
 }

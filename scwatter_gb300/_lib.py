@@ -86,7 +86,7 @@ _SIGS = {
     "scw_mlp_forward": [P, P, I32, P],
     "scw_mlp_gradients": [P, P, P, I32, P, P],
     "scw_mlp_train_step": [P, P, P, I32, F32, P],
-    "scw_eig_warm": [P, I32, P, I32, P, I32, F64, P, P, P, P],
+    "scw_eig_warm": [P, I32, P, I32, P, P, I32, F64, P, P, P, P],
     "scw_sep_create": [P, I32, I32, I32, I32, P, P, P, PP],
     "scw_sep_destroy": [P],
     "scw_sep_set_exterior": [P, P, P, P, P, P, P],

@@ -13,7 +13,9 @@
 //   * every eigenpair has ||A v - lambda v|| <= tol ||A||_F ||v|| (checked against A itself), and
 //   * the mode count is intact: no two eigenpairs converged to the same eigenvector
 //     (eigenvalues within 1e-7 |lambda|_max of each other whose vectors overlap by > 0.5);
-// otherwise it falls back to the plain eigen-solver (zgeev), whose result replaces it.
+// A task that converged onto another task's eigenvector is restarted with that eigenvector (and
+// the ones it met before) projected out of its first iterates, for a few rounds; a matrix still
+// failing a gate falls back to the plain eigen-solver (zgeev), whose result replaces it.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -74,16 +76,35 @@ __global__ void fro_kernel(const double2* __restrict__ A, int n, double* __restr
 }
 
 constexpr int kFixed = 2;   // solves with the proposed shift before the Rayleigh quotient takes over
+constexpr int kMaxExcl = 8; // eigenvectors a repair task projects out
+constexpr int kRepairRounds = 8;
+
+// y <- y - sum_e v_e (v_e^H y) for the excluded unit eigenvectors (columns of Xold)
+__device__ void project_out(double2* y, const double2* Xb, const int* ex, int n, int lane) {
+    for (int e = 0; e < kMaxExcl; e++) {
+        const int c = ex[e];
+        if (c < 0) break;
+        double2 d = make_double2(0.0, 0.0);
+        for (int i = lane; i < n; i += 32) d = cadd(d, cmulc(Xb[(long long)i * n + c], y[i]));
+        d = warp_sum(d);
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) y[i] = csub(y[i], cmul(Xb[(long long)i * n + c], d));
+        __syncwarp();
+    }
+}
 
 // Rayleigh-quotient iteration, one warp per task t = task0 + warp (matrix t / n, eigenvalue t % n).
 __global__ void __launch_bounds__(128)
 rqi_kernel(const double2* __restrict__ H, int n, const double2* __restrict__ shifts, const double* __restrict__ hnorm,
            double2* __restrict__ ws, long long ws_stride, long long task0, long long ntasks, int max_it,
-           double2* __restrict__ lam_out, double2* __restrict__ X, int* __restrict__ iters) {
+           double2* __restrict__ lam_out, double2* __restrict__ X, int* __restrict__ iters,
+           const long long* __restrict__ task_ids, const int* __restrict__ excl, const double2* __restrict__ Xold,
+           const double2* __restrict__ Qm, const int* __restrict__ start_idx) {
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= ntasks) return;
-    const long long t = task0 + w;
+    const long long t = task_ids ? task_ids[task0 + w] : task0 + w;
+    const int* ex = excl ? excl + (task0 + w) * kMaxExcl : nullptr;
     const long long b = t / n;
     const int j = (int)(t % n);
     const double2* Hb = H + b * (long long)n * n;
@@ -92,8 +113,18 @@ rqi_kernel(const double2* __restrict__ H, int n, const double2* __restrict__ shi
     double2* y = x + n;
     const double hn = fmax(hnorm[b], 1e-300);
     const double tiny = 2.220446049250313e-16 * hn;
-    // start vector: a deterministic pseudo-random unit vector per task
+    // start vector: Q^H e_s for a proposed mode s (row s of Q, conjugated: a unit vector), or a
+    // deterministic pseudo-random unit vector per task
+    const int s0 = start_idx ? start_idx[t] : -1;
     double ss = 0;
+    if (s0 >= 0 && s0 < n) {
+        const double2* qrow = Qm + b * (long long)n * n + (long long)s0 * n;
+        for (int i = lane; i < n; i += 32) {
+            const double2 q = qrow[i];
+            x[i] = make_double2(q.x, -q.y);
+            ss += q.x * q.x + q.y * q.y;
+        }
+    } else
     for (int i = lane; i < n; i += 32) {
         unsigned h = (unsigned)(i * 2654435761u) ^ (unsigned)(j * 2246822519u) ^ 0x9e3779b9u;
         h ^= h >> 15;
@@ -107,8 +138,10 @@ rqi_kernel(const double2* __restrict__ H, int n, const double2* __restrict__ shi
     const double inv0 = 1.0 / sqrt(ss);
     for (int i = lane; i < n; i += 32) x[i] = make_double2(x[i].x * inv0, x[i].y * inv0);
     __syncwarp();
+    if (ex) project_out(x, Xold + b * (long long)n * n, ex, n, lane);
     double2 sigma = shifts[t];
     double2 lam_fin = sigma;
+    const int nfix = s0 >= 0 ? 1 : kFixed;
     double best = 1e300;
     int it = 0;
     for (; it < max_it; it++) {
@@ -164,6 +197,7 @@ rqi_kernel(const double2* __restrict__ H, int n, const double2* __restrict__ shi
             }
             __syncwarp();
         }
+        if (ex && it < nfix) project_out(y, Xold + b * (long long)n * n, ex, n, lane);
         // ---- normalise, Rayleigh quotient and residual ----
         double nn2 = 0;
         for (int i = lane; i < n; i += 32) nn2 += y[i].x * y[i].x + y[i].y * y[i].y;
@@ -195,13 +229,14 @@ rqi_kernel(const double2* __restrict__ H, int n, const double2* __restrict__ shi
             it++;
             break;
         }
-        if (it >= kFixed + 1 && r > 0.9 * best) {   // stagnation at rounding level
+        if (it >= nfix + 1 && r <= 1e-10 * hn && r > 0.5 * best) {   // stagnation at rounding level
             it++;
             break;
         }
-        // the first kFixed solves keep the proposed shift (inverse iteration locks onto the
-        // eigenvector nearest to it); then the Rayleigh quotient becomes the shift
-        if (it + 1 >= kFixed) sigma = rq;
+        // the first solves keep the proposed shift (inverse iteration locks onto the eigenvector
+        // nearest to it; one solve when the start vector is a proposed mode, kFixed otherwise);
+        // then the Rayleigh quotient becomes the shift
+        if (it + 1 >= nfix) sigma = rq;
         best = fmin(best, r);
     }
     for (int i = lane; i < n; i += 32) X[b * (long long)n * n + (long long)i * n + j] = x[i];
@@ -234,9 +269,10 @@ __global__ void resid_kernel(const double2* __restrict__ AV, const double2* __re
     atomicMax(worst + b, (unsigned long long)__double_as_longlong(val));
 }
 
-// mode count: pairs (i < k) of nearly equal eigenvalues whose eigenvectors overlap
+// mode count: pairs (i < k) of nearly equal eigenvalues whose eigenvectors overlap; dup_of[k]
+// receives the smallest such i
 __global__ void dup_kernel(const double2* __restrict__ lam, const double2* __restrict__ V, int n, double rel,
-                           int* __restrict__ dup) {
+                           int* __restrict__ dup, int* __restrict__ dup_of) {
     const long long b = blockIdx.y;
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= (long long)n * n) return;
@@ -256,7 +292,10 @@ __global__ void dup_kernel(const double2* __restrict__ lam, const double2* __res
         ni += a.x * a.x + a.y * a.y;
         nk += c.x * c.x + c.y * c.y;
     }
-    if (sqrt(o.x * o.x + o.y * o.y) > 0.5 * sqrt(ni * nk)) atomicExch(dup + b, 1);
+    if (sqrt(o.x * o.x + o.y * o.y) > 0.5 * sqrt(ni * nk)) {
+        atomicExch(dup + b, 1);
+        atomicMin(dup_of + b * n + k, i);
+    }
 }
 
 static unsigned blocks(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -268,13 +307,15 @@ using scw::fail;
 
 extern "C" {
 
-// A: device, batch x n x n complex128 (not modified); shifts: device, batch x n complex128.
+// A: device, batch x n x n complex128 (not modified); shifts: device, batch x n complex128;
+// start_idx: device, batch x n ints (a proposed mode per eigenpair: the start vector is that
+// unit vector of A's basis; -1 or NULL: pseudo-random start).
 // W (batch x n) and V (batch x n x n, column k = eigenvector k): device outputs.
 // accepted_host[b] = 1 when matrix b passed the gates (0: it was solved by the plain eigen-solver).
 // stats_host (may be NULL): [0] mean Rayleigh iterations per eigenpair, [1] largest accepted
-// relative residual, [2] matrices accepted, [3] matrices that fell back.
-scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A_, int batch, const void* shifts_, int max_it, double tol,
-                        void* W_, void* V_, int* accepted_host, double* stats_host) {
+// relative residual, [2] matrices accepted, [3] matrices that fell back, [4] repaired tasks.
+scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A_, int batch, const void* shifts_, const int* start_idx,
+                        int max_it, double tol, void* W_, void* V_, int* accepted_host, double* stats_host) {
     using namespace scw::wm;
     if (!ctx || n < 1 || !A_ || batch < 1 || !shifts_ || !W_ || !V_ || max_it < 1 || !(tol > 0))
         return fail(SCW_ERR_ARG, "scw_eig_warm: bad arguments");
@@ -287,8 +328,9 @@ scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A_, int batch, const voi
     const long long nn = (long long)n * n;
     // workspace: H, Q, X, AV (batch nn each), hessenberg work (batch 3n), norms, flags
     scw::DevBuf buf;
-    const size_t base = sizeof(double2) * (size_t)(4 * nn * batch + 3LL * n * batch) + sizeof(double) * 2 * batch +
-                        sizeof(unsigned long long) * batch + sizeof(int) * (batch + (size_t)n * batch) + 4096;
+    const size_t base = sizeof(double2) * (size_t)(5 * nn * batch + 3LL * n * batch) + sizeof(double) * 2 * batch +
+                        sizeof(unsigned long long) * batch + sizeof(int) * (batch + 2 * (size_t)n * batch) +
+                        (sizeof(long long) + sizeof(int) * kMaxExcl) * (size_t)n * batch + 8192;
     scw_status s = buf.reserve(base);
     if (s != SCW_OK) return s;
     char* p = (char*)buf.ptr;
@@ -307,6 +349,10 @@ scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A_, int batch, const voi
     unsigned long long* worst = (unsigned long long*)take(sizeof(unsigned long long) * batch);
     int* dup = (int*)take(sizeof(int) * batch);
     int* iters = (int*)take(sizeof(int) * (size_t)n * batch);
+    double2* Xold = (double2*)take(sizeof(double2) * nn * batch);
+    int* dup_of = (int*)take(sizeof(int) * (size_t)n * batch);
+    long long* rep_ids = (long long*)take(sizeof(long long) * (size_t)n * batch);
+    int* rep_excl = (int*)take(sizeof(int) * kMaxExcl * (size_t)n * batch);
     // Hessenberg form and its norm
     SCW_CUDA_TRY(cudaMemcpyAsync(Hm, A, sizeof(double2) * nn * batch, cudaMemcpyDeviceToDevice, st));
     s = scw::zgehrd(st, Hm, Qm, n, batch, hw);
@@ -325,28 +371,65 @@ scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A_, int batch, const voi
     scw::DevBuf tw;
     if ((s = tw.reserve(sizeof(double2) * (size_t)ws_stride * chunk)) != SCW_OK) return s;
     long long launches = 4;
-    for (long long t0 = 0; t0 < total; t0 += chunk) {
-        const long long cnt = std::min(chunk, total - t0);
-        rqi_kernel<<<blocks(cnt * 32, 128), 128, 0, st>>>(Hm, n, shifts, hnorm, (double2*)tw.ptr, ws_stride, t0, cnt,
-                                                          max_it, W, Xm, iters);
-        SCW_CUDA_TRY(cudaGetLastError());
-        launches++;
-    }
-    // back-transform V = Q X, residual against A, mode-count check
-    s = scw::zgemm(st, n, n, n, make_double2(1, 0), Qm, n, nn, Xm, n, nn, make_double2(0, 0), V, n, nn, batch);
-    if (s != SCW_OK) return s;
-    s = scw::zgemm(st, n, n, n, make_double2(1, 0), A, n, nn, V, n, nn, make_double2(0, 0), AV, n, nn, batch);
-    if (s != SCW_OK) return s;
-    SCW_CUDA_TRY(cudaMemsetAsync(worst, 0, sizeof(unsigned long long) * batch, st));
-    SCW_CUDA_TRY(cudaMemsetAsync(dup, 0, sizeof(int) * batch, st));
-    resid_kernel<<<dim3(blocks(n), batch), 256, 0, st>>>(AV, V, W, anorm, n, worst);
-    dup_kernel<<<dim3(blocks(nn), batch), 256, 0, st>>>(W, V, n, 1e-7, dup);
-    SCW_CUDA_TRY(cudaGetLastError());
-    launches += 4;
+    auto run_tasks = [&](long long count, const long long* ids, const int* excl) -> scw_status {
+        for (long long t0 = 0; t0 < count; t0 += chunk) {
+            const long long cnt = std::min(chunk, count - t0);
+            rqi_kernel<<<blocks(cnt * 32, 128), 128, 0, st>>>(Hm, n, shifts, hnorm, (double2*)tw.ptr, ws_stride, t0, cnt,
+                                                              max_it, W, Xm, iters, ids, excl, Xold, Qm, start_idx);
+            SCW_CUDA_TRY(cudaGetLastError());
+            launches++;
+        }
+        return SCW_OK;
+    };
+    if ((s = run_tasks(total, nullptr, nullptr)) != SCW_OK) return s;
     std::vector<unsigned long long> hw_worst(batch);
-    std::vector<int> hdup(batch), hit((size_t)n * batch);
-    SCW_CUDA_TRY(cudaMemcpyAsync(hw_worst.data(), worst, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st));
-    SCW_CUDA_TRY(cudaMemcpyAsync(hdup.data(), dup, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
+    std::vector<int> hdup(batch), hdup_of((size_t)n * batch), hit((size_t)n * batch);
+    std::vector<long long> rep_tasks;
+    std::vector<int> rep_ex;
+    std::vector<std::vector<int>> chain((size_t)n * batch);   // eigenvectors each task has to avoid
+    int repairs = 0;
+    for (int round = 0;; round++) {
+        // back-transform V = Q X, residual against A, mode-count check
+        s = scw::zgemm(st, n, n, n, make_double2(1, 0), Qm, n, nn, Xm, n, nn, make_double2(0, 0), V, n, nn, batch);
+        if (s != SCW_OK) return s;
+        s = scw::zgemm(st, n, n, n, make_double2(1, 0), A, n, nn, V, n, nn, make_double2(0, 0), AV, n, nn, batch);
+        if (s != SCW_OK) return s;
+        SCW_CUDA_TRY(cudaMemsetAsync(worst, 0, sizeof(unsigned long long) * batch, st));
+        SCW_CUDA_TRY(cudaMemsetAsync(dup, 0, sizeof(int) * batch, st));
+        SCW_CUDA_TRY(cudaMemsetAsync(dup_of, 0x7f, sizeof(int) * (size_t)n * batch, st));
+        resid_kernel<<<dim3(blocks(n), batch), 256, 0, st>>>(AV, V, W, anorm, n, worst);
+        dup_kernel<<<dim3(blocks(nn), batch), 256, 0, st>>>(W, V, n, 1e-7, dup, dup_of);
+        SCW_CUDA_TRY(cudaGetLastError());
+        launches += 4;
+        SCW_CUDA_TRY(cudaMemcpyAsync(hw_worst.data(), worst, sizeof(unsigned long long) * batch, cudaMemcpyDeviceToHost, st));
+        SCW_CUDA_TRY(cudaMemcpyAsync(hdup.data(), dup, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
+        SCW_CUDA_TRY(cudaMemcpyAsync(hdup_of.data(), dup_of, sizeof(int) * hdup_of.size(), cudaMemcpyDeviceToHost, st));
+        SCW_CUDA_TRY(cudaStreamSynchronize(st));
+        if (round == kRepairRounds) break;
+        // repair: a task that converged onto the eigenvector of a lower-numbered task restarts with
+        // that eigenvector (and the ones it met before) projected out of its first iterates
+        rep_tasks.clear();
+        rep_ex.clear();
+        for (int b = 0; b < batch; b++) {
+            if (!hdup[b]) continue;
+            for (int k = 0; k < n; k++) {
+                const int i = hdup_of[(size_t)b * n + k];
+                if (i < 0 || i >= n) continue;
+                auto& ch = chain[(size_t)b * n + k];
+                if ((int)ch.size() >= kMaxExcl) continue;
+                if (std::find(ch.begin(), ch.end(), i) == ch.end()) ch.push_back(i);
+                rep_tasks.push_back((long long)b * n + k);
+                for (int e = 0; e < kMaxExcl; e++) rep_ex.push_back(e < (int)ch.size() ? ch[e] : -1);
+            }
+        }
+        if (rep_tasks.empty()) break;
+        repairs += (int)rep_tasks.size();
+        SCW_CUDA_TRY(cudaMemcpyAsync(Xold, Xm, sizeof(double2) * nn * batch, cudaMemcpyDeviceToDevice, st));
+        SCW_CUDA_TRY(cudaMemcpyAsync(rep_ids, rep_tasks.data(), sizeof(long long) * rep_tasks.size(),
+                                     cudaMemcpyHostToDevice, st));
+        SCW_CUDA_TRY(cudaMemcpyAsync(rep_excl, rep_ex.data(), sizeof(int) * rep_ex.size(), cudaMemcpyHostToDevice, st));
+        if ((s = run_tasks((long long)rep_tasks.size(), rep_ids, rep_excl)) != SCW_OK) return s;
+    }
     SCW_CUDA_TRY(cudaMemcpyAsync(hit.data(), iters, sizeof(int) * hit.size(), cudaMemcpyDeviceToHost, st));
     SCW_CUDA_TRY(cudaStreamSynchronize(st));
     std::vector<int> reject;
@@ -395,6 +478,7 @@ scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A_, int batch, const voi
         stats_host[1] = max_acc;
         stats_host[2] = (double)(batch - (int)reject.size());
         stats_host[3] = (double)reject.size();
+        stats_host[4] = (double)repairs;
     }
     return SCW_OK;
 }

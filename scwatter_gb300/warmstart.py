@@ -2,10 +2,11 @@
 
 A small network (3 fully connected layers, ReLU, FP32; its own CUDA forward, backward and
 Adam kernels in csrc/mlp.cu) maps a layer's Fourier coefficients (the crops of n^2 and
-n^-2) to that layer's eigenvalues lambda = gamma^2 of the reduced matrix PQ, sorted by
-descending real part.  It predicts the correction to the homogeneous-medium spectrum
-lambda0 = <n^2> - (up^2 + wq^2) / k^2 (every harmonic twice, one per polarisation), the guess
-used without it.  The predicted eigenvalues are the shifts of the warm eigen-solver
+n^-2) to that layer's eigenvalues lambda = gamma^2 of the reduced matrix PQ,
+sorted by descending real part.  It predicts the correction to the homogeneous-medium spectrum
+lambda0 = <n^2> - (up^2 + wq^2) / k^2 (every harmonic twice, one per polarisation) sorted the same
+way, the guess used without it.  The predicted eigenvalues are the shifts of the warm eigen-solver, each task
+starting from the plane-wave mode of its slot in the sorted homogeneous spectrum
 (scw_eig_warm: Rayleigh-quotient iteration per eigenpair on the Hessenberg form, accepted only
 when every residual ||A v - lambda v|| and the mode count pass; otherwise the layer is
 solved by the plain eigen-solver).
@@ -34,13 +35,15 @@ def _p(t):
 @dataclass
 class LayerProblems:
     """Per-slice Fourier crops (host, [Z, 2, MF] complex: n^2 then n^-2) and the reduced
-    matrices PQ (device, torch [Z, n, n] complex128) of one sample, with the baseline spectrum."""
+    matrices PQ (device, torch [Z, n, n] complex128) of one sample, with the homogeneous-medium
+    spectrum (host [Z, n], sorted by descending real part) and the plane-wave mode of each of its
+    entries (host [Z, n] ints: row of PQ, Ex rows then Ey rows)."""
     coef: np.ndarray
     PQ: object
     M0: int
     M1: int
-    baseline: np.ndarray     # [Z, n] complex, sorted by descending real part
-
+    baseline: np.ndarray
+    modes: np.ndarray
 
 def layer_problems(ctx: Context, sample, lam=1.0, direction=(0.0, 0.0, 1.0), ex=(1.0, 0.0), ey=(0.0, 0.0),
                    ez=(0.0, 0.0), n=(1.0, 1.0), kappa=0.0, size=(10.0, 10.0, 2.0), z=0.0, coef=None) -> LayerProblems:
@@ -69,8 +72,9 @@ def layer_problems(ctx: Context, sample, lam=1.0, direction=(0.0, 0.0, 1.0), ex=
     kt2 = (np.add.outer(wq ** 2, up ** 2).ravel() / k ** 2)          # harmonic m = q M0 + p
     n2 = np.mean(vol.astype(np.complex128) ** 2, axis=(1, 2))
     base = n2[:, None] - np.concatenate([kt2, kt2])[None, :]
-    base = -np.sort_complex(-base)                                    # descending real part
-    return LayerProblems(coef=dcoef.cpu().numpy(), PQ=dPQ, M0=M0.value, M1=M1.value, baseline=base)
+    order = np.stack([np.lexsort((-b.imag, -b.real)) for b in base]).astype(np.int32)
+    base = np.take_along_axis(base, order, axis=1)                   # descending real part
+    return LayerProblems(coef=dcoef.cpu().numpy(), PQ=dPQ, M0=M0.value, M1=M1.value, baseline=base, modes=order)
 
 
 def plain_eig(ctx: Context, PQ):
@@ -85,20 +89,23 @@ def plain_eig(ctx: Context, PQ):
     return W, V
 
 
-def warm_eig(ctx: Context, PQ, shifts, max_it=10, tol=1e-11):
-    """scw_eig_warm on the device batch PQ with device shifts [Z, n] complex128."""
+def warm_eig(ctx: Context, PQ, shifts, modes=None, max_it=12, tol=1e-11):
+    """scw_eig_warm on the device batch PQ with device shifts [Z, n] complex128 and optional
+    proposed modes [Z, n] (host ints: the start vector of each eigenpair)."""
     import torch
     Z, n, _ = PQ.shape
     W = torch.zeros((Z, n), dtype=torch.complex128, device="cuda")
     V = torch.zeros((Z, n, n), dtype=torch.complex128, device="cuda")
     acc = np.zeros(Z, np.int32)
-    stats = np.zeros(4, np.float64)
+    stats = np.zeros(5, np.float64)
     sh = shifts.contiguous()
+    md = torch.from_numpy(np.ascontiguousarray(modes, dtype=np.int32)).cuda() if modes is not None else None
     torch.cuda.synchronize()
-    _lib.call("scw_eig_warm", ctx.handle, n, _p(PQ), Z, _p(sh), int(max_it), float(tol), _p(W), _p(V),
+    _lib.call("scw_eig_warm", ctx.handle, n, _p(PQ), Z, _p(sh), _p(md) if md is not None else None, int(max_it),
+              float(tol), _p(W), _p(V),
               ctypes.c_void_p(acc.ctypes.data), ctypes.c_void_p(stats.ctypes.data))
     return W, V, acc, {"mean_iterations": stats[0], "max_residual": stats[1], "accepted": int(stats[2]),
-                       "fell_back": int(stats[3])}
+                       "fell_back": int(stats[3]), "repaired": int(stats[4])}
 
 
 def sorted_desc(lam):
@@ -211,7 +218,7 @@ class WarmStart:
         return hist
 
     def predict(self, coef, baseline):
-        """Predicted eigenvalues [L, 2MF] complex (host)."""
+        """Predicted eigenvalues [L, 2MF] complex (host), in the baseline's sorted slots."""
         import torch
         Xh = (features(coef) - self.fx[0]) / self.fx[1]
         Y = self.net.forward(torch.from_numpy(Xh.astype(np.float32)).cuda()).cpu().numpy()

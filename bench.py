@@ -382,10 +382,144 @@ def run_ours(args):
         if line is not None:
             line["e2e"] = {"value": units / float(np.mean(e2e_t)), "unit": UNIT, "h2d_bytes_per_step": int(q_bytes),
                            "d2h_bytes_per_step": int(out_bytes), "ms_per_step": float(np.mean(e2e_t)) * 1e3}
+    if line is not None and not args.no_solve:
+        line["solve"] = solve_leg(ctx)
     if line is not None:
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+CFG1 = dict(name="spheres[20,64,64] coef20x20, 20 slices (the CPU-runnable sphere workload)", shape=(20, 64, 64),
+            coef=(20, 20), size=(64.0, 64.0, 20.0))
+CPU_SOLVE_SLICES = 2       # slices of the config-1 sample the CPU oracle solve is timed on
+
+
+def solve_leg(ctx):
+    """GPU FP64 solve of the 20-slice sphere sample (samples/s) beside the CPU oracle solve of
+    a 2-slice cut of it (the reference's algorithm: 4MF zgeev per slice, explicit inverses),
+    and the agreement of the two on that cut."""
+    from oracle import solve_oracle as so
+    from scwatter_gb300 import samples, solver
+    c = CFG1
+    vol = samples.spheres(c["shape"], n_spheres=6, radius=(4.0, 12.0), n_sphere=1.4 + 0.01j, seed=0)
+    kw = dict(lam=1.0, direction=(0.0, 0.0, 1.0), ex=(1.0, 0.0), ey=(0.0, 0.0))
+    solver.solve(vol[:1], size=(c["size"][0], c["size"][1], 1.0), coef=c["coef"], ctx=ctx, **kw)   # warm-up
+    launches0 = ctx.launches
+    t0 = time.perf_counter()
+    g = solver.solve(vol, size=c["size"], coef=c["coef"], ctx=ctx, **kw)
+    t_gpu = time.perf_counter() - t0
+    launches = ctx.launches - launches0
+    del g
+    cut = vol[:CPU_SOLVE_SLICES]
+    size_cut = (c["size"][0], c["size"][1], c["size"][2] * CPU_SOLVE_SLICES / c["shape"][0])
+    gc = solver.solve(cut, size=size_cut, coef=c["coef"], ctx=ctx, **kw)
+    prm = so.SolveParams(size=size_cut, coef=c["coef"], **kw)
+    t0 = time.perf_counter()
+    r = so.solve(cut, prm)
+    t_cpu = time.perf_counter() - t0
+    err = float(np.linalg.norm(gc.x - r.x) / np.linalg.norm(r.x))
+    cpu_per_slice = t_cpu / CPU_SOLVE_SLICES
+    return {"workload": c["name"], "gpu_s": t_gpu, "samples_per_s": 1.0 / t_gpu, "gpu_launches": int(launches),
+            "dtype": "c128",
+            "cpu_baseline": {"s_per_slice": cpu_per_slice,
+                             "samples_per_s_extrapolated": 1.0 / (cpu_per_slice * c["shape"][0]),
+                             "kind": "port", "cores": os.cpu_count(),
+                             "sample": f"first {CPU_SOLVE_SLICES} of the 20 slices, scipy LAPACK (OpenBLAS threads)"},
+            "parity": {"x_rel_err_vs_oracle": err, "on": f"the {CPU_SOLVE_SLICES}-slice cut"}}
+
+
+def batch_leg(args):
+    """Uneven batch (256 seeded sphere samples: harmonics 8-32 per axis, 4-64 layers, grids
+    64^2 x 32 to 256^2 x 128, wavelengths 0.5-1.5, incidence 0-30 degrees), solved and evaluated
+    by one CUDA-graph launch; the first ``--batch N`` samples of the seeded list."""
+    import torch
+    from scwatter_gb300 import evaluator as ev
+    from scwatter_gb300.batch import Batch, uneven_items
+    items = uneven_items(256, seed=0)[:args.batch]
+    ctx = ev.Context(0)
+    t0 = time.perf_counter()
+    b = Batch(ctx, items, lanes=args.batch_lanes, method=args.batch_method)
+    t_create = time.perf_counter() - t0
+    info = b.info()
+    b.run()
+    b.wait()
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        b.run()
+        st = b.wait()
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    pm = sum(b.item_info(i)[3] for i in range(len(items)))
+    shapes = [b.item_info(i)[:3] for i in range(len(items))]
+    print(json.dumps({"metric": "samples/s", "value": len(items) / t, "unit": "samples/s", "n_gpus": 1,
+                      "steps": len(times), "warmup": 1, "ms_per_step": t * 1e3, "higher_is_better": True,
+                      "dtype": "c128 solve, c64 field", "data": "synthetic",
+                      "config": {"workload": f"uneven sphere batch, first {len(items)} of 256 seeded samples",
+                                 "harmonics_layers": shapes},
+                      "points_modes_per_s": pm / t, "graph": info, "create_s": t_create,
+                      "item_status": st.tolist()}))
+
+
+def warm_leg(args):
+    """Learned warm start on GRF layers (coef 24 x 24 -> 1152 x 1152 reduced matrices, 32
+    layers per sample): network trained on the plain solver's eigenvalues of ``--warm-train``
+    samples, then eigen-solve of ``--warm`` held-out samples with and without it."""
+    import torch
+    from scwatter_gb300 import evaluator as ev
+    from scwatter_gb300 import samples
+    from scwatter_gb300.warmstart import WarmStart, layer_problems, plain_eig, sorted_desc, warm_eig
+    ctx = ev.Context(0)
+    M, Z = args.warm_coef, 32
+    def problems(seed0, count):
+        out = []
+        for s in range(count):
+            vol = samples.gaussian_random_field((Z, 64, 64), corr_px=8.0, n_range=(1.0, 1.6), kappa_max=0.02,
+                                                seed=seed0 + s)
+            out.append(layer_problems(ctx, vol, lam=1.0, direction=(0.2, 0.1, 1.0), size=(64.0, 64.0, float(Z)),
+                                      coef=(M, M)))
+        return out
+    train = problems(1000, args.warm_train)
+    test = problems(5000, args.warm)
+    t0 = time.perf_counter()
+    eigs = [sorted_desc(plain_eig(ctx, lp.PQ)[0].cpu().numpy()) for lp in train]
+    t_train_data = time.perf_counter() - t0
+    MF = M * M
+    ws = WarmStart(ctx, MF, width=512, seed=0)
+    t0 = time.perf_counter()
+    hist = ws.fit(np.concatenate([lp.coef for lp in train]), np.concatenate(eigs),
+                  np.concatenate([lp.baseline for lp in train]), epochs=args.warm_epochs, lr=1e-3, batch=64)
+    t_fit = time.perf_counter() - t0
+    PQ = torch.cat([lp.PQ for lp in test])
+    base = np.concatenate([lp.baseline for lp in test])
+    modes = np.concatenate([lp.modes for lp in test])
+    coef = np.concatenate([lp.coef for lp in test])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    W0, V0 = plain_eig(ctx, PQ)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    truth = sorted_desc(W0.cpu().numpy())
+    t0 = time.perf_counter()
+    pred = ws.predict(coef, base)
+    _, _, acc, st = warm_eig(ctx, PQ, torch.from_numpy(pred).cuda(), modes)
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    _, _, acc_b, st_b = warm_eig(ctx, PQ, torch.from_numpy(base).cuda(), modes)
+    layers = PQ.shape[0]
+    print(json.dumps({"metric": "layer eigen-solves/s", "value": layers / t_warm, "unit": "layers/s",
+                      "n_gpus": 1, "higher_is_better": True, "dtype": "c128", "data": "synthetic",
+                      "config": {"workload": f"GRF layers, coef {M}x{M} (reduced {2 * MF}x{2 * MF}), {Z} layers "
+                                             f"per sample, {args.warm} held-out samples, {args.warm_train} training"},
+                      "plain": {"layers_per_s": layers / t_plain, "s": t_plain},
+                      "warm": {"layers_per_s": layers / t_warm, "s": t_warm, "accepted": int(acc.sum()),
+                               "stats": st},
+                      "without_network": {"accepted": int(acc_b.sum()), "stats": st_b},
+                      "shift_error": {"network": float(np.abs(pred - truth).mean()),
+                                      "homogeneous": float(np.abs(base - truth).mean())},
+                      "training": {"loss_first": hist[0], "loss_last": hist[-1], "fit_s": t_fit,
+                                   "plain_solves_for_data_s": t_train_data}}))
 
 
 def main():
@@ -397,9 +531,25 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--small", action="store_true", help="8-slice profiling case (2 GB of coefficients)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--no-solve", action="store_true", help="skip the FP64 solve leg")
+    ap.add_argument("--solve-only", action="store_true", help="only the FP64 solve leg (its own JSON line)")
+    ap.add_argument("--batch", type=int, default=0, help="batched-graph measurement on the first N uneven samples")
+    ap.add_argument("--batch-lanes", type=int, default=0)
+    ap.add_argument("--batch-method", type=int, default=0)
+    ap.add_argument("--warm", type=int, default=0, help="warm-start measurement on N held-out GRF samples")
+    ap.add_argument("--warm-train", type=int, default=16)
+    ap.add_argument("--warm-coef", type=int, default=24)
+    ap.add_argument("--warm-epochs", type=int, default=200)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.solve_only:
+        from scwatter_gb300 import evaluator as ev
+        print(json.dumps({"metric": "samples/s", "impl": "ours", **solve_leg(ev.Context(0))}))
+    elif args.batch:
+        batch_leg(args)
+    elif args.warm:
+        warm_leg(args)
     else:
         run_ours(args)
 

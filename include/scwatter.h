@@ -303,6 +303,18 @@ SCW_API scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A, int batch, co
                                 const int* start_index, int max_it, double tol, void* W, void* V,
                                 int* accepted_host, double* stats_host);
 
+/* ---------------------------------------------------------------------------------- */
+/* Viewer display processing on DEVICE buffers -- replaces EvaluateScalarSlices,       */
+/* CalculateMinMax and EvaluateColorValue / EvaluateColorSlices (sCWatterView.cpp:200-352) */
+/* ---------------------------------------------------------------------------------- */
+/* S[i] (complex64) = E[i][mode] for mode 0/1/2 (x, y, z), or |Ex|^2 + |Ey|^2 + |Ez|^2 for 3. */
+SCW_API scw_status scw_view_scalar(scw_ctx ctx, const float* E, int64_t n, int mode, float* S);
+/* out4 = real min, real max, imaginary min, imaginary max over the n complex64 values (synchronises). */
+SCW_API scw_status scw_view_minmax(scw_ctx ctx, const float* S, int64_t n, float* out4);
+/* rgb (n x 3 bytes): params = real_low, real_high, imag_low, imag_high, real_color[3],
+ * imag_color[3], show_real, show_imag (12 floats, HOST). */
+SCW_API scw_status scw_view_color(scw_ctx ctx, const float* S, int64_t n, const float* params, unsigned char* rgb);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,9 @@ _SIGS = {
     "scw_mlp_gradients": [P, P, P, I32, P, P],
     "scw_mlp_train_step": [P, P, P, I32, F32, P],
     "scw_eig_warm": [P, I32, P, I32, P, P, I32, F64, P, P, P, P],
+    "scw_view_scalar": [P, P, I64, I32, P],
+    "scw_view_minmax": [P, P, I64, P],
+    "scw_view_color": [P, P, I64, P, P],
     "scw_sep_create": [P, I32, I32, I32, I32, P, P, P, PP],
     "scw_sep_destroy": [P],
     "scw_sep_set_exterior": [P, P, P, P, P, P, P],

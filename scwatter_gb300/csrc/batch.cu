@@ -13,7 +13,8 @@
 //    capture, so the whole batch is one graph; scw_batch_run is one cudaGraphLaunch;
 //  * results (x, gamma, status words, field volumes) live in arenas indexed per item.
 // The autotuner picks the lane count (bounded by free memory) and the output-GEMM form
-// (3xTF32 or split-BF16 tcgen05, or FP32 SIMT) by timing graphs of a stratified subset.
+// (3xTF32 or split-BF16 tcgen05, or FP32 SIMT) by timing graphs of a stratified subset of the
+// cheaper half of the items.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -369,11 +370,14 @@ scw_status scw_batch_create(scw_ctx ctx, const scw_batch_item* items, int count,
     const int max_lanes = (int)std::max<size_t>(1, std::min<size_t>(16, (size_t)(0.8 * free_b) / std::max<size_t>(max_ws, 1)));
     const auto t0 = std::chrono::steady_clock::now();
     if (lanes == 0 || method == 0) {
+        // calibration subset: 8 items spread over the cheaper half by cost, so tuning costs a
+        // bounded fraction of one batch run
         std::vector<int> by_cost(all);
         std::sort(by_cost.begin(), by_cost.end(), [&](int x, int y) { return b->items[x].cost < b->items[y].cost; });
         std::vector<int> sub;
-        const int want = std::min(count, 8);
-        for (int j = 0; j < want; j++) sub.push_back(by_cost[(size_t)j * count / want]);
+        const int pool = std::max(1, (count + 1) / 2);
+        const int want = std::min(pool, 8);
+        for (int j = 0; j < want; j++) sub.push_back(by_cost[(size_t)j * pool / want]);
         int best_l = lanes ? lanes : 1, best_m = method ? method : SCW_SEP_TF32X3;
         double best = 1e300;
         if (lanes == 0) {

@@ -67,14 +67,33 @@ __global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float*
 constexpr int kCtrWarps = 8;
 constexpr int kCtrChunk = 1024;
 
+// pipeline depth of the Q stream: stages x rows per warp = 16 float4 in flight per lane
+template <int RW, int NK>
+struct CtrCfg {
+    static constexpr int kStages = NK == 8 ? 4 : (16 / RW < 2 ? 2 : 16 / RW);
+    static constexpr size_t kSmem = (size_t)NK * (kCtrChunk / 2) * 16 + (size_t)kCtrWarps * kStages * RW * 32 * 16;
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 template <int NK, int RW>
 __global__ void __launch_bounds__(kCtrWarps * 32, 2)
 sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict__ Phi,
                     const float2* __restrict__ Q, int MF, int J, float2* __restrict__ C) {
-    __shared__ float4 ph[NK][kCtrChunk / 2];    // (phi[j][kk], phi[j+1][kk]) pairs; lanes read consecutive pairs
+    constexpr int S = CtrCfg<RW, NK>::kStages;
+    extern __shared__ float4 smem4[];
+    // (phi[j][kk], phi[j+1][kk]) pairs per plane; then per lane S x RW private Q slots
+    float4 (*ph)[kCtrChunk / 2] = reinterpret_cast<float4 (*)[kCtrChunk / 2]>(smem4);
     const PGroup g = groups[blockIdx.y];
     const int l = g.region - 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* qs = smem4 + NK * (kCtrChunk / 2) + (size_t)warp * S * RW * 32 + lane;   // slot (s, r): qs[(s*RW + r)*32]
     const int row0 = (blockIdx.x * kCtrWarps + warp) * RW;
     float acc[RW][NK][2];
 #pragma unroll
@@ -93,33 +112,53 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
         for (int j0 = 0; j0 < J; j0 += kCtrChunk) {
             const int nj = min(kCtrChunk, J - j0);
             __syncthreads();
+            // consecutive threads fill consecutive pairs of one plane (conflict-free stores)
             for (int e = threadIdx.x; e < (nj / 2) * NK; e += blockDim.x) {
-                const int jp = e / NK, kk = e % NK;
+                const int kk = e / (nj / 2), jp = e % (nj / 2);
                 const float2 a = Pg[((long long)half * J + j0 + 2 * jp) * NK + kk];
                 const float2 b = Pg[((long long)half * J + j0 + 2 * jp + 1) * NK + kk];
                 ph[kk][jp] = make_float4(a.x, a.y, b.x, b.y);
             }
             __syncthreads();
-            // each lane keeps one phase pair in registers and applies it to the warp's RW rows
-#pragma unroll 2
-            for (int jp = lane; jp < nj / 2; jp += 32) {
+            // lane iterations jp = lane + 32 it; the Q pairs of iteration it arrive through an
+            // S-deep cp.async ring (the slot refilled at iteration it is the one read at it - 1)
+            const int npair = nj / 2;
+            const int nit = lane < npair ? (npair - lane + 31) / 32 : 0;
+#pragma unroll
+            for (int st = 0; st < S - 1; st++) {
+                if (st < nit) {
+                    const int jp = lane + 32 * st;
+#pragma unroll
+                    for (int r = 0; r < RW; r++) cp_async16(qs + (st * RW + r) * 32, qrow[r] + j0 / 2 + jp);
+                }
+                cp_async_commit();
+            }
+            for (int it = 0; it < nit; it++) {
+                const int nxt = it + S - 1;
+                if (nxt < nit) {
+                    const int jp = lane + 32 * nxt, sl = nxt % S;
+#pragma unroll
+                    for (int r = 0; r < RW; r++) cp_async16(qs + (sl * RW + r) * 32, qrow[r] + j0 / 2 + jp);
+                }
+                cp_async_commit();
+                cp_async_wait<S - 1>();
+                const int jp = lane + 32 * it, sl = it % S;
                 float4 f[NK];
 #pragma unroll
                 for (int kk = 0; kk < NK; kk++) f[kk] = ph[kk][jp];
-                float4 q[RW];
-#pragma unroll
-                for (int r = 0; r < RW; r++) q[r] = __ldcs(qrow[r] + j0 / 2 + jp);     // streamed once: evict-first
 #pragma unroll
                 for (int r = 0; r < RW; r++) {
+                    const float4 q = qs[(sl * RW + r) * 32];
 #pragma unroll
                     for (int kk = 0; kk < NK; kk++) {
-                        acc[r][kk][0] = fmaf(q[r].x, f[kk].x, fmaf(-q[r].y, f[kk].y, acc[r][kk][0]));
-                        acc[r][kk][1] = fmaf(q[r].x, f[kk].y, fmaf(q[r].y, f[kk].x, acc[r][kk][1]));
-                        acc[r][kk][0] = fmaf(q[r].z, f[kk].z, fmaf(-q[r].w, f[kk].w, acc[r][kk][0]));
-                        acc[r][kk][1] = fmaf(q[r].z, f[kk].w, fmaf(q[r].w, f[kk].z, acc[r][kk][1]));
+                        acc[r][kk][0] = fmaf(q.x, f[kk].x, fmaf(-q.y, f[kk].y, acc[r][kk][0]));
+                        acc[r][kk][1] = fmaf(q.x, f[kk].y, fmaf(q.y, f[kk].x, acc[r][kk][1]));
+                        acc[r][kk][0] = fmaf(q.z, f[kk].z, fmaf(-q.w, f[kk].w, acc[r][kk][0]));
+                        acc[r][kk][1] = fmaf(q.z, f[kk].w, fmaf(q.w, f[kk].z, acc[r][kk][1]));
                     }
                 }
             }
+            cp_async_wait<0>();
         }
     }
 #pragma unroll
@@ -396,14 +435,17 @@ static scw_status stage1_record(scw_sep s, const SepEvalPlan& p, const char* d_d
             ctx->launches++;
             auto grid_for = [&](int rw) { return dim3((3 * MF + kCtrWarps * rw - 1) / (kCtrWarps * rw), (unsigned)groups.size()); };
             LaunchTimer lt(ctx, "sep_contract_kernel");
-            if (nks == 1)
-                sep_contract_kernel<1, 8><<<grid_for(8), kCtrWarps * 32, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
-            else if (nks == 2)
-                sep_contract_kernel<2, 8><<<grid_for(8), kCtrWarps * 32, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
-            else if (nks == 4)
-                sep_contract_kernel<4, 4><<<grid_for(4), kCtrWarps * 32, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
-            else
-                sep_contract_kernel<8, 2><<<grid_for(2), kCtrWarps * 32, 0, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+            auto launch = [&](auto kernel, int rw, size_t smem) -> scw_status {
+                SCW_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                kernel<<<grid_for(rw), kCtrWarps * 32, smem, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+                return SCW_OK;
+            };
+            scw_status ls;
+            if (nks == 1) ls = launch(sep_contract_kernel<1, 8>, 8, CtrCfg<8, 1>::kSmem);
+            else if (nks == 2) ls = launch(sep_contract_kernel<2, 8>, 8, CtrCfg<8, 2>::kSmem);
+            else if (nks == 4) ls = launch(sep_contract_kernel<4, 4>, 4, CtrCfg<4, 4>::kSmem);
+            else ls = launch(sep_contract_kernel<8, 2>, 2, CtrCfg<2, 8>::kSmem);
+            if (ls != SCW_OK) return ls;
             SCW_CUDA_TRY(cudaGetLastError());
             ctx->launches++;
         } else {

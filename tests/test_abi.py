@@ -55,3 +55,11 @@ def test_solve_parameter_block():
     import pytest
     with pytest.raises(ValueError):
         solver._params(1, (0, 0, 1), (1, 0), (0, 0), (0, 0), (1.0, 1.2, 1.5), 0, (8, 8, 2), 0, None, False, True)
+
+
+def test_viewer_options_mirror_the_reference():
+    """sCWatterView's option names and defaults (sCWatterView.cpp:682-697)."""
+    from scwatter_gb300 import scwatterview
+    a = scwatterview.parser().parse_args(["--nogui"])
+    assert a.input == "c.cw" and a.cuda == 0 and a.size == 100.0 and a.resolution == 8 and a.output == "xz.npy"
+    assert a.axis == 1 and a.center == [0.0, 0.0, 0.0] and a.slice == 0.0

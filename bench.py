@@ -43,6 +43,9 @@ UNIT = "points*modes/s"
 
 CFG2 = dict(name="spheres[64,128,128] coef40x40 64 slices, grid 512x512x256", M0=40, M1=40, Z=64,
             size=(128.0, 128.0, 64.0), Nx=512, Ny=512, Nz=256, x0=-64.0, x1=64.0, y0=-64.0, y1=64.0)
+# DRAM bytes / algorithmic bytes of sep_contract_kernel from one ncu capture of the 8-slice case
+# (dram__bytes_read.sum + dram__bytes_write.sum = 1.968409 GB + 4.705 MB for 1.967309 GB of Q and C)
+CONTRACT_TRAFFIC_RATIO = (1.968409e9 + 4.704768e6) / 1.9673088e9
 PLAIN_PATCH = 128          # plain-form sample: PLAIN_PATCH x PLAIN_PATCH points of one interior xy plane
 CPU_SLICE = 3              # the slice the plain and CPU samples lie in
 
@@ -348,7 +351,10 @@ def run_ours(args):
                            "wall_s_timed_region": t_wall},
                 "roofline": {"bound": "hbm", "kernel": "sep_contract_kernel (streams every Q block once)",
                              "achieved": contract_gbs, "peak": hbm_peak, "unit": "GB/s",
-                             "frac": contract_gbs / hbm_peak if contract_gbs else None, "traffic": None,
+                             "frac": contract_gbs / hbm_peak if contract_gbs else None,
+                             "traffic": (q_bytes + c_bytes) * CONTRACT_TRAFFIC_RATIO,
+                             "traffic_source": "ncu DRAM bytes of the 8-slice case (1.973 GB for 1.967 GB "
+                                               "algorithmic), scaled by the units of a full launch",
                              "algorithmic_bytes": q_bytes + c_bytes, "peak_source": peak_src},
                 "kernels_ms": {k: v[0] for k, v in kt.items()},
                 "synth_roofline": {"bound": "hbm", "achieved": synth_gbs, "peak": hbm_peak, "unit": "GB/s",

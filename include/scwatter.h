@@ -315,6 +315,17 @@ SCW_API scw_status scw_view_minmax(scw_ctx ctx, const float* S, int64_t n, float
  * imag_color[3], show_real, show_imag (12 floats, HOST). */
 SCW_API scw_status scw_view_color(scw_ctx ctx, const float* S, int64_t n, const float* params, unsigned char* rgb);
 
+/* ---------------------------------------------------------------------------------- */
+/* Homogeneous multilayer solve -- the computation of the reference program            */
+/* sCWatterLayer (sCWatterLayer.cpp:119-267), batched over incident plane waves         */
+/* ---------------------------------------------------------------------------------- */
+/* ri: L complex refractive indices (HOST, layer 0 = incident medium); z: L - 1 interfaces;
+ * n0 = Re ri[0]; k: vacuum wavenumber; waves: count HOST records of 12 doubles (incident
+ * plane waves); x: count x 6L complex (HOST; per layer the transmitted then the reflected
+ * amplitude, xyz); info: count ints (1 = singular system).  2 <= L <= 16. */
+SCW_API scw_status scw_layer_solve(scw_ctx ctx, int L, const double* ri, const double* z, double n0, double k,
+                                   int count, const double* waves, double* x, int* info);
+
 #ifdef __cplusplus
 }
 #endif

@@ -90,6 +90,7 @@ _SIGS = {
     "scw_view_scalar": [P, P, I64, I32, P],
     "scw_view_minmax": [P, P, I64, P],
     "scw_view_color": [P, P, I64, P, P],
+    "scw_layer_solve": [P, I32, P, P, F64, F64, I32, P, P, P],
     "scw_sep_create": [P, I32, I32, I32, I32, P, P, P, PP],
     "scw_sep_destroy": [P],
     "scw_sep_set_exterior": [P, P, P, P, P, P, P],

@@ -21,12 +21,16 @@ scw_status fail(scw_status st, const std::string& msg);
             return ::scw::fail(SCW_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// Device buffer owned by a context; grows on demand, never shrinks.
+// Device buffer (of a context or a call); grows on demand, never shrinks, freed on destruction.
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
     scw_status reserve(size_t n);
     void release();
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
 };
 
 // Pinned host staging buffer for small per-call descriptor uploads.
@@ -35,6 +39,10 @@ struct PinnedBuf {
     size_t bytes = 0;
     scw_status reserve(size_t n);
     void release();
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() { release(); }
 };
 
 }  // namespace scw

@@ -200,6 +200,15 @@ SCW_API scw_status scw_zgesv(scw_ctx ctx, int n, int nrhs, void* A, void* B, int
 /* eigenvalues W (n) and right eigenvectors V (n x n, column k = eigenvector k) of A (n x n,
  * overwritten); SCW_ERR_NUMERIC if the QR iteration does not converge. */
 SCW_API scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* status_host);
+/* Same contract as scw_zgeev (n <= 4096), computed by the mixed-precision solver: FP32
+ * Householder + QR + triangular eigenvectors, then Newton refinement of all eigenpairs with FP64
+ * residuals (clusters of close eigenvalues solved as small FP64 Schur problems).  Refinement stops
+ * once max_i ||A x_i - lambda_i x_i|| / (||A||_1 ||x_i||) <= 1e-14; a matrix still above 1e-12
+ * after 6 steps is solved by the FP64 QR solver instead (and only then overwritten).  Optional per-matrix
+ * outputs: accepted_host (1 = refined result), steps_host (refinement steps), residual_host
+ * (last relative residual of the refined result). */
+SCW_API scw_status scw_zgeev_mixed(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* accepted_host,
+                                   int* steps_host, double* residual_host);
 
 /* ---------------------------------------------------------------------------------- */
 /* Per-layer coupled-wave solve (FP64, on the GPU) -- the computation of the reference  */
@@ -217,6 +226,9 @@ typedef struct scw_solve_params {
     int external;         /* --external: keep only the exterior waves */
     int pz;               /* 1 = compute Ez of the modes; 0 = the reference's --npz */
     int psf;              /* --psf: every harmonic carries the incident field (sCWatter.cpp:665-669) */
+    int eig_fp64;         /* no reference counterpart.  0 (default): FP32 Householder + QR eigen-solve
+                           * refined to FP64 residuals by Newton steps, FP64 QR for any slice that
+                           * does not converge; 1: FP64 Householder + QR for every slice */
 } scw_solve_params;
 
 /* sample: [Z][Y][X] complex128 refractive index in HOST memory (the .npy volume).  Runs the
@@ -226,6 +238,12 @@ SCW_API scw_status scw_solve(scw_ctx ctx, const double* sample, int Z, int Y, in
                              scw_solution* out);
 SCW_API scw_status scw_solution_destroy(scw_solution s);
 SCW_API scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_slices, double* k);
+/* No reference counterpart: how the eigen-solves went.  mixed = 1 when the FP32 + refinement
+ * path ran; accepted = slices it finished (the others went through the FP64 QR solver);
+ * max_steps = most refinement steps an accepted slice needed; max_residual = largest
+ * accepted max_i ||A x_i - lambda_i x_i|| / (||A||_1 ||x_i||). */
+SCW_API scw_status scw_solution_eig_info(scw_solution s, int* mixed, int* accepted, int* max_steps,
+                                         double* max_residual);
 /* gamma: Z x 2MF complex downward roots (the reference's even-slot eigenvalues); x: 6MF
  * complex reflected / transmitted amplitudes (sCWatter.cpp:722); ef: 3MF incident Fourier
  * amplitudes; z_boundaries: Z + 1.  Any pointer may be NULL. */

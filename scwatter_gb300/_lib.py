@@ -66,6 +66,7 @@ _SIGS = {
     "scw_solve": [P, P, I32, I32, I32, P, PP],
     "scw_solution_destroy": [P],
     "scw_solution_info": [P, P, P, P, P],
+    "scw_solution_eig_info": [P, P, P, P, P],
     "scw_solution_get": [P, P, P, P, P],
     "scw_solution_get_modes": [P, I32, P, P],
     "scw_solution_to_sep": [P, PP],
@@ -105,6 +106,7 @@ _SIGS = {
     "scw_zgemm": [P, I32, I32, I32, P, P, P, P, P, I32],
     "scw_zgesv": [P, I32, I32, P, P, I32, P],
     "scw_zgeev": [P, I32, P, P, P, I32, P],
+    "scw_zgeev_mixed": [P, I32, P, P, P, I32, P, P, P],
 }
 
 

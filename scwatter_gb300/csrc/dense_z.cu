@@ -16,32 +16,10 @@
 #include <vector>
 
 #include "scw_dense.h"
+#include "scw_complex.cuh"
 
 namespace scw {
 namespace z {
-
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {   // conj(a) * b
-    return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {   // a * b + c
-    return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
-}
-__device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
-__device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
-__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
-    // Smith's algorithm
-    if (fabs(b.x) >= fabs(b.y)) {
-        const double r = b.y / b.x, d = b.x + b.y * r;
-        return make_double2((a.x + a.y * r) / d, (a.y - a.x * r) / d);
-    }
-    const double r = b.x / b.y, d = b.x * r + b.y;
-    return make_double2((a.x * r + a.y) / d, (a.y * r - a.x) / d);
-}
 
 // ------------------------------------------------------------------------------------
 // GEMM: C = alpha * op(A) * B + beta * C, op = identity.  64 x 64 tiles, 256 threads, each
@@ -49,35 +27,37 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 // ------------------------------------------------------------------------------------
 constexpr int kGT = 64, kGK = 16;
 
+template <typename C>
 __global__ void __launch_bounds__(256)
-zgemm_kernel(int M, int N, int K, double2 alpha, const double2* __restrict__ A, int lda, long long sA,
-             const double2* __restrict__ B, int ldb, long long sB, double2 beta, double2* __restrict__ C, int ldc,
-             long long sC) {
-    __shared__ double2 As[kGK][kGT + 1];
-    __shared__ double2 Bs[kGK][kGT + 1];
+gemm_kernel(int M, int N, int K, C alpha, const C* __restrict__ A, int lda, long long sA, const C* __restrict__ B,
+            int ldb, long long sB, C beta, C* __restrict__ Cm, int ldc, long long sC, const int* __restrict__ skip) {
+    if (skipped(skip, blockIdx.z)) return;
+    __shared__ C As[kGK][kGT + 1];
+    __shared__ C Bs[kGK][kGT + 1];
     A += sA * blockIdx.z;
     B += sB * blockIdx.z;
-    C += sC * blockIdx.z;
+    Cm += sC * blockIdx.z;
     const int i0 = blockIdx.y * kGT, j0 = blockIdx.x * kGT;
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    double2 acc[4][4];
+    const C zero = CT<C>::mk(0, 0);
+    C acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; a++)
 #pragma unroll
-        for (int b = 0; b < 4; b++) acc[a][b] = make_double2(0.0, 0.0);
+        for (int b = 0; b < 4; b++) acc[a][b] = zero;
     for (int k0 = 0; k0 < K; k0 += kGK) {
         for (int e = threadIdx.x; e < kGK * kGT; e += 256) {
             const int r = e / kGK, kk = e % kGK;         // A tile: rows i0 + r, cols k0 + kk
             const int gi = i0 + r, gk = k0 + kk;
-            As[kk][r] = (gi < M && gk < K) ? A[(long long)gi * lda + gk] : make_double2(0.0, 0.0);
+            As[kk][r] = (gi < M && gk < K) ? A[(long long)gi * lda + gk] : zero;
             const int kk2 = e / kGT, c = e % kGT;         // B tile: rows k0 + kk2, cols j0 + c
             const int gk2 = k0 + kk2, gj = j0 + c;
-            Bs[kk2][c] = (gk2 < K && gj < N) ? B[(long long)gk2 * ldb + gj] : make_double2(0.0, 0.0);
+            Bs[kk2][c] = (gk2 < K && gj < N) ? B[(long long)gk2 * ldb + gj] : zero;
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < kGK; kk++) {
-            double2 a[4], b[4];
+            C a[4], b[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 a[q] = As[kk][ty + 16 * q];
@@ -98,9 +78,9 @@ zgemm_kernel(int M, int N, int K, double2 alpha, const double2* __restrict__ A, 
         for (int q = 0; q < 4; q++) {
             const int gj = j0 + tx + 16 * q;
             if (gj >= N) continue;
-            double2* c = C + (long long)gi * ldc + gj;
-            double2 v = cmul(alpha, acc[p][q]);
-            if (beta.x != 0.0 || beta.y != 0.0) v = cfma(beta, *c, v);
+            C* c = Cm + (long long)gi * ldc + gj;
+            C v = cmul(alpha, acc[p][q]);
+            if (beta.x != 0 || beta.y != 0) v = cfma(beta, *c, v);
             *c = v;
         }
     }
@@ -114,20 +94,22 @@ zgemm_kernel(int M, int N, int K, double2 alpha, const double2* __restrict__ A, 
 // ------------------------------------------------------------------------------------
 constexpr int kNB = 32;
 
+template <typename C>
 __global__ void __launch_bounds__(512)
-lu_panel_kernel(double2* __restrict__ A, int n, int lda, long long sA, int k0, int nb, int* __restrict__ piv,
-                long long sP, int* __restrict__ info) {
+lu_panel_kernel(C* __restrict__ A, int n, int lda, long long sA, int k0, int nb, int* __restrict__ piv, long long sP,
+                int* __restrict__ info) {
+    using R = typename CT<C>::R;
     A += sA * blockIdx.x;
     piv += sP * blockIdx.x;
-    __shared__ double red_v[512];
+    __shared__ R red_v[512];
     __shared__ int red_i[512];
-    __shared__ double2 pivrow[kNB];
+    __shared__ C pivrow[kNB];
     for (int k = k0; k < k0 + nb; k++) {
         // pivot search over rows k..n-1 of column k
-        double best = -1.0;
+        R best = -1;
         int bi = k;
         for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
-            const double v = cabs1(A[(long long)i * lda + k]);
+            const R v = cabs1(A[(long long)i * lda + k]);
             if (v > best) {
                 best = v;
                 bi = i;
@@ -138,7 +120,7 @@ lu_panel_kernel(double2* __restrict__ A, int n, int lda, long long sA, int k0, i
         __syncthreads();
         for (int s = blockDim.x / 2; s > 0; s >>= 1) {
             if (threadIdx.x < s) {
-                const double o = red_v[threadIdx.x + s];
+                const R o = red_v[threadIdx.x + s];
                 const int oi = red_i[threadIdx.x + s];
                 if (o > red_v[threadIdx.x] || (o == red_v[threadIdx.x] && oi < red_i[threadIdx.x])) {
                     red_v[threadIdx.x] = o;
@@ -148,7 +130,7 @@ lu_panel_kernel(double2* __restrict__ A, int n, int lda, long long sA, int k0, i
             __syncthreads();
         }
         const int p = red_i[0];
-        const bool zero = red_v[0] == 0.0;
+        const bool zero = red_v[0] == 0;
         if (threadIdx.x == 0) {
             piv[k] = p;
             if (zero && info[blockIdx.x] == 0) info[blockIdx.x] = k + 1;
@@ -156,20 +138,20 @@ lu_panel_kernel(double2* __restrict__ A, int n, int lda, long long sA, int k0, i
         // swap rows k and p inside the panel columns k0 .. k0+nb-1
         if (p != k) {
             for (int j = k0 + threadIdx.x; j < k0 + nb; j += blockDim.x) {
-                const double2 t = A[(long long)k * lda + j];
+                const C t = A[(long long)k * lda + j];
                 A[(long long)k * lda + j] = A[(long long)p * lda + j];
                 A[(long long)p * lda + j] = t;
             }
         }
         __syncthreads();
-        const double2 d = A[(long long)k * lda + k];
+        const C d = A[(long long)k * lda + k];
         for (int j = k + 1 + threadIdx.x; j < k0 + nb; j += blockDim.x) pivrow[j - k0] = A[(long long)k * lda + j];
         __syncthreads();
         // scale the column below the pivot and update the remaining panel columns
-        const double2 inv = zero ? make_double2(0.0, 0.0) : cdiv(make_double2(1.0, 0.0), d);
+        const C inv = zero ? CT<C>::mk(0, 0) : cdiv(CT<C>::mk(1, 0), d);
         for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
-            double2* row = A + (long long)i * lda;
-            const double2 l = cmul(row[k], inv);
+            C* row = A + (long long)i * lda;
+            const C l = cmul(row[k], inv);
             row[k] = l;
             for (int j = k + 1; j < k0 + nb; j++) row[j] = csub(row[j], cmul(l, pivrow[j - k0]));
         }
@@ -178,9 +160,10 @@ lu_panel_kernel(double2* __restrict__ A, int n, int lda, long long sA, int k0, i
 }
 
 // apply the panel's swaps to the columns outside the panel, then solve L11 U12 = A12
+template <typename C>
 __global__ void __launch_bounds__(256)
-lu_swap_trsm_kernel(double2* __restrict__ A, int n, int lda, long long sA, int k0, int nb,
-                    const int* __restrict__ piv, long long sP) {
+lu_swap_trsm_kernel(C* __restrict__ A, int n, int lda, long long sA, int k0, int nb, const int* __restrict__ piv,
+                    long long sP) {
     A += sA * blockIdx.y;
     piv += sP * blockIdx.y;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;    // one column per thread
@@ -188,23 +171,23 @@ lu_swap_trsm_kernel(double2* __restrict__ A, int n, int lda, long long sA, int k
     for (int k = k0; k < k0 + nb; k++) {
         const int p = piv[k];
         if (p != k) {
-            const double2 t = A[(long long)k * lda + j];
+            const C t = A[(long long)k * lda + j];
             A[(long long)k * lda + j] = A[(long long)p * lda + j];
             A[(long long)p * lda + j] = t;
         }
     }
     if (j < k0 + nb) return;                                // columns left of the panel: swaps only
     for (int k = k0; k < k0 + nb; k++) {                    // unit lower triangular solve
-        double2 v = A[(long long)k * lda + j];
+        C v = A[(long long)k * lda + j];
         for (int m = k0; m < k; m++) v = csub(v, cmul(A[(long long)k * lda + m], A[(long long)m * lda + j]));
         A[(long long)k * lda + j] = v;
     }
 }
 
-// Row interchanges of B from zgetrf's pivots (LAPACK laswp order), one thread per column.
+// Row interchanges of B from getrf's pivots (LAPACK laswp order), one thread per column.
+template <typename C>
 __global__ void __launch_bounds__(256)
-laswp_kernel(const int* __restrict__ piv, long long sP, double2* __restrict__ B, int ldb, long long sB, int n,
-             int nrhs) {
+laswp_kernel(const int* __restrict__ piv, long long sP, C* __restrict__ B, int ldb, long long sB, int n, int nrhs) {
     piv += sP * blockIdx.y;
     B += sB * blockIdx.y;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -212,7 +195,7 @@ laswp_kernel(const int* __restrict__ piv, long long sP, double2* __restrict__ B,
     for (int k = 0; k < n; k++) {
         const int p = piv[k];
         if (p != k) {
-            const double2 t = B[(long long)k * ldb + j];
+            const C t = B[(long long)k * ldb + j];
             B[(long long)k * ldb + j] = B[(long long)p * ldb + j];
             B[(long long)p * ldb + j] = t;
         }
@@ -222,24 +205,25 @@ laswp_kernel(const int* __restrict__ piv, long long sP, double2* __restrict__ B,
 // Triangular solve restricted to the diagonal block rows [k0, k0 + nb) of the LU factors, one
 // thread per right-hand-side column: unit lower L (upper == 0) or U (upper == 1).  Rows
 // outside the block were already folded in by the GEMM updates of the blocked solve.
+template <typename C>
 __global__ void __launch_bounds__(256)
-trsm_block_kernel(const double2* __restrict__ LU, int lda, long long sA, int k0, int nb, double2* __restrict__ B,
-                  int ldb, long long sB, int nrhs, int upper) {
+trsm_block_kernel(const C* __restrict__ LU, int lda, long long sA, int k0, int nb, C* __restrict__ B, int ldb,
+                  long long sB, int nrhs, int upper) {
     LU += sA * blockIdx.y;
     B += sB * blockIdx.y;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nrhs) return;
     if (!upper) {
         for (int i = k0; i < k0 + nb; i++) {
-            double2 v = B[(long long)i * ldb + j];
-            const double2* row = LU + (long long)i * lda;
+            C v = B[(long long)i * ldb + j];
+            const C* row = LU + (long long)i * lda;
             for (int m = k0; m < i; m++) v = csub(v, cmul(row[m], B[(long long)m * ldb + j]));
             B[(long long)i * ldb + j] = v;
         }
     } else {
         for (int i = k0 + nb - 1; i >= k0; i--) {
-            double2 v = B[(long long)i * ldb + j];
-            const double2* row = LU + (long long)i * lda;
+            C v = B[(long long)i * ldb + j];
+            const C* row = LU + (long long)i * lda;
             for (int m = i + 1; m < k0 + nb; m++) v = csub(v, cmul(row[m], B[(long long)m * ldb + j]));
             B[(long long)i * ldb + j] = cdiv(v, row[i]);
         }
@@ -250,92 +234,110 @@ trsm_block_kernel(const double2* __restrict__ LU, int lda, long long sA, int k0,
 // Hessenberg reduction A -> Q^H A Q (zgehd2 semantics: H(k) = I - tau v v^H, v(k+1) = 1),
 // one CTA per matrix, with the explicit unitary Q accumulated (Q := Q H(k)).
 // ------------------------------------------------------------------------------------
-__device__ double block_sum(double v, double* sh) {
+template <typename R>
+__device__ R block_sum(R v, R* sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     __syncthreads();
     if (lane == 0) sh[w] = v;
     __syncthreads();
-    double s = 0.0;
+    R s = 0;
     for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[i];
     return s;
 }
 
+// y[i] = tau * sum_{j >= j0} M[i][j] v[j] for every row i: a warp per row, lanes along the row
+// (coalesced), then a butterfly sum
+template <typename C>
+__device__ __forceinline__ void row_products(const C* __restrict__ M, const C* __restrict__ v, C* __restrict__ y, int n,
+                                             int j0, C tau) {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = threadIdx.x >> 5; i < n; i += nw) {
+        const C* row = M + (long long)i * n;
+        C s = CT<C>::mk(0, 0);
+#pragma unroll 4
+        for (int j = j0 + lane; j < n; j += 32) s = cfma(row[j], v[j], s);
+        for (int o = 16; o > 0; o >>= 1) {
+            s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+            s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+        }
+        if (lane == 0) y[i] = cmul(tau, s);
+    }
+}
+
+template <typename C>
 __global__ void __launch_bounds__(1024)
-hessenberg_kernel(double2* __restrict__ A, double2* __restrict__ Q, int n, long long sA, double2* __restrict__ work) {
+hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* __restrict__ work,
+                  const int* __restrict__ skip) {
+    using R = typename CT<C>::R;
+    if (skipped(skip, blockIdx.x)) return;
     A += sA * blockIdx.x;
     Q += sA * blockIdx.x;
-    double2* v = work + (long long)blockIdx.x * 3 * n;      // Householder vector (rows k+1..n-1)
-    double2* w = v + n;                                       // v^H A (row vector) / A v (column)
-    double2* y = w + n;
-    __shared__ double sh[32];
-    __shared__ double2 s_tau, s_beta;
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) Q[i] = make_double2((i / n) == (i % n) ? 1.0 : 0.0, 0.0);
+    C* v = work + (long long)blockIdx.x * 3 * n;      // Householder vector (rows k+1..n-1)
+    C* w = v + n;                                       // v^H A (row vector) / A v (column)
+    C* y = w + n;
+    __shared__ R sh[32];
+    __shared__ C s_tau, s_beta;
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) Q[i] = CT<C>::mk((i / n) == (i % n) ? 1 : 0, 0);
     __syncthreads();
     for (int k = 0; k + 2 < n; k++) {
         // Householder for x = A[k+1:n, k] (zlarfg)
-        double xn2 = 0.0;
+        R xn2 = 0;
         for (int i = k + 2 + threadIdx.x; i < n; i += blockDim.x) xn2 += cabs2(A[(long long)i * n + k]);
         xn2 = block_sum(xn2, sh);
-        const double2 alpha = A[(long long)(k + 1) * n + k];
+        const C alpha = A[(long long)(k + 1) * n + k];
         if (threadIdx.x == 0) {
-            if (xn2 == 0.0 && alpha.y == 0.0) {
-                s_tau = make_double2(0.0, 0.0);
+            if (xn2 == 0 && alpha.y == 0) {
+                s_tau = CT<C>::mk(0, 0);
                 s_beta = alpha;
             } else {
-                const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
-                s_tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-                s_beta = make_double2(beta, 0.0);
+                const R beta = -r_copysign(r_sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+                s_tau = CT<C>::mk((beta - alpha.x) / beta, -alpha.y / beta);
+                s_beta = CT<C>::mk(beta, 0);
             }
         }
         __syncthreads();
-        const double2 tau = s_tau;
-        if (tau.x == 0.0 && tau.y == 0.0) {
+        const C tau = s_tau;
+        if (tau.x == 0 && tau.y == 0) {
             __syncthreads();
             continue;
         }
-        const double2 scal = cdiv(make_double2(1.0, 0.0), csub(alpha, s_beta));
+        const C scal = cdiv(CT<C>::mk(1, 0), csub(alpha, s_beta));
         for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x)
-            v[i] = (i == k + 1) ? make_double2(1.0, 0.0) : cmul(A[(long long)i * n + k], scal);
+            v[i] = (i == k + 1) ? CT<C>::mk(1, 0) : cmul(A[(long long)i * n + k], scal);
         __syncthreads();
-        // right: A[:, k+1:] -= tau (A[:, k+1:] v) v^H   (all rows)
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            double2 s = make_double2(0.0, 0.0);
-            const double2* row = A + (long long)i * n;
-            for (int j = k + 1; j < n; j++) s = cfma(row[j], v[j], s);
-            y[i] = cmul(tau, s);
-        }
+        // right: A[:, k+1:] -= tau (A[:, k+1:] v) v^H   (all rows; a warp per row for the products)
+        row_products(A, v, y, n, k + 1, tau);
         __syncthreads();
         for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
-            const double2 vc = make_double2(v[j].x, -v[j].y);
+            const C vc = CT<C>::mk(v[j].x, -v[j].y);
+#pragma unroll 4
             for (int i = 0; i < n; i++) A[(long long)i * n + j] = csub(A[(long long)i * n + j], cmul(y[i], vc));
         }
         __syncthreads();
         // left: A[k+1:, k+1:] -= conj(tau) v (v^H A[k+1:, k+1:])
         for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
-            double2 s = make_double2(0.0, 0.0);
-            for (int i = k + 1; i < n; i++) s = cfma(make_double2(v[i].x, -v[i].y), A[(long long)i * n + j], s);
-            w[j] = cmul(make_double2(tau.x, -tau.y), s);
+            C s = CT<C>::mk(0, 0);
+#pragma unroll 4
+            for (int i = k + 1; i < n; i++) s = cfma(CT<C>::mk(v[i].x, -v[i].y), A[(long long)i * n + j], s);
+            w[j] = cmul(CT<C>::mk(tau.x, -tau.y), s);
         }
         __syncthreads();
         for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
-            const double2 wj = w[j];
+            const C wj = w[j];
+#pragma unroll 4
             for (int i = k + 1; i < n; i++) A[(long long)i * n + j] = csub(A[(long long)i * n + j], cmul(v[i], wj));
         }
         // column k below the subdiagonal
         for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x)
-            A[(long long)i * n + k] = (i == k + 1) ? s_beta : make_double2(0.0, 0.0);
+            A[(long long)i * n + k] = (i == k + 1) ? s_beta : CT<C>::mk(0, 0);
         // Q[:, k+1:] -= (Q[:, k+1:] v) tau v^H
         __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            double2 s = make_double2(0.0, 0.0);
-            const double2* row = Q + (long long)i * n;
-            for (int j = k + 1; j < n; j++) s = cfma(row[j], v[j], s);
-            y[i] = cmul(tau, s);
-        }
+        row_products(Q, v, y, n, k + 1, tau);
         __syncthreads();
         for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
-            const double2 vc = make_double2(v[j].x, -v[j].y);
+            const C vc = CT<C>::mk(v[j].x, -v[j].y);
+#pragma unroll 4
             for (int i = 0; i < n; i++) Q[(long long)i * n + j] = csub(Q[(long long)i * n + j], cmul(y[i], vc));
         }
         __syncthreads();
@@ -347,92 +349,152 @@ hessenberg_kernel(double2* __restrict__ A, double2* __restrict__ Q, int n, long 
 // Schur vectors accumulated into Z (Z := Z G^H).  One CTA per matrix.  status[b]: 0 ok,
 // 1 no convergence within 30 n iterations.
 // ------------------------------------------------------------------------------------
-__device__ __forceinline__ void zlartg(double2 f, double2 g, double& c, double2& s, double2& r) {
-    // c s: [c, s; -conj(s), c] [f; g] = [r; 0], c real
-    const double gf = cabs2(g);
-    if (gf == 0.0) {
-        c = 1.0;
-        s = make_double2(0.0, 0.0);
-        r = f;
-        return;
-    }
-    const double ff = cabs2(f);
-    if (ff == 0.0) {
-        c = 0.0;
-        const double ag = sqrt(gf);
-        s = make_double2(g.x / ag, -g.y / ag);            // conj(g) / |g|
-        r = make_double2(ag, 0.0);
-        return;
-    }
-    const double af = sqrt(ff), d = sqrt(ff + gf);
-    c = af / d;
-    const double2 fs = make_double2(f.x / af, f.y / af);  // f / |f|
-    s = cmulc(g, fs);                                       // conj(g) f / |f|  ... scaled below
-    s = make_double2(s.x / d, s.y / d);
-    r = make_double2(fs.x * d, fs.y * d);
+// G [x; y] (rows) and [x, y] G^H (columns) for G = [c, s; -conj(s), c]
+template <typename C>
+__device__ __forceinline__ void rot_rows(typename CT<C>::R c, C s, C& x, C& y) {
+    const C nx = CT<C>::mk(c * x.x + (s.x * y.x - s.y * y.y), c * x.y + (s.x * y.y + s.y * y.x));
+    const C ny = CT<C>::mk(c * y.x - (s.x * x.x + s.y * x.y), c * y.y - (s.x * x.y - s.y * x.x));
+    x = nx;
+    y = ny;
+}
+template <typename C>
+__device__ __forceinline__ void rot_cols(typename CT<C>::R c, C s, C& x, C& y) {
+    const C nx = CT<C>::mk(c * x.x + (y.x * s.x + y.y * s.y), c * x.y + (y.y * s.x - y.x * s.y));
+    const C ny = CT<C>::mk(c * y.x - (x.x * s.x - x.y * s.y), c * y.y - (x.x * s.y + x.y * s.x));
+    x = nx;
+    y = ny;
 }
 
+// Rotations k0 .. k1-1 of a single-shift sweep over the active block [l, ihi].  Rotation k
+// touches rows / columns k, k+1 only, so the chase needs just the window rows k0..k1+1,
+// columns k0-1..k1: warp 0 runs it in shared memory (one rotation after another, no block
+// barrier) and records the rotations.  Then the whole CTA applies them, in order, to what lies
+// outside the window: rows k0..k1 right of column k1, columns k0..k1 above row k0, and the
+// Schur vectors Z[:, k0..k1], each thread streaming one column or row with two values live.
+// Every element sees the same operations in the same order as rotation-by-rotation.
+constexpr int kHqrW = 64;
+
+template <typename C>
+__device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, int ihi, int k0, int k1, C shift,
+                          C* hw, typename CT<C>::R* hc, C* hs) {
+    using R = typename CT<C>::R;
+    constexpr int ldw = kHqrW + 2;
+    const int r1 = min(k1 + 1, ihi);
+    const int c0 = (k0 > l) ? k0 - 1 : k0;
+    const int nr = r1 - k0 + 1, nc = k1 - c0 + 1;
+    for (int e = threadIdx.x; e < nr * nc; e += blockDim.x) {
+        const int i = e / nc, j = e % nc;
+        hw[i * ldw + j] = H[(long long)(k0 + i) * n + c0 + j];
+    }
+    __syncthreads();
+#define HW(i, j) hw[((i) - k0) * ldw + ((j) - c0)]
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        for (int k = k0; k < k1; k++) {
+            if (lane == 0) {
+                C f, g, r, s;
+                R c;
+                if (k == l) {
+                    f = csub(HW(l, l), shift);
+                    g = HW(l + 1, l);
+                } else {
+                    f = HW(k, k - 1);
+                    g = HW(k + 1, k - 1);
+                }
+                zlartg(f, g, c, s, r);
+                if (k > l) {
+                    HW(k, k - 1) = r;
+                    HW(k + 1, k - 1) = CT<C>::mk(0, 0);
+                }
+                hc[k - k0] = c;
+                hs[k - k0] = s;
+            }
+            __syncwarp();
+            const R c = hc[k - k0];
+            const C s = hs[k - k0];
+            for (int j = k + lane; j <= k1; j += 32) rot_rows(c, s, HW(k, j), HW(k + 1, j));
+            __syncwarp();
+            const int rmax = min(k + 2, ihi);
+            for (int i = k0 + lane; i <= rmax; i += 32) rot_cols(c, s, HW(i, k), HW(i, k + 1));
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nr * nc; e += blockDim.x) {
+        const int i = e / nc, j = e % nc;
+        H[(long long)(k0 + i) * n + c0 + j] = hw[i * ldw + j];
+    }
+#undef HW
+    const int nright = n - 1 - k1, nabove = k0;
+    for (int t = threadIdx.x; t < nright + nabove + n; t += blockDim.x) {
+        if (t < nright) {                           // column j, rows k0..k1
+            C* col = H + k1 + 1 + t;
+            C x = col[(long long)k0 * n];
+#pragma unroll 4
+            for (int k = k0; k < k1; k++) {
+                C y = col[(long long)(k + 1) * n];
+                rot_rows(hc[k - k0], hs[k - k0], x, y);
+                col[(long long)k * n] = x;
+                x = y;
+            }
+            col[(long long)k1 * n] = x;
+        } else {                                    // row i of H (above the window) or of Z, columns k0..k1
+            C* row = (t < nright + nabove) ? H + (long long)(t - nright) * n : Z + (long long)(t - nright - nabove) * n;
+            C x = row[k0];
+#pragma unroll 4
+            for (int k = k0; k < k1; k++) {
+                C y = row[k + 1];
+                rot_cols(hc[k - k0], hs[k - k0], x, y);
+                row[k] = x;
+                x = y;
+            }
+            row[k1] = x;
+        }
+    }
+    __syncthreads();
+}
+
+template <typename C>
+constexpr size_t hqr_smem_bytes() {
+    return sizeof(C) * ((kHqrW + 2) * (kHqrW + 2) + kHqrW) + sizeof(typename CT<C>::R) * kHqrW;
+}
+
+template <typename C>
 __global__ void __launch_bounds__(1024)
-hqr_kernel(double2* __restrict__ H, double2* __restrict__ Z, int n, long long sA, double2* __restrict__ eig,
-           int* __restrict__ status) {
+hqr_kernel(C* __restrict__ H, C* __restrict__ Z, int n, long long sA, C* __restrict__ eig, int* __restrict__ status,
+           const int* __restrict__ skip) {
+    using R = typename CT<C>::R;
+    if (skipped(skip, blockIdx.x)) return;
     H += sA * blockIdx.x;
     Z += sA * blockIdx.x;
     eig += (long long)n * blockIdx.x;
-    __shared__ double s_c;
-    __shared__ double2 s_s;
-    __shared__ int s_l, s_done;
-    const double ulp = 2.220446049250313e-16;
-    const double smlnum = 2.2250738585072014e-308 * ((double)n / ulp);
+    __shared__ C s_s;
+    __shared__ int s_red[32];
+    extern __shared__ __align__(16) unsigned char hqr_smem[];
+    C* hw = reinterpret_cast<C*>(hqr_smem);                         // (kHqrW + 2)^2 window
+    C* hs = hw + (kHqrW + 2) * (kHqrW + 2);                         // kHqrW rotation sines
+    R* hc = reinterpret_cast<R*>(hs + kHqrW);                       // kHqrW rotation cosines
     int ihi = n - 1;
     int its = 0;
     const int itmax = 30 * max(10, n);
     int total = 0;
     while (ihi >= 0) {
-        // look for a small subdiagonal element in [0, ihi]
-        if (threadIdx.x == 0) {
-            int l = 0;
-            for (int k = ihi; k > 0; k--) {
-                const double2 hkk1 = H[(long long)k * n + k - 1];
-                if (cabs1(hkk1) <= smlnum) {
-                    l = k;
-                    break;
-                }
-                double tst = cabs1(H[(long long)(k - 1) * n + k - 1]) + cabs1(H[(long long)k * n + k]);
-                if (tst == 0.0) {
-                    if (k - 2 >= 0) tst += fabs(H[(long long)(k - 1) * n + k - 2].x);
-                    if (k + 1 <= ihi) tst += fabs(H[(long long)(k + 1) * n + k].x);
-                }
-                if (fabs(hkk1.x) <= ulp * tst) {
-                    // Ahues & Tisseur conservative deflation criterion (as in zlahqr)
-                    const double2 hk1k = H[(long long)(k - 1) * n + k];
-                    const double2 hkk = H[(long long)k * n + k];
-                    const double2 hk1k1 = H[(long long)(k - 1) * n + k - 1];
-                    const double ab = fmax(cabs1(hkk1), cabs1(hk1k));
-                    const double ba = fmin(cabs1(hkk1), cabs1(hk1k));
-                    const double2 dd = csub(hk1k1, hkk);
-                    const double aa = fmax(cabs1(hkk), cabs1(dd));
-                    const double bb = fmin(cabs1(hkk), cabs1(dd));
-                    const double s = aa + ab;
-                    if (ba * (ab / s) <= fmax(smlnum, ulp * (bb * (aa / s)))) {
-                        l = k;
-                        break;
-                    }
-                    // coincident diagonal entries (bb = 0 above): zeroing the subdiagonal moves
-                    // the two eigenvalues by at most sqrt(|h(k,k-1) h(k-1,k)|), below rounding
-                    // of h(k,k) when this holds (a diagonal matrix with repeated eigenvalues
-                    // and rounding-level couplings would otherwise never deflate)
-                    if (ba * ab <= (ulp * cabs1(hkk)) * (ulp * cabs1(hkk))) {
-                        l = k;
-                        break;
-                    }
-                }
+        // the largest k in [1, ihi] whose subdiagonal entry may be set to zero (0: none);
+        // each thread scans its ks downwards, then a block maximum
+        int lk = 0;
+        for (int k = ihi - (int)threadIdx.x; k > 0; k -= blockDim.x)
+            if (hqr_deflates(H, n, k, ihi)) {
+                lk = k;
+                break;
             }
-            s_l = l;
-        }
+        lk = __reduce_max_sync(0xffffffffu, lk);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = lk;
         __syncthreads();
-        const int l = s_l;
+        int l = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) l = max(l, s_red[w]);
+        __syncthreads();
         if (l > 0) {
-            if (threadIdx.x == 0) H[(long long)l * n + l - 1] = make_double2(0.0, 0.0);
+            if (threadIdx.x == 0) H[(long long)l * n + l - 1] = CT<C>::mk(0, 0);
         }
         if (l >= ihi) {                                   // 1x1 block: eigenvalue converged
             if (threadIdx.x == 0) eig[ihi] = H[(long long)ihi * n + ihi];
@@ -447,86 +509,41 @@ hqr_kernel(double2* __restrict__ H, double2* __restrict__ Z, int n, long long sA
         }
         its++;
         total++;
-        // exceptional shifts every 10 iterations without a deflation (zlahqr's KEXSH rule)
-        // shift
+        // shift; exceptional shifts every 10 iterations without a deflation (zlahqr's KEXSH rule)
         if (threadIdx.x == 0) {
-            double2 t;
-            const double2 hii = H[(long long)ihi * n + ihi];
+            C t;
+            const C hii = H[(long long)ihi * n + ihi];
             if (its % 20 == 0) {
-                t = make_double2(0.75 * fabs(H[(long long)ihi * n + ihi - 1].x) + hii.x, hii.y);
+                t = CT<C>::mk(R(0.75) * r_abs(H[(long long)ihi * n + ihi - 1].x) + hii.x, hii.y);
             } else if (its % 10 == 0) {
-                t = make_double2(0.75 * fabs(H[(long long)(l + 1) * n + l].x) + H[(long long)l * n + l].x,
-                                 H[(long long)l * n + l].y);
+                t = CT<C>::mk(R(0.75) * r_abs(H[(long long)(l + 1) * n + l].x) + H[(long long)l * n + l].x,
+                              H[(long long)l * n + l].y);
             } else {
                 // Wilkinson shift from the trailing 2x2 block
-                const double2 a = H[(long long)(ihi - 1) * n + ihi - 1];
-                const double2 b = H[(long long)(ihi - 1) * n + ihi];
-                const double2 c = H[(long long)ihi * n + ihi - 1];
-                const double2 d = hii;
-                const double2 half = make_double2(0.5 * (a.x - d.x), 0.5 * (a.y - d.y));
-                const double2 bc = cmul(b, c);
-                const double2 disc = cfma(half, half, bc);
-                // complex sqrt
-                const double2 sq = zsqrt(disc);
+                const C a = H[(long long)(ihi - 1) * n + ihi - 1];
+                const C b = H[(long long)(ihi - 1) * n + ihi];
+                const C c = H[(long long)ihi * n + ihi - 1];
+                const C d = hii;
+                const C half = CT<C>::mk(R(0.5) * (a.x - d.x), R(0.5) * (a.y - d.y));
+                const C bc = cmul(b, c);
+                const C disc = cfma(half, half, bc);
+                const C sq = zsqrt(disc);
                 // choose the root that makes the shift closer to d
-                double2 e1 = cadd(half, sq), e2 = csub(half, sq);
-                const double2 den = cabs2(e1) >= cabs2(e2) ? e1 : e2;
-                t = (cabs2(den) == 0.0) ? d : csub(d, cdiv(bc, den));
+                C e1 = cadd(half, sq), e2 = csub(half, sq);
+                const C den = cabs2(e1) >= cabs2(e2) ? e1 : e2;
+                t = (cabs2(den) == 0) ? d : csub(d, cdiv(bc, den));
             }
             s_s = t;                                      // reuse as shift storage
         }
         __syncthreads();
-        const double2 shift = s_s;
+        const C shift = s_s;
         __syncthreads();
-        // implicit single-shift QR sweep over the active block [l, ihi]
-        for (int k = l; k < ihi; k++) {
-            if (threadIdx.x == 0) {
-                double2 f, g;
-                if (k == l) {
-                    f = csub(H[(long long)l * n + l], shift);
-                    g = H[(long long)(l + 1) * n + l];
-                } else {
-                    f = H[(long long)k * n + k - 1];
-                    g = H[(long long)(k + 1) * n + k - 1];
-                }
-                double c;
-                double2 s, r;
-                zlartg(f, g, c, s, r);
-                if (k > l) {
-                    H[(long long)k * n + k - 1] = r;
-                    H[(long long)(k + 1) * n + k - 1] = make_double2(0.0, 0.0);
-                }
-                s_c = c;
-                s_s = s;
-            }
-            __syncthreads();
-            const double c = s_c;
-            const double2 s = s_s;
-            // rows k, k+1, columns from k (or k-1 handled above) to n-1:  G [x; y]
-            for (int j = k + threadIdx.x; j < n; j += blockDim.x) {
-                const double2 x = H[(long long)k * n + j], yv = H[(long long)(k + 1) * n + j];
-                H[(long long)k * n + j] = make_double2(c * x.x + (s.x * yv.x - s.y * yv.y), c * x.y + (s.x * yv.y + s.y * yv.x));
-                // -conj(s) x + c y
-                H[(long long)(k + 1) * n + j] = make_double2(c * yv.x - (s.x * x.x + s.y * x.y), c * yv.y - (s.x * x.y - s.y * x.x));
-            }
-            __syncthreads();
-            // columns k, k+1, rows 0 .. min(k+2, ihi):  [x, y] G^H
-            const int rmax = min(k + 2, ihi);
-            for (int i = threadIdx.x; i <= rmax; i += blockDim.x) {
-                const double2 x = H[(long long)i * n + k], yv = H[(long long)i * n + k + 1];
-                // x c + y conj(s);  -x s + y c
-                H[(long long)i * n + k] = make_double2(c * x.x + (yv.x * s.x + yv.y * s.y), c * x.y + (yv.y * s.x - yv.x * s.y));
-                H[(long long)i * n + k + 1] = make_double2(c * yv.x - (x.x * s.x - x.y * s.y), c * yv.y - (x.x * s.y + x.y * s.x));
-            }
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                const double2 x = Z[(long long)i * n + k], yv = Z[(long long)i * n + k + 1];
-                Z[(long long)i * n + k] = make_double2(c * x.x + (yv.x * s.x + yv.y * s.y), c * x.y + (yv.y * s.x - yv.x * s.y));
-                Z[(long long)i * n + k + 1] = make_double2(c * yv.x - (x.x * s.x - x.y * s.y), c * yv.y - (x.x * s.y + x.y * s.x));
-            }
-            __syncthreads();
+        // implicit single-shift QR sweep over the active block [l, ihi], kHqrW rotations at a time
+        for (int k0 = l; k0 < ihi; k0 += kHqrW) {
+            const int k1 = min(k0 + kHqrW, ihi);
+            hqr_chunk(H, Z, n, l, ihi, k0, k1, shift, hw, hc, hs);
         }
     }
-    (void)s_done;
 }
 
 // ------------------------------------------------------------------------------------
@@ -534,35 +551,48 @@ hqr_kernel(double2* __restrict__ H, double2* __restrict__ Z, int n, long long sA
 // X[:, k] solves (T - T_kk I) x = 0 with x_k = 1, x_i = 0 for i > k.  One warp per vector.
 // X is written row-major (column k = eigenvector k).
 // ------------------------------------------------------------------------------------
+template <typename C>
 __global__ void __launch_bounds__(256)
-trevc_kernel(const double2* __restrict__ T, double2* __restrict__ X, int n, long long sA) {
+trevc_kernel(const C* __restrict__ T, C* __restrict__ X, int n, long long sA, const int* __restrict__ skip) {
+    using R = typename CT<C>::R;
+    if (skipped(skip, blockIdx.y)) return;
     T += sA * blockIdx.y;
     X += sA * blockIdx.y;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= n) return;
     const int k = warp;
-    const double ulp = 2.220446049250313e-16;
-    const double2 lam = T[(long long)k * n + k];
-    const double smin = fmax(ulp * cabs1(lam), 2.2250738585072014e-308 * ((double)n / ulp));
+    const R ulp = CT<C>::ulp;
+    const C lam = T[(long long)k * n + k];
+    const R smin = r_max(ulp * cabs1(lam), CT<C>::safmin * ((R)n / ulp));
     // x_k = 1, x_{k+1..} = 0
-    for (int i = lane; i < n; i += 32) X[(long long)i * n + k] = make_double2(i == k ? 1.0 : 0.0, 0.0);
+    for (int i = lane; i < n; i += 32) X[(long long)i * n + k] = CT<C>::mk(i == k ? 1 : 0, 0);
     __syncwarp();
     for (int i = k - 1; i >= 0; i--) {
         // x_i = -(sum_{j=i+1..k} T_ij x_j) / (T_ii - lam)
-        double2 s = make_double2(0.0, 0.0);
+        C s = CT<C>::mk(0, 0);
         for (int j = i + 1 + lane; j <= k; j += 32) s = cfma(T[(long long)i * n + j], X[(long long)j * n + k], s);
         for (int o = 16; o > 0; o >>= 1) {
             s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
             s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
         }
         if (lane == 0) {
-            double2 d = csub(T[(long long)i * n + i], lam);
-            if (cabs1(d) < smin) d = make_double2(smin, 0.0);
-            X[(long long)i * n + k] = cdiv(make_double2(-s.x, -s.y), d);
+            C d = csub(T[(long long)i * n + i], lam);
+            if (cabs1(d) < smin) d = CT<C>::mk(smin, 0);
+            X[(long long)i * n + k] = cdiv(CT<C>::mk(-s.x, -s.y), d);
         }
         __syncwarp();
     }
+}
+
+// copy of the batch entries that are not skipped
+template <typename C>
+__global__ void copy_kernel(const C* __restrict__ src, C* __restrict__ dst, long long count, const int* __restrict__ skip) {
+    if (skipped(skip, blockIdx.y)) return;
+    src += count * blockIdx.y;
+    dst += count * blockIdx.y;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
 }
 
 }  // namespace z
@@ -570,66 +600,69 @@ trevc_kernel(const double2* __restrict__ T, double2* __restrict__ X, int n, long
 // ------------------------------------------------------------------------------------
 // Host wrappers
 // ------------------------------------------------------------------------------------
-scw_status zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2* A, int lda, long long sA,
-                 const double2* B, int ldb, long long sB, double2 beta, double2* C, int ldc, long long sC,
-                 int batch) {
+template <typename C>
+scw_status gemm(cudaStream_t st, int M, int N, int K, C alpha, const C* A, int lda, long long sA, const C* B, int ldb,
+                long long sB, C beta, C* Cm, int ldc, long long sC, int batch, const int* skip) {
     if (M <= 0 || N <= 0 || batch <= 0) return SCW_OK;
     dim3 grid((N + z::kGT - 1) / z::kGT, (M + z::kGT - 1) / z::kGT, batch);
-    z::zgemm_kernel<<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC);
+    z::gemm_kernel<C><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, Cm, ldc, sC, skip);
     SCW_CUDA_TRY(cudaGetLastError());
     return SCW_OK;
 }
 
-scw_status zgetrf(cudaStream_t st, double2* A, int n, long long sA, int* piv, long long sP, int* info, int batch,
-                  double2* /*unused*/) {
+template <typename C>
+scw_status getrf(cudaStream_t st, C* A, int n, long long sA, int* piv, long long sP, int* info, int batch) {
     if (n <= 0 || batch <= 0) return SCW_OK;
     SCW_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
+    const C one = {1, 0}, minus = {-1, 0};
     for (int k0 = 0; k0 < n; k0 += z::kNB) {
         const int nb = std::min(z::kNB, n - k0);
-        z::lu_panel_kernel<<<batch, 512, 0, st>>>(A, n, n, sA, k0, nb, piv, sP, info);
+        z::lu_panel_kernel<C><<<batch, 512, 0, st>>>(A, n, n, sA, k0, nb, piv, sP, info);
         SCW_CUDA_TRY(cudaGetLastError());
         dim3 g2((n + 255) / 256, batch);
-        z::lu_swap_trsm_kernel<<<g2, 256, 0, st>>>(A, n, n, sA, k0, nb, piv, sP);
+        z::lu_swap_trsm_kernel<C><<<g2, 256, 0, st>>>(A, n, n, sA, k0, nb, piv, sP);
         SCW_CUDA_TRY(cudaGetLastError());
         const int rem = n - k0 - nb;
         if (rem > 0) {
             // A22 -= L21 U12
-            scw_status s = zgemm(st, rem, rem, nb, make_double2(-1.0, 0.0), A + (long long)(k0 + nb) * n + k0, n, sA,
-                                 A + (long long)k0 * n + k0 + nb, n, sA, make_double2(1.0, 0.0),
-                                 A + (long long)(k0 + nb) * n + k0 + nb, n, sA, batch);
+            scw_status s = gemm<C>(st, rem, rem, nb, minus, A + (long long)(k0 + nb) * n + k0, n, sA,
+                                   A + (long long)k0 * n + k0 + nb, n, sA, one, A + (long long)(k0 + nb) * n + k0 + nb,
+                                   n, sA, batch);
             if (s != SCW_OK) return s;
         }
     }
     return SCW_OK;
 }
 
-scw_status zgetrs(cudaStream_t st, const double2* LU, int n, long long sA, const int* piv, long long sP, double2* B,
-                  int nrhs, long long sB, int batch) {
+template <typename C>
+scw_status getrs(cudaStream_t st, const C* LU, int n, long long sA, const int* piv, long long sP, C* B, int nrhs,
+                 long long sB, int batch) {
     // blocked: per diagonal block a small triangular solve, the rest of the rows updated by GEMM
     if (n <= 0 || nrhs <= 0 || batch <= 0) return SCW_OK;
     constexpr int kTB = 64;
+    const C one = {1, 0}, minus = {-1, 0};
     const dim3 g((nrhs + 255) / 256, batch);
-    z::laswp_kernel<<<g, 256, 0, st>>>(piv, sP, B, nrhs, sB, n, nrhs);
+    z::laswp_kernel<C><<<g, 256, 0, st>>>(piv, sP, B, nrhs, sB, n, nrhs);
     SCW_CUDA_TRY(cudaGetLastError());
     for (int k0 = 0; k0 < n; k0 += kTB) {
         const int nb = std::min(kTB, n - k0);
-        z::trsm_block_kernel<<<g, 256, 0, st>>>(LU, n, sA, k0, nb, B, nrhs, sB, nrhs, 0);
+        z::trsm_block_kernel<C><<<g, 256, 0, st>>>(LU, n, sA, k0, nb, B, nrhs, sB, nrhs, 0);
         SCW_CUDA_TRY(cudaGetLastError());
         const int rem = n - k0 - nb;
         if (rem > 0) {
-            scw_status s = zgemm(st, rem, nrhs, nb, make_double2(-1.0, 0.0), LU + (long long)(k0 + nb) * n + k0, n, sA,
-                                 B + (long long)k0 * nrhs, nrhs, sB, make_double2(1.0, 0.0),
-                                 B + (long long)(k0 + nb) * nrhs, nrhs, sB, batch);
+            scw_status s = gemm<C>(st, rem, nrhs, nb, minus, LU + (long long)(k0 + nb) * n + k0, n, sA,
+                                   B + (long long)k0 * nrhs, nrhs, sB, one, B + (long long)(k0 + nb) * nrhs, nrhs, sB,
+                                   batch);
             if (s != SCW_OK) return s;
         }
     }
     for (int k0 = ((n - 1) / kTB) * kTB; k0 >= 0; k0 -= kTB) {
         const int nb = std::min(kTB, n - k0);
-        z::trsm_block_kernel<<<g, 256, 0, st>>>(LU, n, sA, k0, nb, B, nrhs, sB, nrhs, 1);
+        z::trsm_block_kernel<C><<<g, 256, 0, st>>>(LU, n, sA, k0, nb, B, nrhs, sB, nrhs, 1);
         SCW_CUDA_TRY(cudaGetLastError());
         if (k0 > 0) {
-            scw_status s = zgemm(st, k0, nrhs, nb, make_double2(-1.0, 0.0), LU + k0, n, sA, B + (long long)k0 * nrhs,
-                                 nrhs, sB, make_double2(1.0, 0.0), B, nrhs, sB, batch);
+            scw_status s = gemm<C>(st, k0, nrhs, nb, minus, LU + k0, n, sA, B + (long long)k0 * nrhs, nrhs, sB, one, B,
+                                   nrhs, sB, batch);
             if (s != SCW_OK) return s;
         }
     }
@@ -638,33 +671,48 @@ scw_status zgetrs(cudaStream_t st, const double2* LU, int n, long long sA, const
 
 scw_status zgehrd(cudaStream_t st, double2* A, double2* Q, int n, int batch, double2* work) {
     if (n <= 0 || batch <= 0) return SCW_OK;
-    z::hessenberg_kernel<<<batch, 1024, 0, st>>>(A, Q, n, (long long)n * n, work);
+    z::hessenberg_kernel<double2><<<batch, 1024, 0, st>>>(A, Q, n, (long long)n * n, work, nullptr);
     SCW_CUDA_TRY(cudaGetLastError());
     return SCW_OK;
 }
 
-scw_status zgeev(cudaStream_t st, double2* A, double2* W, double2* V, int n, int batch, double2* work, int* status) {
+template <typename C>
+scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, int* status, const int* skip) {
     // A (overwritten): n x n per batch entry; W: n eigenvalues; V: n x n right eigenvectors (columns)
-    // work: >= batch * (n*n + 3 n) double2
+    // work: >= batch * (n*n + 3 n) elements
     if (n <= 0 || batch <= 0) return SCW_OK;
     const long long nn = (long long)n * n;
-    double2* Q = work;                       // batch * n * n: Schur vectors
-    double2* hw = work + nn * batch;         // batch * 3n
+    C* Q = work;                             // batch * n * n: Schur vectors
+    C* hw = work + nn * batch;               // batch * 3n
     SCW_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * batch, st));
-    z::hessenberg_kernel<<<batch, 1024, 0, st>>>(A, Q, n, nn, hw);
+    z::hessenberg_kernel<C><<<batch, 1024, 0, st>>>(A, Q, n, nn, hw, skip);
     SCW_CUDA_TRY(cudaGetLastError());
-    z::hqr_kernel<<<batch, 1024, 0, st>>>(A, Q, n, nn, W, status);
+    SCW_CUDA_TRY(cudaFuncSetAttribute(z::hqr_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)z::hqr_smem_bytes<C>()));
+    z::hqr_kernel<C><<<batch, 1024, z::hqr_smem_bytes<C>(), st>>>(A, Q, n, nn, W, status, skip);
     SCW_CUDA_TRY(cudaGetLastError());
-    // X (triangular eigenvectors) into V, then V := Q X
+    // X (triangular eigenvectors) into V, then A := Q X, copied to V
     dim3 gt((n * 32 + 255) / 256, batch);
-    z::trevc_kernel<<<gt, 256, 0, st>>>(A, V, n, nn);
+    z::trevc_kernel<C><<<gt, 256, 0, st>>>(A, V, n, nn, skip);
     SCW_CUDA_TRY(cudaGetLastError());
-    // A is free now: A := Q X, then copy to V
-    scw_status s = zgemm(st, n, n, n, make_double2(1.0, 0.0), Q, n, nn, V, n, nn, make_double2(0.0, 0.0), A, n, nn, batch);
+    const C one = {1, 0}, zero = {0, 0};
+    scw_status s = gemm<C>(st, n, n, n, one, Q, n, nn, V, n, nn, zero, A, n, nn, batch, skip);
     if (s != SCW_OK) return s;
-    SCW_CUDA_TRY(cudaMemcpyAsync(V, A, sizeof(double2) * nn * batch, cudaMemcpyDeviceToDevice, st));
+    z::copy_kernel<C><<<dim3((unsigned)std::min<long long>((nn + 255) / 256, 4096), batch), 256, 0, st>>>(A, V, nn, skip);
+    SCW_CUDA_TRY(cudaGetLastError());
     return SCW_OK;
 }
+
+#define SCW_DENSE_INSTANTIATE(C)                                                                                    \
+    template scw_status gemm<C>(cudaStream_t, int, int, int, C, const C*, int, long long, const C*, int, long long, \
+                                C, C*, int, long long, int, const int*);                                           \
+    template scw_status getrf<C>(cudaStream_t, C*, int, long long, int*, long long, int*, int);                    \
+    template scw_status getrs<C>(cudaStream_t, const C*, int, long long, const int*, long long, C*, int, long long, \
+                                 int);                                                                             \
+    template scw_status geev<C>(cudaStream_t, C*, C*, C*, int, int, C*, int*, const int*);
+SCW_DENSE_INSTANTIATE(double2)
+SCW_DENSE_INSTANTIATE(float2)
+#undef SCW_DENSE_INSTANTIATE
 
 }  // namespace scw
 

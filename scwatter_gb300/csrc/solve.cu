@@ -47,6 +47,10 @@ struct scw_solution_s {
     std::vector<cd> Sz0, Sz1, EF, x;       // MF, MF, 3MF incident, 6MF boundary solution
     std::vector<cd> gam;                   // Z x 2MF downward roots
     double2* dQ = nullptr;                 // device [Z][2][3MF][2MF]: Q_check, Q_hat (FP64)
+    // mixed eigen-solver per slice: state (1 accepted, else FP64 fallback), refinement steps
+    // used, last relative residual; empty when the FP64 solver ran throughout
+    std::vector<int> eig_state, eig_steps;
+    std::vector<double> eig_res;
     ~scw_solution_s() {
         if (dQ) {
             cudaSetDevice(ctx->device);
@@ -389,6 +393,7 @@ scw_status plan_solve(const scw_solve_params* prm, int Zs, int Y, int X, SolvePl
     p.n1 = n1r;
     p.external = prm->external != 0;
     p.pz = prm->pz != 0;
+    p.eig_mixed = prm->eig_fp64 == 0 && 2 * (long long)p.MF <= mx::kMaxN;
     p.zb.resize(ZL);
     p.zb[0] = prm->z - prm->size[2] / 2.0;
     for (int i = 1; i < ZL; i++) p.zb[i] = p.zb[i - 1] + prm->size[2] / Zs;
@@ -527,6 +532,20 @@ void carve_ws(const SolvePlan& p, Carver& c, SolveWs& ws) {
     ws.beta = c.take<double2>(Z * N4);
     ws.v = c.take<double2>(N4);
     ws.piv = c.take<int>(std::max(Z * n, M6));
+    // mixed eigen-solver: small buffers of its own; S0, S1 (adjacent), its QR work and the FP32
+    // eigenvalues inside P (Z (n^2 + 3 n) double2 >= 2 Z n^2 + 4 Z n float2), S2, S3 inside W
+    if (p.eig_mixed) {
+        char* small = c.take<char>(mx::eigmix_small_bytes((int)n, (int)Z));
+        mx::eigmix_carve_small(ws.mix, small, (int)n, (int)Z);
+        float2* Pf = reinterpret_cast<float2*>(ws.P);
+        float2* Wf = reinterpret_cast<float2*>(ws.W);
+        ws.mix.S0 = Pf;
+        ws.mix.S1 = Pf + Z * nn;
+        ws.mix.hw = Pf + 2 * Z * nn;
+        ws.mix.lam32 = ws.mix.hw + 3 * Z * n;
+        ws.mix.S2 = Wf;
+        ws.mix.S3 = Wf + Z * nn;
+    }
     // temporary region, three overlays
     const size_t t0 = (c.off + 255) / 256 * 256;
     Carver ca{c.base, t0};
@@ -604,14 +623,19 @@ scw_status record_solve(const SolvePlan& p, const SolveIn& in, const SolveWs& ws
     build_pq_kernel<<<dim3(nblk(n), n, Zs), 256, 0, st>>>(ws.coef, in.up, in.wq, in.qs, in.ps, M0, M1, k, ws.P, ws.Q);
     SCW_CUDA_TRY(cudaGetLastError());
     SCW_TRY(zgemm(st, n, n, n, kOne, ws.P, n, nn, ws.Q, n, nn, kZero, ws.PQ, n, nn, Zs));
-    SCW_TRY(zgeev(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.P, out.status));
+    if (p.eig_mixed) {
+        SCW_TRY(mx::geev_mixed(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.mix, ws.P, out.status, mx::EigMixParams{}, &L));
+    } else {
+        SCW_TRY(zgeev(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.P, out.status));
+        L += 5;
+    }
     roots_kernel<<<nblk((long long)n * Zs), 256, 0, st>>>(ws.lam, n, Zs, in.dz, k, out.gam, ws.E);
     SCW_CUDA_TRY(cudaGetLastError());
     // W = Q U Gamma^-1
     SCW_TRY(zgemm(st, n, n, n, kOne, ws.Q, n, nn, ws.U, n, nn, kZero, ws.W, n, nn, Zs));
     coldiv_kernel<<<nblk(nn * Zs), 256, 0, st>>>(ws.W, n, out.gam, Zs);
     SCW_CUDA_TRY(cudaGetLastError());
-    L += 12;
+    L += 8;
     // U^-1 into P, W^-1 into PQ (LU factors in Q)
     double2* Uinv = ws.P;
     double2* Winv = ws.PQ;
@@ -804,6 +828,14 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
     SCW_CUDA_TRY(cudaMemcpyAsync(status.data(), o.status, sizeof(int) * status.size(), cudaMemcpyDeviceToHost, s));
     SCW_CUDA_TRY(cudaMemcpyAsync(sol->x.data(), o.x, sizeof(double2) * sol->x.size(), cudaMemcpyDeviceToHost, s));
     SCW_CUDA_TRY(cudaMemcpyAsync(sol->gam.data(), o.gam, sizeof(double2) * sol->gam.size(), cudaMemcpyDeviceToHost, s));
+    if (p.eig_mixed) {
+        sol->eig_state.resize(Zs);
+        sol->eig_steps.resize(Zs);
+        sol->eig_res.resize(Zs);
+        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_state.data(), ws.mix.state, sizeof(int) * Zs, cudaMemcpyDeviceToHost, s));
+        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_steps.data(), ws.mix.steps, sizeof(int) * Zs, cudaMemcpyDeviceToHost, s));
+        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_res.data(), ws.mix.res, sizeof(double) * Zs, cudaMemcpyDeviceToHost, s));
+    }
     SCW_CUDA_TRY(cudaStreamSynchronize(s));
     ctx->launches += launches;
     const std::string msg = solve_status_message(status, Zs);
@@ -873,6 +905,24 @@ scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_slices, do
     if (M1) *M1 = s->M1;
     if (n_slices) *n_slices = s->Z;
     if (k) *k = s->k;
+    return SCW_OK;
+}
+
+scw_status scw_solution_eig_info(scw_solution s, int* mixed, int* accepted, int* max_steps, double* max_residual) {
+    if (!s) return fail(SCW_ERR_ARG, "null solution");
+    int acc = 0, ms = -1;
+    double mr = 0.0;
+    for (size_t b = 0; b < s->eig_state.size(); b++) {
+        if (s->eig_state[b] == 1) {
+            acc++;
+            ms = std::max(ms, s->eig_steps[b]);
+            mr = std::max(mr, s->eig_res[b]);
+        }
+    }
+    if (mixed) *mixed = s->eig_state.empty() ? 0 : 1;
+    if (accepted) *accepted = acc;
+    if (max_steps) *max_steps = ms;
+    if (max_residual) *max_residual = mr;
     return SCW_OK;
 }
 

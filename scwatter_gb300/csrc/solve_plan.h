@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "scw_dense.h"
+#include "scw_eigmix.h"
 
 namespace scw {
 namespace sv {
@@ -26,6 +27,7 @@ struct SolvePlan {
     int M0 = 0, M1 = 0, MF = 0, n = 0;      // n = 2 MF
     double k = 0, n0 = 1, n1 = 1;
     bool external = false, pz = true;
+    bool eig_mixed = true;                  // FP32 QR + FP64 refinement (else FP64 QR throughout)
     std::vector<double> zb, dz;             // Z + 1 boundaries, Z thicknesses
     std::vector<int> ps, qs;                // integer harmonic series
     std::vector<double> up, wq;             // k grids (reference PI)
@@ -59,6 +61,8 @@ struct SolveWs {                            // scratch, reusable once the solve 
     int* piv;
     // temporary region: DFT stage (data planes, T) / cascade + boundary (X, A1, A2, A, b) / modes (Kn, Hm, Qtmp)
     double2 *F, *T, *X, *A1, *A2, *A, *b, *Kn, *Hm, *Qtmp;
+    // mixed-precision eigen-solver: FP32 slots overlay P and W (free during the eigen-solve)
+    mx::EigMixWs mix;
 };
 
 struct SolveOut {                           // results

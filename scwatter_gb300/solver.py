@@ -36,10 +36,11 @@ class _Params(ctypes.Structure):
     _fields_ = [("lam", ctypes.c_double), ("direction", ctypes.c_double * 3), ("ex", ctypes.c_double * 2),
                 ("ey", ctypes.c_double * 2), ("ez", ctypes.c_double * 2), ("n", ctypes.c_double * 2),
                 ("kappa", ctypes.c_double), ("size", ctypes.c_double * 3), ("z", ctypes.c_double),
-                ("coef", ctypes.c_int * 2), ("external", ctypes.c_int), ("pz", ctypes.c_int), ("psf", ctypes.c_int)]
+                ("coef", ctypes.c_int * 2), ("external", ctypes.c_int), ("pz", ctypes.c_int), ("psf", ctypes.c_int),
+                ("eig_fp64", ctypes.c_int)]
 
 
-def _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz, psf=False) -> _Params:
+def _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz, psf=False, eig_fp64=False) -> _Params:
     p = _Params()
     p.lam = float(lam)
     p.direction[:] = [float(v) for v in direction]
@@ -62,6 +63,7 @@ def _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz, p
     p.external = 1 if external else 0
     p.pz = 1 if pz else 0
     p.psf = 1 if psf else 0
+    p.eig_fp64 = 1 if eig_fp64 else 0
     return p
 
 
@@ -84,6 +86,12 @@ class Solution:
         self.z = np.zeros(self.Z + 1)
         _lib.call("scw_solution_get", handle, *(ctypes.c_void_p(a.ctypes.data) for a in
                                                 (self.gamma, self.x, self.EF, self.z)))
+        mixed, acc, steps, res = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _lib.call("scw_solution_eig_info", handle, ctypes.byref(mixed), ctypes.byref(acc), ctypes.byref(steps),
+                  ctypes.byref(res))
+        # eigen-solver record: mixed path on / slices it finished / most steps / largest residual
+        self.eig = {"mixed": bool(mixed.value), "accepted": acc.value, "fell_back": self.Z - acc.value if mixed.value
+                    else self.Z, "max_steps": steps.value, "max_residual": res.value}
 
     def modes(self, l: int):
         """(Q_check, Q_hat) of slice ``l``: [3MF, 2MF] complex128 each."""
@@ -129,15 +137,18 @@ class Solution:
 
 def solve(sample, lam=1.0, direction=(0.0, 0.0, 1.0), ex=(0.0, 0.0), ey=(1.0, 0.0), ez=(0.0, 0.0), n=(1.0, 1.0),
           kappa=0.0, size=(10.0, 10.0, 2.0), z=0.0, coef=None, external=False, pz=True, psf=False,
-          ctx: Context | None = None) -> Solution:
-    """Solves the sample (``[Z, Y, X]`` or ``[Y, X]`` complex refractive index) on the GPU."""
+          ctx: Context | None = None, eig_fp64=False) -> Solution:
+    """Solves the sample (``[Z, Y, X]`` or ``[Y, X]`` complex refractive index) on the GPU.
+
+    ``eig_fp64``: eigen-solve every slice with the FP64 Householder + QR solver instead of the
+    default FP32 factorisation refined to FP64 residuals."""
     vol = np.ascontiguousarray(sample, dtype=np.complex128)
     if vol.ndim == 2:
         vol = vol[None]
     if vol.ndim != 3:
         raise ValueError("sample must be [Z, Y, X] or [Y, X]")
     ctx = ctx or Context(0)
-    prm = _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz, psf)
+    prm = _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz, psf, eig_fp64)
     h = ctypes.c_void_p()
     Z, Y, X = vol.shape
     _lib.call("scw_solve", ctx.handle, ctypes.c_void_p(vol.ctypes.data), Z, Y, X, ctypes.byref(prm), ctypes.byref(h))

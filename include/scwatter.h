@@ -205,8 +205,13 @@ SCW_API scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int 
  * residuals (clusters of close eigenvalues solved as small FP64 Schur problems).  Refinement stops
  * once max_i ||A x_i - lambda_i x_i|| / (||A||_1 ||x_i||) <= 1e-14; a matrix still above 1e-12
  * after 6 steps is solved by the FP64 QR solver instead (and only then overwritten).  Optional per-matrix
- * outputs: accepted_host (1 = refined result), steps_host (refinement steps), residual_host
- * (last relative residual of the refined result). */
+ * outputs: accepted_host (1 = refined result; else why the FP64 solver took it: 2 FP32 QR not
+ * converged, 3 a cluster above 64 eigenvalues, 4 singular FP32 eigenvector matrix, 5 a cluster's
+ * small Schur solve not converged, 6 residual above 1e-12 after the last step), steps_host
+ * (refinement steps), residual_host (last relative residual of the refined result). */
+/* FP32 counterpart of scw_zgeev (complex64 A, W, V; LAPACK cgeev semantics), the first stage of
+ * scw_zgeev_mixed.  No reference counterpart. */
+SCW_API scw_status scw_cgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* status_host);
 SCW_API scw_status scw_zgeev_mixed(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* accepted_host,
                                    int* steps_host, double* residual_host);
 

@@ -107,6 +107,7 @@ _SIGS = {
     "scw_zgesv": [P, I32, I32, P, P, I32, P],
     "scw_zgeev": [P, I32, P, P, P, I32, P],
     "scw_zgeev_mixed": [P, I32, P, P, P, I32, P, P, P],
+    "scw_cgeev": [P, I32, P, P, P, I32, P],
 }
 
 

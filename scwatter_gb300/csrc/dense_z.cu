@@ -278,6 +278,18 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
     C* y = w + n;
     __shared__ R sh[32];
     __shared__ C s_tau, s_beta;
+    // FP32 (first stage of the mixed solver): a column whose part below the diagonal is under
+    // ulp ||A||_F is set to zero instead of reflected.  That is a backward error of rounding size,
+    // and it keeps a (nearly) diagonal matrix, e.g. the reduced matrix of a homogeneous layer
+    // whose off-diagonal entries are DFT rounding, from being scrambled by reflectors built
+    // from noise.  FP64 keeps zgehd2's behaviour.
+    constexpr bool kDropNegligible = sizeof(R) == sizeof(float);
+    R neg2 = 0;
+    if (kDropNegligible) {
+        R a2 = 0;
+        for (long long i = threadIdx.x; i < (long long)n * n; i += blockDim.x) a2 += cabs2(A[i]);
+        neg2 = block_sum(a2, sh) * CT<C>::ulp * CT<C>::ulp;
+    }
     for (int i = threadIdx.x; i < n * n; i += blockDim.x) Q[i] = CT<C>::mk((i / n) == (i % n) ? 1 : 0, 0);
     __syncthreads();
     for (int k = 0; k + 2 < n; k++) {
@@ -286,6 +298,11 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
         for (int i = k + 2 + threadIdx.x; i < n; i += blockDim.x) xn2 += cabs2(A[(long long)i * n + k]);
         xn2 = block_sum(xn2, sh);
         const C alpha = A[(long long)(k + 1) * n + k];
+        if (kDropNegligible && xn2 + cabs2(alpha) <= neg2) {
+            for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[(long long)i * n + k] = CT<C>::mk(0, 0);
+            __syncthreads();
+            continue;
+        }
         if (threadIdx.x == 0) {
             if (xn2 == 0 && alpha.y == 0) {
                 s_tau = CT<C>::mk(0, 0);
@@ -550,11 +567,17 @@ hqr_kernel(C* __restrict__ H, C* __restrict__ Z, int n, long long sA, C* __restr
 // Eigenvectors of the upper triangular Schur factor T (ztrevc semantics, right vectors):
 // X[:, k] solves (T - T_kk I) x = 0 with x_k = 1, x_i = 0 for i > k.  One warp per vector.
 // X is written row-major (column k = eigenvector k).
+// FP64: a denominator T_ii - T_kk below smin is replaced by smin, as ztrevc does.  FP32 (the
+// first stage of the mixed solver): diagonal entries within 16 ulp of max |T_jj| of each other
+// count as one degenerate eigenvalue and x_i = 0, so each keeps its own Schur vector.  (Dividing
+// rounding noise by rounding noise gives numerically parallel vectors for the exactly degenerate
+// eigenvalues of homogeneous layers; the refinement resolves such clusters in FP64.)
 // ------------------------------------------------------------------------------------
 template <typename C>
 __global__ void __launch_bounds__(256)
 trevc_kernel(const C* __restrict__ T, C* __restrict__ X, int n, long long sA, const int* __restrict__ skip) {
     using R = typename CT<C>::R;
+    constexpr bool kDegenerateSkip = sizeof(R) == sizeof(float);
     if (skipped(skip, blockIdx.y)) return;
     T += sA * blockIdx.y;
     X += sA * blockIdx.y;
@@ -565,6 +588,12 @@ trevc_kernel(const C* __restrict__ T, C* __restrict__ X, int n, long long sA, co
     const R ulp = CT<C>::ulp;
     const C lam = T[(long long)k * n + k];
     const R smin = r_max(ulp * cabs1(lam), CT<C>::safmin * ((R)n / ulp));
+    R deg = 0;
+    if (kDegenerateSkip) {
+        for (int i = lane; i < n; i += 32) deg = r_max(deg, cabs1(T[(long long)i * n + i]));
+        for (int o = 16; o > 0; o >>= 1) deg = r_max(deg, __shfl_xor_sync(0xffffffffu, deg, o));
+        deg *= R(16) * ulp;
+    }
     // x_k = 1, x_{k+1..} = 0
     for (int i = lane; i < n; i += 32) X[(long long)i * n + k] = CT<C>::mk(i == k ? 1 : 0, 0);
     __syncwarp();
@@ -578,8 +607,12 @@ trevc_kernel(const C* __restrict__ T, C* __restrict__ X, int n, long long sA, co
         }
         if (lane == 0) {
             C d = csub(T[(long long)i * n + i], lam);
-            if (cabs1(d) < smin) d = CT<C>::mk(smin, 0);
-            X[(long long)i * n + k] = cdiv(CT<C>::mk(-s.x, -s.y), d);
+            if (kDegenerateSkip && cabs1(d) <= deg) {
+                X[(long long)i * n + k] = CT<C>::mk(0, 0);
+            } else {
+                if (cabs1(d) < smin) d = CT<C>::mk(smin, 0);
+                X[(long long)i * n + k] = cdiv(CT<C>::mk(-s.x, -s.y), d);
+            }
         }
         __syncwarp();
     }
@@ -794,6 +827,36 @@ scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, i
         if (status[b]) bad = 1;
     }
     return bad ? fail(SCW_ERR_NUMERIC, "scw_zgeev: QR iteration did not converge") : SCW_OK;
+}
+
+scw_status scw_cgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* status_host) {
+    if (!ctx || !A || !W || !V || n < 1 || batch < 1) return fail(SCW_ERR_ARG, "scw_cgeev: bad arguments");
+    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    float2* work = nullptr;
+    int* dst = nullptr;
+    const size_t wbytes = sizeof(float2) * ((size_t)n * n + 3 * (size_t)n) * batch;
+    if (cudaMalloc(&work, wbytes) != cudaSuccess || cudaMalloc(&dst, sizeof(int) * batch) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(work);
+        return fail(SCW_ERR_NOMEM, "scw_cgeev: workspace");
+    }
+    scw_status st = scw::geev<float2>(ctx->stream, (float2*)A, (float2*)W, (float2*)V, n, batch, work, dst);
+    ctx->launches += 5;
+    std::vector<int> status(batch, 0);
+    if (st == SCW_OK) {
+        cudaError_t e = cudaMemcpyAsync(status.data(), dst, sizeof(int) * batch, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = fail(SCW_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaFree(work);
+    cudaFree(dst);
+    if (st != SCW_OK) return st;
+    int bad = 0;
+    for (int b = 0; b < batch; b++) {
+        if (status_host) status_host[b] = status[b];
+        if (status[b]) bad = 1;
+    }
+    return bad ? fail(SCW_ERR_NUMERIC, "scw_cgeev: QR iteration did not converge") : SCW_OK;
 }
 
 }  // extern "C"

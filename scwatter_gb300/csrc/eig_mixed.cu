@@ -67,8 +67,16 @@ void eigmix_carve_small(EigMixWs& w, char* base, int n, int Z) {
     w.res = (double*)take(sizeof(double) * Z);
 }
 
-// slice states
-enum : int { kRefining = 0, kConverged = 1, kRejected = 2 };
+// slice states: refining, converged, or the reason it goes to the FP64 solver
+enum : int {
+    kRefining = 0,
+    kConverged = 1,
+    kQrFailed = 2,          // FP32 QR iteration did not converge
+    kClusterTooLarge = 3,   // a cluster above kMaxCluster eigenvalues (or label propagation did not settle)
+    kSingularX = 4,         // zero pivot in the FP32 LU of the eigenvector matrix
+    kClusterFailed = 5,     // the small FP64 Schur solve of a cluster did not converge
+    kNotConverged = 6       // residual above tol_accept after the last step
+};
 
 // ||A||_1 (largest column sum of |a_ij|) per matrix
 __global__ void __launch_bounds__(256) norm1_kernel(const double2* __restrict__ A, int n, double* __restrict__ anorm) {
@@ -112,7 +120,7 @@ __global__ void init_kernel(const float2* __restrict__ lam32, const float2* __re
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        state[b] = qr[b] ? kRejected : kRefining;
+        state[b] = qr[b] ? kQrFailed : kRefining;
         steps[b] = -1;
         res[b] = INFINITY;
     }
@@ -174,7 +182,7 @@ cluster_kernel(const double2* __restrict__ lam, int n, const double* __restrict_
     }
     if (pass == 64) {
         if (threadIdx.x == 0) {
-            state[b] = kRejected;
+            state[b] = kClusterTooLarge;
             ncl[b] = 0;
         }
         return;
@@ -202,7 +210,7 @@ cluster_kernel(const double2* __restrict__ lam, int n, const double* __restrict_
             if (id >= 0) member[nxt[id]++] = i;
         }
         if (reject) {
-            state[b] = kRejected;
+            state[b] = kClusterTooLarge;
             ncl[b] = 0;
         }
     }
@@ -297,7 +305,7 @@ __global__ void to32_kernel(const double2* __restrict__ X, float2* __restrict__ 
 
 __global__ void lu_check_kernel(const int* __restrict__ info, int Z, int* __restrict__ state) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < Z && state[b] == kRefining && info[b] != 0) state[b] = kRejected;
+    if (b < Z && state[b] == kRefining && info[b] != 0) state[b] = kSingularX;
 }
 
 // lambda_i += E_ii for eigenvalues outside every cluster
@@ -497,7 +505,7 @@ cluster_eig_kernel(const float2* __restrict__ E, const int* __restrict__ member,
     }
     __syncthreads();
     if (s_fail) {
-        if (t == 0) state[b] = kRejected;
+        if (t == 0) state[b] = kClusterFailed;
         return;
     }
     // eigenvectors of T: column t, unit diagonal, degenerate pairs uncoupled
@@ -588,9 +596,11 @@ rotate_kernel(double2* __restrict__ X, const int* __restrict__ member, const int
     }
 }
 
-__global__ void final_kernel(const int* __restrict__ state, int* __restrict__ accepted, int Z) {
+__global__ void final_kernel(int* __restrict__ state, int* __restrict__ accepted, int Z) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < Z) accepted[b] = state[b] == kConverged;
+    if (b >= Z) return;
+    if (state[b] == kRefining) state[b] = kNotConverged;
+    accepted[b] = state[b] == kConverged;
 }
 
 static scw_status set_smem(const void* fn, size_t bytes) {
@@ -717,7 +727,7 @@ extern "C" scw_status scw_zgeev_mixed(scw_ctx ctx, int n, void* A, void* W, void
     if (st != SCW_OK) return st;
     int bad = 0;
     for (int b = 0; b < batch; b++) {
-        if (accepted_host) accepted_host[b] = state[b] == 1;
+        if (accepted_host) accepted_host[b] = state[b];
         if (steps_host) steps_host[b] = steps[b];
         if (residual_host) residual_host[b] = res[b];
         if (status[b]) bad = 1;

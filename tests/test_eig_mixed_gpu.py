@@ -53,7 +53,7 @@ def test_random_matrices(ctx):
     A = rng.standard_normal((3, 96, 96)) + 1j * rng.standard_normal((3, 96, 96))
     W, V, acc, steps, res = _mixed(ctx, A)
     _check(A, W, V)
-    assert acc.all() and (res <= 1e-12).all()
+    assert (acc == 1).all() and (res <= 1e-12).all()
 
 
 def test_layer_matrices(ctx):
@@ -71,7 +71,7 @@ def test_layer_matrices(ctx):
     A = lp.PQ.cpu().numpy()
     W, V, acc, steps, res = _mixed(ctx, A)
     _check(A, W, V)
-    assert acc.sum() >= 5                        # the cylinder slice may take the FP64 solver
+    assert (acc == 1).sum() >= 5                 # the cylinder slice may take the FP64 solver
     W64, V64 = plain_eig(ctx, lp.PQ)
     for b in range(A.shape[0]):
         d = np.abs(W[b][:, None] - W64[b].cpu().numpy()[None, :]).min(axis=1)
@@ -80,14 +80,14 @@ def test_layer_matrices(ctx):
 
 def test_fallback_on_defective_matrix(ctx):
     """A Jordan block cannot be refined to a residual basis: that matrix goes through the FP64
-    QR solver (accepted = 0) while its neighbour in the batch is refined."""
+    QR solver (accepted != 1: the reason code) while its neighbour in the batch is refined."""
     rng = np.random.default_rng(3)
     n = 48
     J = np.diag(np.full(n, 0.5 + 0.1j)) + np.diag(np.ones(n - 1), 1)
     G = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
     A = np.stack([J, G])
     W, V, acc, steps, res = _mixed(ctx, A)
-    assert acc[1] == 1 and acc[0] == 0
+    assert acc[1] == 1 and acc[0] in (2, 3, 4, 5, 6)
     _check(A[1:], W[1:], V[1:])
     assert np.abs(W[0] - (0.5 + 0.1j)).max() < 1e-1          # the FP64 QR's (perturbed) eigenvalues
 

@@ -401,6 +401,22 @@ CFG1 = dict(name="spheres[20,64,64] coef20x20, 20 slices (the CPU-runnable spher
 CPU_SOLVE_SLICES = 2       # slices of the config-1 sample the CPU oracle solve is timed on
 
 
+FP64_PEAK_TFLOPS = 1.25   # GB300 FP64 (nominal; our zgemm measures 1.12-1.25 on these GPUs)
+
+
+def fp64_solve_macs(M0, M1, Z, Y, X, checks, pz=True):
+    """Complex multiply-adds of the FP64 GEMM / LU work of one coupled-wave solve, the operation
+    counts of the products the solver issues: per slice the two DFT crops, PQ, W = Q U, the LU
+    inverses of U and W (n^3 / 3 + n^3 each), the cascade (4 products n x n x 3MF), the Ez rows
+    (2 x MF x MF x 2MF) and, per sample, the boundary LU ((6MF)^3 / 3); plus the eigen-solver's
+    FP64 residual products (``checks`` of n^3).  The FP32 eigen stage is not counted."""
+    MF = M0 * M1
+    n = 2 * MF
+    per_slice = (2 * (X * Y * M1 + M0 * M1 * X) + n ** 3 + n ** 3 + 2 * (n ** 3 / 3 + n ** 3)
+                 + 4 * n * n * 3 * MF + (2 * MF * MF * n if pz else 0))
+    return Z * per_slice + (6 * MF) ** 3 / 3 + checks * n ** 3
+
+
 def solve_leg(ctx):
     """GPU FP64 solve of the 20-slice sphere sample (samples/s) beside the CPU oracle solve of
     a 2-slice cut of it (the reference's algorithm: 4MF zgeev per slice, explicit inverses),
@@ -416,6 +432,9 @@ def solve_leg(ctx):
     g = solver.solve(vol, size=c["size"], coef=c["coef"], ctx=ctx, **kw)
     t_gpu = time.perf_counter() - t0
     launches = ctx.launches - launches0
+    eig = g.eig
+    macs = fp64_solve_macs(c["coef"][0], c["coef"][1], c["shape"][0], c["shape"][1], c["shape"][2],
+                           eig["residual_checks"])
     del g
     cut = vol[:CPU_SOLVE_SLICES]
     size_cut = (c["size"][0], c["size"][1], c["size"][2] * CPU_SOLVE_SLICES / c["shape"][0])
@@ -432,7 +451,12 @@ def solve_leg(ctx):
                              "samples_per_s_extrapolated": 1.0 / (cpu_per_slice * c["shape"][0]),
                              "kind": "port", "cores": os.cpu_count(),
                              "sample": f"first {CPU_SOLVE_SLICES} of the 20 slices, scipy LAPACK (OpenBLAS threads)"},
-            "parity": {"x_rel_err_vs_oracle": err, "on": f"the {CPU_SOLVE_SLICES}-slice cut"}}
+            "parity": {"x_rel_err_vs_oracle": err, "on": f"the {CPU_SOLVE_SLICES}-slice cut"},
+            "eigen": eig,
+            "roofline": {"bound": "fp64", "achieved": 8 * macs / t_gpu / 1e12, "peak": FP64_PEAK_TFLOPS,
+                         "unit": "TFLOP/s", "frac": 8 * macs / t_gpu / 1e12 / FP64_PEAK_TFLOPS,
+                         "note": "FP64 GEMM/LU operation count of the solve over its wall time (the FP32 eigen "
+                                 "stage, one CTA per slice, runs beside it uncounted); peak nominal"}}
 
 
 def batch_leg(args):
@@ -459,13 +483,22 @@ def batch_leg(args):
     t = float(np.mean(times))
     pm = sum(b.item_info(i)[3] for i in range(len(items)))
     shapes = [b.item_info(i)[:3] for i in range(len(items))]
+    eigs = [b.item_eig(i) for i in range(len(items))]
+    macs = sum(fp64_solve_macs(M0, M1, Z, it.sample.shape[1], it.sample.shape[2], e["residual_checks"])
+               for (M0, M1, Z), it, e in zip(shapes, items, eigs))
+    eig = {"slices": sum(sh[2] for sh in shapes), "accepted": sum(e["accepted"] for e in eigs),
+           "max_steps": max(e["max_steps"] for e in eigs), "max_residual": max(e["max_residual"] for e in eigs)}
     print(json.dumps({"metric": "samples/s", "value": len(items) / t, "unit": "samples/s", "n_gpus": 1,
                       "steps": len(times), "warmup": 1, "ms_per_step": t * 1e3, "higher_is_better": True,
                       "dtype": "c128 solve, c64 field", "data": "synthetic",
                       "config": {"workload": f"uneven sphere batch, first {len(items)} of 256 seeded samples",
                                  "harmonics_layers": shapes},
                       "points_modes_per_s": pm / t, "graph": info, "create_s": t_create,
-                      "item_status": st.tolist()}))
+                      "item_status": st.tolist(), "eigen": eig,
+                      "roofline": {"bound": "fp64", "achieved": 8 * macs / t / 1e12, "peak": FP64_PEAK_TFLOPS,
+                                   "unit": "TFLOP/s", "frac": 8 * macs / t / 1e12 / FP64_PEAK_TFLOPS,
+                                   "note": "FP64 GEMM/LU operation count of all solves over the launch time; "
+                                           "peak nominal"}}))
 
 
 def warm_leg(args):

@@ -246,9 +246,10 @@ SCW_API scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_sl
 /* No reference counterpart: how the eigen-solves went.  mixed = 1 when the FP32 + refinement
  * path ran; accepted = slices it finished (the others went through the FP64 QR solver);
  * max_steps = most refinement steps an accepted slice needed; max_residual = largest
- * accepted max_i ||A x_i - lambda_i x_i|| / (||A||_1 ||x_i||). */
+ * accepted max_i ||A x_i - lambda_i x_i|| / (||A||_1 ||x_i||); residual_checks = FP64 residual
+ * products (one n x n x n GEMM each) summed over the slices. */
 SCW_API scw_status scw_solution_eig_info(scw_solution s, int* mixed, int* accepted, int* max_steps,
-                                         double* max_residual);
+                                         double* max_residual, int* residual_checks);
 /* gamma: Z x 2MF complex downward roots (the reference's even-slot eigenvalues); x: 6MF
  * complex reflected / transmitted amplitudes (sCWatter.cpp:722); ef: 3MF incident Fourier
  * amplitudes; z_boundaries: Z + 1.  Any pointer may be NULL. */
@@ -287,6 +288,9 @@ SCW_API scw_status scw_batch_get(scw_batch b, int i, double* x, double* gamma, f
 SCW_API scw_status scw_batch_item_info(scw_batch b, int i, int* M0, int* M1, int* n_slices, int64_t* points_modes);
 /* chosen lanes / method, graph nodes, kernels per launch, tuning time and its log
  * (triples lanes, method, ms; n_tune entries). */
+/* The mixed eigen-solver's record of item i after a run, as scw_solution_eig_info. */
+SCW_API scw_status scw_batch_item_eig(scw_batch b, int i, int* mixed, int* accepted, int* max_steps,
+                                      double* max_residual, int* residual_checks);
 SCW_API scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int64_t* graph_nodes, int64_t* kernels,
                                   double* tune_ms, double* tune_log, int* n_tune);
 SCW_API scw_status scw_batch_destroy(scw_batch b);

@@ -66,7 +66,7 @@ _SIGS = {
     "scw_solve": [P, P, I32, I32, I32, P, PP],
     "scw_solution_destroy": [P],
     "scw_solution_info": [P, P, P, P, P],
-    "scw_solution_eig_info": [P, P, P, P, P],
+    "scw_solution_eig_info": [P, P, P, P, P, P],
     "scw_solution_get": [P, P, P, P, P],
     "scw_solution_get_modes": [P, I32, P, P],
     "scw_solution_to_sep": [P, PP],
@@ -76,6 +76,7 @@ _SIGS = {
     "scw_batch_wait": [P, P],
     "scw_batch_get": [P, I32, P, P, P, PP],
     "scw_batch_item_info": [P, I32, P, P, P, P],
+    "scw_batch_item_eig": [P, I32, P, P, P, P, P],
     "scw_batch_info": [P, P, P, P, P, P, P, P],
     "scw_batch_destroy": [P],
     "scw_layer_problem": [P, P, I32, I32, I32, P, P, P, P, P],

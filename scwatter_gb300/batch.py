@@ -86,6 +86,17 @@ class Batch:
                   ctypes.byref(pm))
         return M0.value, M1.value, Z.value, pm.value
 
+    def item_eig(self, i: int) -> dict:
+        """The mixed eigen-solver's record of item ``i`` after a run (as ``Solution.eig``)."""
+        mixed, acc, steps, res, checks = (ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double(),
+                                          ctypes.c_int())
+        _lib.call("scw_batch_item_eig", self.handle, int(i), ctypes.byref(mixed), ctypes.byref(acc),
+                  ctypes.byref(steps), ctypes.byref(res), ctypes.byref(checks))
+        Z = self.item_info(i)[2]
+        return {"mixed": bool(mixed.value), "accepted": acc.value,
+                "fell_back": Z - acc.value if mixed.value else Z, "max_steps": steps.value,
+                "max_residual": res.value, "residual_checks": checks.value}
+
     def result(self, i: int):
         """(x [6MF], gamma [Z, 2MF], field [Nz, Ny, Nx, 3] complex64) of item ``i``."""
         M0, M1, Z, _ = self.item_info(i)

@@ -504,6 +504,28 @@ scw_status scw_batch_item_info(scw_batch b, int i, int* M0, int* M1, int* n_slic
     return SCW_OK;
 }
 
+// The mixed eigen-solver's record of item i (after a run): as scw_solution_eig_info.
+scw_status scw_batch_item_eig(scw_batch b, int i, int* mixed, int* accepted, int* max_steps, double* max_residual,
+                              int* residual_checks) {
+    if (!b || i < 0 || i >= (int)b->items.size()) return fail(SCW_ERR_ARG, "scw_batch_item_eig: item out of range");
+    const Item& it = b->items[i];
+    const int Z = it.sp.Z;
+    std::vector<int> st(2 * Z, 0);
+    std::vector<double> res(Z, 0.0);
+    if (it.out.eig) {
+        SCW_CUDA_TRY(cudaSetDevice(b->ctx->device));
+        SCW_CUDA_TRY(cudaMemcpy(st.data(), it.out.eig, sizeof(int) * 2 * Z, cudaMemcpyDeviceToHost));
+        SCW_CUDA_TRY(cudaMemcpy(res.data(), it.out.eig_res, sizeof(double) * Z, cudaMemcpyDeviceToHost));
+    }
+    const scw::sv::EigSummary e = scw::sv::eig_summary(st.data(), st.data() + Z, res.data(), it.out.eig ? Z : 0);
+    if (mixed) *mixed = it.out.eig ? 1 : 0;
+    if (accepted) *accepted = e.accepted;
+    if (max_steps) *max_steps = e.max_steps;
+    if (max_residual) *max_residual = e.max_res;
+    if (residual_checks) *residual_checks = e.checks;
+    return SCW_OK;
+}
+
 scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int64_t* graph_nodes, int64_t* kernels,
                           double* tune_ms, double* tune_log, int* n_tune) {
     if (!b) return fail(SCW_ERR_ARG, "null batch");

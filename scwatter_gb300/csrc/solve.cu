@@ -574,6 +574,23 @@ void carve_out(const SolvePlan& p, Carver& c, SolveOut& out, bool q64, bool sep)
     out.Qsep = (sep && !p.external) ? c.take<float2>(Z * 2 * 3 * MF * n) : nullptr;
     out.sepKz = (sep && !p.external) ? c.take<double2>(Z * 2 * n) : nullptr;
     out.sepExt = sep ? c.take<double2>(12 * MF) : nullptr;
+    out.eig = p.eig_mixed ? c.take<int>(2 * Z) : nullptr;
+    out.eig_res = p.eig_mixed ? c.take<double>(Z) : nullptr;
+}
+
+EigSummary eig_summary(const int* state, const int* steps, const double* res, int Z) {
+    EigSummary e;
+    for (int b = 0; b < Z; b++) {
+        if (state[b] == 1) {
+            e.accepted++;
+            e.max_steps = std::max(e.max_steps, steps[b]);
+            e.max_res = std::max(e.max_res, res[b]);
+            e.checks += steps[b] + 1;
+        } else {
+            e.checks += mx::EigMixParams{}.steps + 1;
+        }
+    }
+    return e;
 }
 
 scw_status upload_inputs(const SolvePlan& p, const double* sample, const SolveIn& in, cudaStream_t st) {
@@ -625,6 +642,11 @@ scw_status record_solve(const SolvePlan& p, const SolveIn& in, const SolveWs& ws
     SCW_TRY(zgemm(st, n, n, n, kOne, ws.P, n, nn, ws.Q, n, nn, kZero, ws.PQ, n, nn, Zs));
     if (p.eig_mixed) {
         SCW_TRY(mx::geev_mixed(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.mix, ws.P, out.status, mx::EigMixParams{}, &L));
+        if (out.eig) {
+            SCW_CUDA_TRY(cudaMemcpyAsync(out.eig, ws.mix.state, sizeof(int) * Zs, cudaMemcpyDeviceToDevice, st));
+            SCW_CUDA_TRY(cudaMemcpyAsync(out.eig + Zs, ws.mix.steps, sizeof(int) * Zs, cudaMemcpyDeviceToDevice, st));
+            SCW_CUDA_TRY(cudaMemcpyAsync(out.eig_res, ws.mix.res, sizeof(double) * Zs, cudaMemcpyDeviceToDevice, st));
+        }
     } else {
         SCW_TRY(zgeev(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.P, out.status));
         L += 5;
@@ -832,9 +854,9 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
         sol->eig_state.resize(Zs);
         sol->eig_steps.resize(Zs);
         sol->eig_res.resize(Zs);
-        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_state.data(), ws.mix.state, sizeof(int) * Zs, cudaMemcpyDeviceToHost, s));
-        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_steps.data(), ws.mix.steps, sizeof(int) * Zs, cudaMemcpyDeviceToHost, s));
-        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_res.data(), ws.mix.res, sizeof(double) * Zs, cudaMemcpyDeviceToHost, s));
+        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_state.data(), o.eig, sizeof(int) * Zs, cudaMemcpyDeviceToHost, s));
+        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_steps.data(), o.eig + Zs, sizeof(int) * Zs, cudaMemcpyDeviceToHost, s));
+        SCW_CUDA_TRY(cudaMemcpyAsync(sol->eig_res.data(), o.eig_res, sizeof(double) * Zs, cudaMemcpyDeviceToHost, s));
     }
     SCW_CUDA_TRY(cudaStreamSynchronize(s));
     ctx->launches += launches;
@@ -908,21 +930,16 @@ scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_slices, do
     return SCW_OK;
 }
 
-scw_status scw_solution_eig_info(scw_solution s, int* mixed, int* accepted, int* max_steps, double* max_residual) {
+scw_status scw_solution_eig_info(scw_solution s, int* mixed, int* accepted, int* max_steps, double* max_residual,
+                                 int* residual_checks) {
     if (!s) return fail(SCW_ERR_ARG, "null solution");
-    int acc = 0, ms = -1;
-    double mr = 0.0;
-    for (size_t b = 0; b < s->eig_state.size(); b++) {
-        if (s->eig_state[b] == 1) {
-            acc++;
-            ms = std::max(ms, s->eig_steps[b]);
-            mr = std::max(mr, s->eig_res[b]);
-        }
-    }
+    const scw::sv::EigSummary e =
+        scw::sv::eig_summary(s->eig_state.data(), s->eig_steps.data(), s->eig_res.data(), (int)s->eig_state.size());
     if (mixed) *mixed = s->eig_state.empty() ? 0 : 1;
-    if (accepted) *accepted = acc;
-    if (max_steps) *max_steps = ms;
-    if (max_residual) *max_residual = mr;
+    if (accepted) *accepted = e.accepted;
+    if (max_steps) *max_steps = e.max_steps;
+    if (max_residual) *max_residual = e.max_res;
+    if (residual_checks) *residual_checks = e.checks;
     return SCW_OK;
 }
 

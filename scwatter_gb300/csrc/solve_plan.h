@@ -73,7 +73,17 @@ struct SolveOut {                           // results
     float2* Qsep;                           // [Z][2][3][MF][2MF] complex64 (separable layout), or null
     double2* sepKz;                         // [Z][2][2MF] kz = +-gamma k for the separable set, or null
     double2* sepExt;                        // [12 MF] exterior blocks of the separable set, or null
+    int* eig;                               // mixed eigen-solver per slice: [0, Z) state, [Z, 2Z) steps, or null
+    double* eig_res;                        // [Z] last relative residual, or null
 };
+
+// Summary of the mixed eigen-solver's per-slice record (state 1 = accepted): accepted slices,
+// most steps, largest accepted residual, FP64 residual GEMMs issued.
+struct EigSummary {
+    int accepted = 0, max_steps = -1, checks = 0;
+    double max_res = 0.0;
+};
+EigSummary eig_summary(const int* state, const int* steps, const double* res, int Z);
 
 scw_status plan_solve(const scw_solve_params* prm, int Z, int Y, int X, SolvePlan& p);
 void carve_in(const SolvePlan& p, Carver& c, SolveIn& in);

@@ -86,12 +86,15 @@ class Solution:
         self.z = np.zeros(self.Z + 1)
         _lib.call("scw_solution_get", handle, *(ctypes.c_void_p(a.ctypes.data) for a in
                                                 (self.gamma, self.x, self.EF, self.z)))
-        mixed, acc, steps, res = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        mixed, acc, steps, res, checks = (ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double(),
+                                          ctypes.c_int())
         _lib.call("scw_solution_eig_info", handle, ctypes.byref(mixed), ctypes.byref(acc), ctypes.byref(steps),
-                  ctypes.byref(res))
-        # eigen-solver record: mixed path on / slices it finished / most steps / largest residual
+                  ctypes.byref(res), ctypes.byref(checks))
+        # eigen-solver record: mixed path on / slices it finished / most steps / largest residual /
+        # FP64 residual GEMMs issued
         self.eig = {"mixed": bool(mixed.value), "accepted": acc.value, "fell_back": self.Z - acc.value if mixed.value
-                    else self.Z, "max_steps": steps.value, "max_residual": res.value}
+                    else self.Z, "max_steps": steps.value, "max_residual": res.value,
+                    "residual_checks": checks.value}
 
     def modes(self, l: int):
         """(Q_check, Q_hat) of slice ``l``: [3MF, 2MF] complex128 each."""

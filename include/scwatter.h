@@ -174,6 +174,13 @@ SCW_API scw_status scw_sep_set_slice_device(scw_sep s, int l, const double* kz_d
 /* factors a .cw written by the volume solver; SCW_ERR_UNSUPPORTED if its waves do not have
  * the separable structure (use the plain evaluator then). */
 SCW_API scw_status scw_sep_from_cw(scw_ctx ctx, scw_cw cw, scw_sep* out);
+/* Compact factored coefficient file (.cwf; no reference counterpart): the separable set as it is
+ * -- "SCWSEP01", int32 M0, M1, Z, J, region rule, 0; float64 kx[M0], ky[M1], z[Z+1];
+ * complex128 exterior[12 MF], kz[Z][2][Jp]; complex64 Q[Z][2][3][MF][Jp] (Jp = J rounded up to
+ * even), little-endian -- streamed one slice at a time.  Load checks the magic and that the
+ * file size matches the header (SCW_ERR_FORMAT otherwise). */
+SCW_API scw_status scw_sep_save(scw_sep s, const char* path);
+SCW_API scw_status scw_sep_load(scw_ctx ctx, const char* path, scw_sep* out);
 SCW_API scw_status scw_sep_info(scw_sep s, int* M0, int* M1, int* n_slices, int* modes_per_half);
 SCW_API scw_status scw_sep_set_region_rule(scw_sep s, int rule);
 SCW_API scw_status scw_sep_eval_volume_device(scw_sep s, float x_start, float y_start, float z_start,
@@ -260,6 +267,10 @@ SCW_API scw_status scw_solution_get_modes(scw_solution s, int l, double* Q_check
 SCW_API scw_status scw_solution_to_sep(scw_solution s, scw_sep* out);
 /* The .cw structure that sCWatter writes (sCWatter.cpp:890-956). */
 SCW_API scw_status scw_solution_to_cw(scw_solution s, scw_cw* out);
+/* The same structure written straight to a .cw file (CoupledWaveStructure.h:72-100 layout),
+ * layer by layer: host memory stays at one slice's mode amplitudes.  Byte-identical to
+ * scw_solution_to_cw + scw_cw_save. */
+SCW_API scw_status scw_solution_write_cw(scw_solution s, const char* path);
 
 /* ---------------------------------------------------------------------------------- */
 /* Batched solve + evaluate (no counterpart in the reference, which solves one sample   */

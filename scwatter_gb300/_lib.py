@@ -71,6 +71,9 @@ _SIGS = {
     "scw_solution_get_modes": [P, I32, P, P],
     "scw_solution_to_sep": [P, PP],
     "scw_solution_to_cw": [P, PP],
+    "scw_solution_write_cw": [P, ctypes.c_char_p],
+    "scw_sep_save": [P, ctypes.c_char_p],
+    "scw_sep_load": [P, ctypes.c_char_p, P],
     "scw_batch_create": [P, P, I32, I32, I32, PP],
     "scw_batch_run": [P],
     "scw_batch_wait": [P, P],

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -1025,11 +1026,74 @@ scw_status scw_solution_to_sep(scw_solution s, scw_sep* out) {
 // The .cw structure written by sCWatter (sCWatter.cpp:890-956): per harmonic p the incident
 // wave, the reflected wave (wound to z_0), the transmitted wave (wound to z_Z) and, unless
 // external, the 2MF downward / upward modes of each slice wound to their boundary.
+extern "C++" {
+// One .cw record (tira::planewave<double>: E0 xyz, k xyz as re/im pairs) of a wave wound to z = 0
+// from its reference plane zw: E0 exp(-i kz zw) (wind(0, 0, -z), sCWatter.cpp:469-482).
+static void cw_record(double* v, cd ex, cd ey, cd ez, cd kx, cd ky, cd kz, double zw) {
+    const cd f = std::exp(cd(0, -1) * kz * zw);
+    const cd E[3] = {ex * f, ey * f, ez * f};
+    const cd K[3] = {kx, ky, kz};
+    for (int c = 0; c < 3; c++) {
+        v[2 * c] = E[c].real();
+        v[2 * c + 1] = E[c].imag();
+    }
+    for (int c = 0; c < 3; c++) {
+        v[6 + 2 * c] = K[c].real();
+        v[6 + 2 * c + 1] = K[c].imag();
+    }
+}
+
+// The waves of one .cw layer in the order sCWatter writes them (sCWatter.cpp:890-956): harmonic
+// p outer; per p either the one exterior wave or the 2MF modes of the adjacent slice half.
+// Qup / Qdn: [3MF][2MF] amplitudes of slice l-1's upward / slice l's downward half (host), or
+// null where the layer has none.  emit(record) is called once per wave.
+template <typename Emit>
+static void cw_layer_waves(const scw_solution_s* s, int l, bool reflected, const cd* Qup, const cd* Qdn, Emit&& emit) {
+    const int MF = s->MF, n = 2 * MF, ZL = s->Z + 1;
+    const double k = s->k;
+    double r[12];
+    for (int p = 0; p < MF; p++) {
+        const cd kx = s->Sx[p] * k, ky = s->Sy[p] * k;
+        if (reflected) {                       // Pr
+            if (l == 0) {
+                cw_record(r, s->x[p], s->x[MF + p], s->x[2 * MF + p], kx, ky, -s->Sz0[p] * k * s->n0, s->zb[0]);
+                emit(r);
+            } else if (Qup) {
+                const cd* gam = s->gam.data() + (size_t)(l - 1) * n;
+                for (int j = 0; j < n; j++) {
+                    cw_record(r, Qup[(size_t)p * n + j], Qup[(size_t)(MF + p) * n + j], Qup[(size_t)(2 * MF + p) * n + j],
+                              kx, ky, -1.0 * gam[j] * k, s->zb[l]);
+                    emit(r);
+                }
+            }
+        } else {                               // Pt
+            if (l == ZL - 1) {
+                cw_record(r, s->x[3 * MF + p], s->x[4 * MF + p], s->x[5 * MF + p], kx, ky, s->Sz1[p] * k * s->n1,
+                          s->zb[l]);
+                emit(r);
+            } else if (Qdn) {
+                const cd* gam = s->gam.data() + (size_t)l * n;
+                for (int j = 0; j < n; j++) {
+                    cw_record(r, Qdn[(size_t)p * n + j], Qdn[(size_t)(MF + p) * n + j], Qdn[(size_t)(2 * MF + p) * n + j],
+                              kx, ky, 1.0 * gam[j] * k, s->zb[l]);
+                    emit(r);
+                }
+            }
+        }
+    }
+}
+
+static double cw_layer_z(const scw_solution_s* s, int l) {
+    const int ZL = s->Z + 1;
+    return (l == 0 || l == ZL - 1 || !s->external) ? s->zb[l] : 0.0;
+}
+
+}  // extern "C++"
+
 scw_status scw_solution_to_cw(scw_solution s, scw_cw* out) {
     if (!s || !out) return fail(SCW_ERR_ARG, "null argument");
     *out = nullptr;
     const int MF = s->MF, n = 2 * MF, Z = s->Z, ZL = Z + 1;
-    const double k = s->k;
     const size_t blk = (size_t)3 * MF * n;
     std::vector<cd> Qh;
     try {
@@ -1044,55 +1108,91 @@ scw_status scw_solution_to_cw(scw_solution s, scw_cw* out) {
     std::unique_ptr<scw_cw_s> cw(new (std::nothrow) scw_cw_s());
     if (!cw) return fail(SCW_ERR_NOMEM, "host allocation");
     try {
-        cw->layers.resize(ZL);
-        for (int l = 0; l < ZL; l++) cw->layers[l].z = 0.0;
-        auto rec = [](std::vector<double>& v, cd ex, cd ey, cd ez, cd kx, cd ky, cd kz, double zw) {
-            const cd f = std::exp(cd(0, -1) * kz * zw);     // wind(0, 0, -z): E0 exp(-i kz z)
-            const cd E[3] = {ex * f, ey * f, ez * f};
-            const cd K[3] = {kx, ky, kz};
-            for (int c = 0; c < 3; c++) {
-                v.push_back(E[c].real());
-                v.push_back(E[c].imag());
-            }
-            for (int c = 0; c < 3; c++) {
-                v.push_back(K[c].real());
-                v.push_back(K[c].imag());
-            }
-        };
-        auto modes = [&](std::vector<double>& v, const cd* Q, int p, cd kx, cd ky, const cd* gam, double sgn, double zw) {
-            for (int j = 0; j < n; j++)
-                rec(v, Q[(size_t)p * n + j], Q[(size_t)(MF + p) * n + j], Q[(size_t)(2 * MF + p) * n + j], kx, ky,
-                    sgn * gam[j] * k, zw);
-        };
+        double r[12];
         for (int p = 0; p < MF; p++) {
-            const cd kx = s->Sx[p] * k, ky = s->Sy[p] * k;
-            rec(cw->Pi, s->EF[p], s->EF[MF + p], s->EF[2 * MF + p], kx, ky, s->Sz0[p] * k, 0.0);
-            for (int l = 0; l < ZL; l++) {
-                auto& L = cw->layers[l];
-                if (l == 0) {
-                    L.z = s->zb[0];
-                    rec(L.Pr, s->x[p], s->x[MF + p], s->x[2 * MF + p], kx, ky, -s->Sz0[p] * k * s->n0, s->zb[0]);
-                    if (!s->external) modes(L.Pt, Qh.data(), p, kx, ky, s->gam.data(), 1.0, s->zb[0]);
-                } else if (l == ZL - 1) {
-                    L.z = s->zb[l];
-                    rec(L.Pt, s->x[3 * MF + p], s->x[4 * MF + p], s->x[5 * MF + p], kx, ky, s->Sz1[p] * k * s->n1,
-                        s->zb[l]);
-                    if (!s->external)
-                        modes(L.Pr, Qh.data() + ((size_t)(l - 1) * 2 + 1) * blk, p, kx, ky,
-                              s->gam.data() + (size_t)(l - 1) * n, -1.0, s->zb[l]);
-                } else if (!s->external) {
-                    L.z = s->zb[l];
-                    modes(L.Pr, Qh.data() + ((size_t)(l - 1) * 2 + 1) * blk, p, kx, ky,
-                          s->gam.data() + (size_t)(l - 1) * n, -1.0, s->zb[l]);
-                    modes(L.Pt, Qh.data() + (size_t)l * 2 * blk, p, kx, ky, s->gam.data() + (size_t)l * n, 1.0,
-                          s->zb[l]);
-                }
-            }
+            cw_record(r, s->EF[p], s->EF[MF + p], s->EF[2 * MF + p], s->Sx[p] * s->k, s->Sy[p] * s->k, s->Sz0[p] * s->k,
+                      0.0);
+            cw->Pi.insert(cw->Pi.end(), r, r + 12);
+        }
+        cw->layers.resize(ZL);
+        for (int l = 0; l < ZL; l++) {
+            auto& L = cw->layers[l];
+            L.z = cw_layer_z(s, l);
+            const cd* Qup = (!s->external && l > 0) ? Qh.data() + ((size_t)(l - 1) * 2 + 1) * blk : nullptr;
+            const cd* Qdn = (!s->external && l < ZL - 1) ? Qh.data() + (size_t)l * 2 * blk : nullptr;
+            cw_layer_waves(s, l, true, Qup, Qdn, [&](const double* w) { L.Pr.insert(L.Pr.end(), w, w + 12); });
+            cw_layer_waves(s, l, false, Qup, Qdn, [&](const double* w) { L.Pt.insert(L.Pt.end(), w, w + 12); });
         }
     } catch (const std::bad_alloc&) {
         return fail(SCW_ERR_NOMEM, "host allocation of the wave lists");
     }
     *out = cw.release();
+    return SCW_OK;
+}
+
+// Streaming writer of the same .cw file (CoupledWaveStructure.h:72-100 layout): one layer's
+// two slice halves on the host at a time, records written in chunks, so host memory stays
+// O(slice) whatever the file size (about 63 GB at config 2).
+scw_status scw_solution_write_cw(scw_solution s, const char* path) {
+    if (!s || !path) return fail(SCW_ERR_ARG, "null argument");
+    const int MF = s->MF, n = 2 * MF, Z = s->Z, ZL = Z + 1;
+    const size_t blk = (size_t)3 * MF * n;
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(SCW_ERR_IO, std::string("cannot create ") + path);
+    std::unique_ptr<FILE, int (*)(FILE*)> guard(f, fclose);
+    std::vector<cd> Qup, Qdn;
+    std::vector<double> chunk;
+    try {
+        if (!s->external) {
+            Qup.resize(blk);
+            Qdn.resize(blk);
+        }
+        chunk.reserve(12 * 65536);
+    } catch (const std::bad_alloc&) {
+        return fail(SCW_ERR_NOMEM, "host allocation of one slice");
+    }
+    bool ok = true;
+    auto put = [&](const void* p, size_t bytes) { ok = ok && fwrite(p, 1, bytes, f) == bytes; };
+    auto flush = [&]() {
+        put(chunk.data(), chunk.size() * sizeof(double));
+        chunk.clear();
+    };
+    auto emit = [&](const double* w) {
+        chunk.insert(chunk.end(), w, w + 12);
+        if (chunk.size() >= 12 * 65536) flush();
+    };
+    const uint64_t sz = 8, nPi = (uint64_t)MF, nL = (uint64_t)ZL;
+    put(&sz, 8);
+    put(&nPi, 8);
+    double r[12];
+    for (int p = 0; p < MF; p++) {
+        cw_record(r, s->EF[p], s->EF[MF + p], s->EF[2 * MF + p], s->Sx[p] * s->k, s->Sy[p] * s->k, s->Sz0[p] * s->k,
+                  0.0);
+        emit(r);
+    }
+    flush();
+    put(&nL, 8);
+    if (!s->external) SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    for (int l = 0; l < ZL && ok; l++) {
+        const bool up = !s->external && l > 0, dn = !s->external && l < ZL - 1;
+        if (up)
+            SCW_CUDA_TRY(cudaMemcpy(Qup.data(), s->dQ + ((size_t)(l - 1) * 2 + 1) * blk, sizeof(double2) * blk,
+                                    cudaMemcpyDeviceToHost));
+        if (dn)
+            SCW_CUDA_TRY(cudaMemcpy(Qdn.data(), s->dQ + (size_t)l * 2 * blk, sizeof(double2) * blk,
+                                    cudaMemcpyDeviceToHost));
+        const double z = cw_layer_z(s, l);
+        put(&z, 8);
+        for (int half = 0; half < 2; half++) {
+            const bool refl = half == 0;
+            const uint64_t cnt = refl ? (l == 0 ? (uint64_t)MF : (up ? (uint64_t)MF * n : 0))
+                                      : (l == ZL - 1 ? (uint64_t)MF : (dn ? (uint64_t)MF * n : 0));
+            put(&cnt, 8);
+            cw_layer_waves(s, l, refl, up ? Qup.data() : nullptr, dn ? Qdn.data() : nullptr, emit);
+            flush();
+        }
+    }
+    if (!ok || fflush(f) != 0) return fail(SCW_ERR_IO, std::string("write failed: ") + path);
     return SCW_OK;
 }
 

@@ -35,6 +35,10 @@ def parser() -> argparse.ArgumentParser:
     p.add_argument("--log", action="store_true", help="print stage timings")
     p.add_argument("--npz", action="store_true", help="skip Ez of the modes (Px and Py only)")
     p.add_argument("--device", type=int, default=0, help="CUDA device")
+    p.add_argument("--factored", default=None,
+                   help="also write the compact factored coefficient file (.cwf) the evaluator reads directly")
+    p.add_argument("--eig-fp64", action="store_true",
+                   help="FP64 Householder + QR eigen-solver for every slice (default: FP32 + FP64 refinement)")
     return p
 
 
@@ -49,9 +53,12 @@ def main(argv=None) -> int:
     t0 = time.perf_counter()
     ctx = ev.Context(a.device)
     sol = solver.solve(sample, lam=a.lam, direction=a.direction, ex=a.ex, ey=a.ey, ez=a.ez, n=a.n, kappa=a.kappa,
-                       size=a.size, z=a.z, coef=a.coef, external=a.external, pz=not a.npz, psf=a.psf, ctx=ctx)
+                       size=a.size, z=a.z, coef=a.coef, external=a.external, pz=not a.npz, psf=a.psf, ctx=ctx,
+                       eig_fp64=a.eig_fp64)
     t1 = time.perf_counter()
     sol.save(a.output)
+    if a.factored:
+        sol.to_sep().save(a.factored)
     t2 = time.perf_counter()
     vol = np.asarray(sample)
     Y, X = vol.shape[-2], vol.shape[-1]

@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import os
 import sys
 import time
 
@@ -30,7 +31,8 @@ MODES = {"x": 0, "y": 1, "z": 2, "intensity": 3}
 
 def parser() -> argparse.ArgumentParser:
     p = argparse.ArgumentParser(prog="scwatterview", description="headless field evaluation of a .cw structure")
-    p.add_argument("input", nargs="?", default="c.cw", help="coupled wave structure (.cw)")
+    p.add_argument("input", nargs="?", default="c.cw",
+                   help="coupled wave structure (.cw) or compact factored coefficient file (.cwf)")
     p.add_argument("--cuda", "-c", type=int, default=0, help="CUDA device number")
     p.add_argument("--nogui", action="store_true", help="save an output file without loading the GUI")
     p.add_argument("--verbose", "-v", action="store_true")
@@ -62,8 +64,12 @@ def main(argv=None) -> int:
     from .cw import CoupledWaveStructure
 
     t0 = time.perf_counter()
+    factored = str(a.input).endswith(".cwf")
+    if factored and a.method == "plain":
+        print("a factored coefficient file (.cwf) is evaluated by the GEMM-form methods only", file=sys.stderr)
+        return 2
     S = CoupledWaveStructure()
-    if not S.load(a.input):
+    if not os.path.exists(a.input) or (not factored and not S.load(a.input)):
         print(f"ERROR: file {a.input} not found", file=sys.stderr)
         return 1
     N = 2 ** a.resolution
@@ -79,7 +85,7 @@ def main(argv=None) -> int:
         E_xy, E_xz, E_yz = obj.evaluate_planes_host(xs, ys, zs, plane[0], plane[1], plane[2], d, N)
     else:
         m = {"tf32x3": sp.TF32X3, "bf16x3": sp.BF16X3, "fp32": sp.FP32}[a.method]
-        obj = sp.SeparableSet.from_cw(ctx, S)
+        obj = sp.SeparableSet.load(ctx, a.input) if factored else sp.SeparableSet.from_cw(ctx, S)
         E_xy, E_xz, E_yz = obj.evaluate_planes_host(xs, ys, zs, plane[0], plane[1], plane[2], d, N, method=m)
     t1 = time.perf_counter()
     sel = {0: E_yz, 1: E_xz, 2: E_xy}[a.axis]

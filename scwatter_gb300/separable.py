@@ -67,6 +67,18 @@ class SeparableSet:
             _lib.load().scw_cw_destroy(native)
         return cls(ctx, h)
 
+    @classmethod
+    def load(cls, ctx: Context, filename: str) -> "SeparableSet":
+        """Reads a compact factored coefficient file (.cwf) written by :meth:`save`."""
+        h = ctypes.c_void_p()
+        _lib.call("scw_sep_load", ctx.handle, str(filename).encode(), ctypes.byref(h))
+        return cls(ctx, h)
+
+    def save(self, filename: str) -> None:
+        """Writes the set as a compact factored coefficient file (.cwf): per slice Q_check /
+        Q_hat in complex64 and the modes' kz, plus the exterior blocks and k grids."""
+        _lib.call("scw_sep_save", self.handle, str(filename).encode())
+
     def info(self):
         v = [ctypes.c_int() for _ in range(4)]
         _lib.call("scw_sep_info", self.handle, *[ctypes.byref(x) for x in v])

@@ -113,13 +113,8 @@ class Solution:
             _lib.load().scw_cw_destroy(h)
 
     def save(self, filename: str) -> None:
-        """Writes the .cw file sCWatter would write (sCWatter.cpp:956)."""
-        h = ctypes.c_void_p()
-        _lib.call("scw_solution_to_cw", self.handle, ctypes.byref(h))
-        try:
-            _lib.call("scw_cw_save", h, str(filename).encode())
-        finally:
-            _lib.load().scw_cw_destroy(h)
+        """Writes the .cw file sCWatter would write (sCWatter.cpp:956), streamed layer by layer."""
+        _lib.call("scw_solution_write_cw", self.handle, str(filename).encode())
 
     def to_sep(self) -> SeparableSet:
         h = ctypes.c_void_p()

@@ -243,9 +243,27 @@ typedef struct scw_solve_params {
                            * does not converge; 1: FP64 Householder + QR for every slice */
 } scw_solve_params;
 
-/* sample: [Z][Y][X] complex128 refractive index in HOST memory (the .npy volume).  Runs the
+/* sample: [Z][Y][X] complex128 refractive index in host or device memory (the .npy volume;
+ * unified addressing tells them apart).  Runs the
  * whole solve on the context's device and blocks until it is done.  SCW_ERR_NUMERIC when an
  * eigen-solve does not converge or a mode / boundary matrix is singular. */
+/* Sample volumes on the device (no reference counterpart; the reference reads the .npy on the
+ * host, FourierWave.h:269, and generates samples with tilesample.py).  out: [Z][Y][X]
+ * complex128 device buffer.
+ * scw_gen_spheres: background index, then each sphere (spheres[4 s ..]: cz, cy, cx, r in voxel
+ * units) overwrites the voxels with (z-cz)^2 + (y-cy)^2 + (x-cx)^2 <= r^2, in order.
+ * scw_gen_grf: Gaussian random field -- counter-based normal noise (splitmix64 of seed and index,
+ * Box-Muller), periodic separable Gaussian filter exp(-t^2 / (2 corr^2)) truncated at 4 corr,
+ * min-max normalised to t in [0, 1]; n = n_lo + (n_hi - n_lo) t + i kappa t with kappa drawn from
+ * the seed in [0, kappa_max].
+ * scw_npy_read: dims[3] = Z, Y, X of a 2-D or 3-D '<c16' / '<f8' .npy; with out != NULL the
+ * volume is streamed into out (ctx needed then). */
+SCW_API scw_status scw_gen_spheres(scw_ctx ctx, int Z, int Y, int X, int n_spheres, const double* spheres,
+                                   const double* n_background, const double* n_sphere, void* out);
+SCW_API scw_status scw_gen_grf(scw_ctx ctx, int Z, int Y, int X, double corr_px, double n_lo, double n_hi,
+                               double kappa_max, uint64_t seed, void* out);
+SCW_API scw_status scw_npy_read(scw_ctx ctx, const char* path, int* dims, void* out);
+
 SCW_API scw_status scw_solve(scw_ctx ctx, const double* sample, int Z, int Y, int X, const scw_solve_params* prm,
                              scw_solution* out);
 SCW_API scw_status scw_solution_destroy(scw_solution s);

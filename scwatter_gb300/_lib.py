@@ -63,6 +63,10 @@ _SIGS = {
     "scw_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P],
     "scw_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P],
     "scw_eval_plane_device_static": [P, I32, F32, F32, F32, F32, I32, P],
+    "scw_gen_spheres": [P, I32, I32, I32, I32, P, P, P, P],
+    "scw_gen_grf": [P, I32, I32, I32, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                    ctypes.c_uint64, P],
+    "scw_npy_read": [P, ctypes.c_char_p, P, P],
     "scw_solve": [P, P, I32, I32, I32, P, PP],
     "scw_solution_destroy": [P],
     "scw_solution_info": [P, P, P, P, P],

@@ -600,7 +600,8 @@ scw_status upload_inputs(const SolvePlan& p, const double* sample, const SolveIn
         return SCW_OK;
     };
     const size_t MF = p.MF;
-    SCW_TRY(up(in.data, sample, sizeof(double2) * p.Z * p.Y * p.X));
+    // the sample may be in host or device memory
+    SCW_CUDA_TRY(cudaMemcpyAsync(in.data, sample, sizeof(double2) * p.Z * p.Y * p.X, cudaMemcpyDefault, st));
     SCW_TRY(up(in.tw1, p.tw1.data(), sizeof(double2) * p.tw1.size()));
     SCW_TRY(up(in.tw2, p.tw2.data(), sizeof(double2) * p.tw2.size()));
     SCW_TRY(up(in.Sz0, p.Sz0.data(), sizeof(double2) * MF));

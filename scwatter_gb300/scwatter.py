@@ -49,9 +49,13 @@ def main(argv=None) -> int:
     if len(a.n) != 2:
         print("the volume solver takes exactly two media: --n n_upper n_lower", file=sys.stderr)
         return 2
-    sample = np.load(a.sample)
+    from . import _lib, samples
     t0 = time.perf_counter()
     ctx = ev.Context(a.device)
+    try:                                      # streamed from the file into device memory
+        sample = samples.npy_to_device(ctx, a.sample)
+    except _lib.ScwError:
+        sample = np.load(a.sample)
     sol = solver.solve(sample, lam=a.lam, direction=a.direction, ex=a.ex, ey=a.ey, ez=a.ez, n=a.n, kappa=a.kappa,
                        size=a.size, z=a.z, coef=a.coef, external=a.external, pz=not a.npz, psf=a.psf, ctx=ctx,
                        eig_fp64=a.eig_fp64)
@@ -60,8 +64,7 @@ def main(argv=None) -> int:
     if a.factored:
         sol.to_sep().save(a.factored)
     t2 = time.perf_counter()
-    vol = np.asarray(sample)
-    Y, X = vol.shape[-2], vol.shape[-1]
+    Y, X = sample.shape[-2], sample.shape[-1]
     print(f"Field saved in {a.output}.")
     print(f"Number of pixels (x, y): [{X},{Y}]")
     print(f"Number of sublayers: {sol.Z}")

@@ -137,17 +137,30 @@ def solve(sample, lam=1.0, direction=(0.0, 0.0, 1.0), ex=(0.0, 0.0), ey=(1.0, 0.
           kappa=0.0, size=(10.0, 10.0, 2.0), z=0.0, coef=None, external=False, pz=True, psf=False,
           ctx: Context | None = None, eig_fp64=False) -> Solution:
     """Solves the sample (``[Z, Y, X]`` or ``[Y, X]`` complex refractive index) on the GPU.
+    The sample is a numpy array or a complex128 CUDA tensor (then it never leaves the device).
 
     ``eig_fp64``: eigen-solve every slice with the FP64 Householder + QR solver instead of the
     default FP32 factorisation refined to FP64 residuals."""
-    vol = np.ascontiguousarray(sample, dtype=np.complex128)
-    if vol.ndim == 2:
-        vol = vol[None]
-    if vol.ndim != 3:
-        raise ValueError("sample must be [Z, Y, X] or [Y, X]")
     ctx = ctx or Context(0)
     prm = _params(lam, direction, ex, ey, ez, n, kappa, size, z, coef, external, pz, psf, eig_fp64)
     h = ctypes.c_void_p()
-    Z, Y, X = vol.shape
-    _lib.call("scw_solve", ctx.handle, ctypes.c_void_p(vol.ctypes.data), Z, Y, X, ctypes.byref(prm), ctypes.byref(h))
+    if hasattr(sample, "data_ptr") and getattr(sample, "is_cuda", False):
+        import torch
+        vol = sample.contiguous()
+        if vol.dtype != torch.complex128:
+            raise ValueError("a device sample must be complex128")
+        if vol.dim() == 2:
+            vol = vol[None]
+        Z, Y, X = vol.shape
+        torch.cuda.synchronize()
+        ptr = ctypes.c_void_p(vol.data_ptr())
+    else:
+        vol = np.ascontiguousarray(sample, dtype=np.complex128)
+        if vol.ndim == 2:
+            vol = vol[None]
+        if vol.ndim != 3:
+            raise ValueError("sample must be [Z, Y, X] or [Y, X]")
+        Z, Y, X = vol.shape
+        ptr = ctypes.c_void_p(vol.ctypes.data)
+    _lib.call("scw_solve", ctx.handle, ptr, Z, Y, X, ctypes.byref(prm), ctypes.byref(h))
     return Solution(ctx, h)

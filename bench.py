@@ -561,6 +561,44 @@ def warm_leg(args):
                                    "plain_solves_for_data_s": t_train_data}}))
 
 
+def probe(kind):
+    """Small single-shot cases for ncu captures (one pass of the kernels named, nothing timed):
+    ``eig-mixed``: the mixed eigen-solver on the first 2 slices of the sphere sample (n = 800);
+    ``zgemm``: 4 batched 800 x 800 x 800 complex128 products."""
+    import ctypes
+    import torch
+    from scwatter_gb300 import _lib, samples
+    from scwatter_gb300 import evaluator as ev
+    ctx = ev.Context(0)
+    if kind == "eig-mixed":
+        from scwatter_gb300.warmstart import layer_problems
+        c = CFG1
+        vol = samples.spheres(c["shape"], seed=0)[:2]
+        lp = layer_problems(ctx, vol, lam=1.0, size=(c["size"][0], c["size"][1], 2.0), coef=c["coef"])
+        A = lp.PQ.clone()
+        Z, n, _ = A.shape
+        W = torch.zeros((Z, n), dtype=torch.complex128, device="cuda")
+        V = torch.zeros((Z, n, n), dtype=torch.complex128, device="cuda")
+        acc = np.zeros(Z, np.int32)
+        torch.cuda.synchronize()
+        _lib.call("scw_zgeev_mixed", ctx.handle, n, ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(W.data_ptr()),
+                  ctypes.c_void_p(V.data_ptr()), Z, ctypes.c_void_p(acc.ctypes.data), None, None)
+        print(json.dumps({"probe": kind, "n": n, "matrices": Z, "accepted": acc.tolist()}))
+    elif kind == "zgemm":
+        n, B = 800, 4
+        g = torch.Generator(device="cuda").manual_seed(0)
+        A = torch.randn(B, n, n, dtype=torch.complex128, device="cuda", generator=g)
+        Bm = torch.randn(B, n, n, dtype=torch.complex128, device="cuda", generator=g)
+        C = torch.zeros(B, n, n, dtype=torch.complex128, device="cuda")
+        al = (ctypes.c_double * 2)(1.0, 0.0)
+        be = (ctypes.c_double * 2)(0.0, 0.0)
+        torch.cuda.synchronize()
+        _lib.call("scw_zgemm", ctx.handle, n, n, n, al, ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(Bm.data_ptr()),
+                  be, ctypes.c_void_p(C.data_ptr()), B)
+        torch.cuda.synchronize()
+        print(json.dumps({"probe": kind, "n": n, "batch": B}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -579,8 +617,12 @@ def main():
     ap.add_argument("--warm-train", type=int, default=16)
     ap.add_argument("--warm-coef", type=int, default=24)
     ap.add_argument("--warm-epochs", type=int, default=200)
+    ap.add_argument("--probe", choices=["eig-mixed", "zgemm"], default=None,
+                    help="run one small case for an ncu capture and exit")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.probe:
+        probe(args.probe)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.solve_only:
         from scwatter_gb300 import evaluator as ev

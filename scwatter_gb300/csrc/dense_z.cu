@@ -101,8 +101,8 @@ lu_panel_kernel(C* __restrict__ A, int n, int lda, long long sA, int k0, int nb,
     using R = typename CT<C>::R;
     A += sA * blockIdx.x;
     piv += sP * blockIdx.x;
-    __shared__ R red_v[512];
-    __shared__ int red_i[512];
+    __shared__ R red_v[16];
+    __shared__ int red_i[16];
     __shared__ C pivrow[kNB];
     for (int k = k0; k < k0 + nb; k++) {
         // pivot search over rows k..n-1 of column k
@@ -115,22 +115,29 @@ lu_panel_kernel(C* __restrict__ A, int n, int lda, long long sA, int k0, int nb,
                 bi = i;
             }
         }
-        red_v[threadIdx.x] = best;
-        red_i[threadIdx.x] = bi;
-        __syncthreads();
-        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-            if (threadIdx.x < s) {
-                const R o = red_v[threadIdx.x + s];
-                const int oi = red_i[threadIdx.x + s];
-                if (o > red_v[threadIdx.x] || (o == red_v[threadIdx.x] && oi < red_i[threadIdx.x])) {
-                    red_v[threadIdx.x] = o;
-                    red_i[threadIdx.x] = oi;
-                }
+        // arg-max (largest |a|, then smallest row): butterfly within each warp, then over the
+        // warps' winners
+        for (int o = 16; o > 0; o >>= 1) {
+            const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
             }
-            __syncthreads();
         }
-        const int p = red_i[0];
-        const bool zero = red_v[0] == 0;
+        if ((threadIdx.x & 31) == 0) {
+            red_v[threadIdx.x >> 5] = best;
+            red_i[threadIdx.x >> 5] = bi;
+        }
+        __syncthreads();
+        R pv = red_v[0];
+        int p = red_i[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+            if (red_v[w] > pv || (red_v[w] == pv && red_i[w] < p)) {
+                pv = red_v[w];
+                p = red_i[w];
+            }
+        const bool zero = pv == 0;
         if (threadIdx.x == 0) {
             piv[k] = p;
             if (zero && info[blockIdx.x] == 0) info[blockIdx.x] = k + 1;
@@ -326,22 +333,22 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
         // right: A[:, k+1:] -= tau (A[:, k+1:] v) v^H   (all rows; a warp per row for the products)
         row_products(A, v, y, n, k + 1, tau);
         __syncthreads();
+        // then left: A[k+1:, k+1:] -= conj(tau) v (v^H A[k+1:, k+1:]).  Both act on one column
+        // at a time, so each thread owns its columns: right update (all rows) while summing
+        // v^H of the updated column, then the left update of that column.
+        (void)w;
         for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
             const C vc = CT<C>::mk(v[j].x, -v[j].y);
-#pragma unroll 4
-            for (int i = 0; i < n; i++) A[(long long)i * n + j] = csub(A[(long long)i * n + j], cmul(y[i], vc));
-        }
-        __syncthreads();
-        // left: A[k+1:, k+1:] -= conj(tau) v (v^H A[k+1:, k+1:])
-        for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
             C s = CT<C>::mk(0, 0);
 #pragma unroll 4
-            for (int i = k + 1; i < n; i++) s = cfma(CT<C>::mk(v[i].x, -v[i].y), A[(long long)i * n + j], s);
-            w[j] = cmul(CT<C>::mk(tau.x, -tau.y), s);
-        }
-        __syncthreads();
-        for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
-            const C wj = w[j];
+            for (int i = 0; i <= k; i++) A[(long long)i * n + j] = csub(A[(long long)i * n + j], cmul(y[i], vc));
+#pragma unroll 4
+            for (int i = k + 1; i < n; i++) {
+                const C a = csub(A[(long long)i * n + j], cmul(y[i], vc));
+                A[(long long)i * n + j] = a;
+                s = cfma(CT<C>::mk(v[i].x, -v[i].y), a, s);
+            }
+            const C wj = cmul(CT<C>::mk(tau.x, -tau.y), s);
 #pragma unroll 4
             for (int i = k + 1; i < n; i++) A[(long long)i * n + j] = csub(A[(long long)i * n + j], cmul(v[i], wj));
         }
@@ -391,6 +398,36 @@ __device__ __forceinline__ void rot_cols(typename CT<C>::R c, C s, C& x, C& y) {
 // Every element sees the same operations in the same order as rotation-by-rotation.
 constexpr int kHqrW = 64;
 
+// Givens generator of the chase: FP64 as zlartg; FP32 from two reciprocal square roots (c =
+// |f| / d, s = conj(g) f / (|f| d), r = f d / |f| with d = sqrt(|f|^2 + |g|^2)), which keeps
+// the rotation unitary to a few ulp -- enough for the FP32 stage the FP64 refinement follows
+__device__ __forceinline__ void givens_chase(double2 f, double2 g, double& c, double2& s, double2& r) {
+    zlartg(f, g, c, s, r);
+}
+__device__ __forceinline__ void givens_chase(float2 f, float2 g, float& c, float2& s, float2& r) {
+    const float gf = cabs2(g), ff = cabs2(f);
+    if (gf == 0.0f) {
+        c = 1.0f;
+        s = make_float2(0.0f, 0.0f);
+        r = f;
+        return;
+    }
+    if (ff == 0.0f) {
+        const float ig = rsqrtf(gf);
+        c = 0.0f;
+        s = make_float2(g.x * ig, -g.y * ig);
+        r = make_float2(gf * ig, 0.0f);
+        return;
+    }
+    const float iaf = rsqrtf(ff), id = rsqrtf(ff + gf);
+    c = ff * iaf * id;
+    const float2 fs = make_float2(f.x * iaf, f.y * iaf);
+    const float2 t = cmulc(g, fs);
+    s = make_float2(t.x * id, t.y * id);
+    const float d = (ff + gf) * id;
+    r = make_float2(fs.x * d, fs.y * d);
+}
+
 template <typename C>
 __device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, int ihi, int k0, int k1, C shift,
                           C* hw, typename CT<C>::R* hc, C* hs) {
@@ -408,17 +445,19 @@ __device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, in
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
         for (int k = k0; k < k1; k++) {
+            // every lane generates the rotation (no broadcast needed); lane 0 records it
+            C f, g, r, s;
+            R c;
+            if (k == l) {
+                f = csub(HW(l, l), shift);
+                g = HW(l + 1, l);
+            } else {
+                f = HW(k, k - 1);
+                g = HW(k + 1, k - 1);
+            }
+            givens_chase(f, g, c, s, r);
+            __syncwarp();
             if (lane == 0) {
-                C f, g, r, s;
-                R c;
-                if (k == l) {
-                    f = csub(HW(l, l), shift);
-                    g = HW(l + 1, l);
-                } else {
-                    f = HW(k, k - 1);
-                    g = HW(k + 1, k - 1);
-                }
-                zlartg(f, g, c, s, r);
                 if (k > l) {
                     HW(k, k - 1) = r;
                     HW(k + 1, k - 1) = CT<C>::mk(0, 0);
@@ -426,9 +465,6 @@ __device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, in
                 hc[k - k0] = c;
                 hs[k - k0] = s;
             }
-            __syncwarp();
-            const R c = hc[k - k0];
-            const C s = hs[k - k0];
             for (int j = k + lane; j <= k1; j += 32) rot_rows(c, s, HW(k, j), HW(k + 1, j));
             __syncwarp();
             const int rmax = min(k + 2, ihi);

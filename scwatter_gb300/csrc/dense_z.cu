@@ -272,6 +272,24 @@ __device__ __forceinline__ void row_products(const C* __restrict__ M, const C* _
     }
 }
 
+// col[i * ld] += u[i] * alpha for i in [i0, i1): kStripe rows at a time, loads before the
+// updates, so that a thread has kStripe independent loads in flight instead of one
+// load-update-store chain per row
+template <typename C>
+__device__ __forceinline__ void column_axpy(C* __restrict__ col, long long ld, int i0, int i1, const C* __restrict__ u,
+                                            C alpha) {
+    constexpr int kStripe = sizeof(typename CT<C>::R) == sizeof(float) ? 8 : 4;
+    for (int b = i0; b < i1; b += kStripe) {
+        C a[kStripe];
+#pragma unroll
+        for (int q = 0; q < kStripe; q++)
+            if (b + q < i1) a[q] = col[(long long)(b + q) * ld];
+#pragma unroll
+        for (int q = 0; q < kStripe; q++)
+            if (b + q < i1) col[(long long)(b + q) * ld] = cfma(u[b + q], alpha, a[q]);
+    }
+}
+
 template <typename C>
 __global__ void __launch_bounds__(1024)
 hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* __restrict__ work,
@@ -291,6 +309,7 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
     // whose off-diagonal entries are DFT rounding, from being scrambled by reflectors built
     // from noise.  FP64 keeps zgehd2's behaviour.
     constexpr bool kDropNegligible = sizeof(R) == sizeof(float);
+    constexpr int kStripe = sizeof(R) == sizeof(float) ? 8 : 4;
     R neg2 = 0;
     if (kDropNegligible) {
         R a2 = 0;
@@ -340,17 +359,25 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
         for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
             const C vc = CT<C>::mk(v[j].x, -v[j].y);
             C s = CT<C>::mk(0, 0);
-#pragma unroll 4
-            for (int i = 0; i <= k; i++) A[(long long)i * n + j] = csub(A[(long long)i * n + j], cmul(y[i], vc));
-#pragma unroll 4
-            for (int i = k + 1; i < n; i++) {
-                const C a = csub(A[(long long)i * n + j], cmul(y[i], vc));
-                A[(long long)i * n + j] = a;
-                s = cfma(CT<C>::mk(v[i].x, -v[i].y), a, s);
+            C* col = A + j;
+            // kStripe rows at a time: loads first, then the updates (see column_axpy)
+            for (int i0 = 0; i0 < n; i0 += kStripe) {
+                C a[kStripe];
+#pragma unroll
+                for (int q = 0; q < kStripe; q++)
+                    if (i0 + q < n) a[q] = col[(long long)(i0 + q) * n];
+#pragma unroll
+                for (int q = 0; q < kStripe; q++) {
+                    const int i = i0 + q;
+                    if (i < n) {
+                        a[q] = csub(a[q], cmul(y[i], vc));
+                        col[(long long)i * n] = a[q];
+                        if (i > k) s = cfma(CT<C>::mk(v[i].x, -v[i].y), a[q], s);
+                    }
+                }
             }
             const C wj = cmul(CT<C>::mk(tau.x, -tau.y), s);
-#pragma unroll 4
-            for (int i = k + 1; i < n; i++) A[(long long)i * n + j] = csub(A[(long long)i * n + j], cmul(v[i], wj));
+            column_axpy(col, n, k + 1, n, v, CT<C>::mk(-wj.x, -wj.y));
         }
         // column k below the subdiagonal
         for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x)
@@ -359,11 +386,8 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
         __syncthreads();
         row_products(Q, v, y, n, k + 1, tau);
         __syncthreads();
-        for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
-            const C vc = CT<C>::mk(v[j].x, -v[j].y);
-#pragma unroll 4
-            for (int i = 0; i < n; i++) Q[(long long)i * n + j] = csub(Q[(long long)i * n + j], cmul(y[i], vc));
-        }
+        for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x)
+            column_axpy(Q + j, n, 0, n, y, CT<C>::mk(-v[j].x, v[j].y));
         __syncthreads();
     }
 }
@@ -478,31 +502,43 @@ __device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, in
         H[(long long)(k0 + i) * n + c0 + j] = hw[i * ldw + j];
     }
 #undef HW
+    // Each task streams one stripe of k1 - k0 + 1 values.  The values are loaded kStripe at a
+    // time into registers before the rotations run through them: a load-rotate-store chain
+    // per element would wait a full memory latency per element (the compiler cannot move a
+    // load of the stripe above the store to the element before it).
+    constexpr int kStripe = sizeof(R) == sizeof(float) ? 16 : 4;
     const int nright = n - 1 - k1, nabove = k0;
     for (int t = threadIdx.x; t < nright + nabove + n; t += blockDim.x) {
-        if (t < nright) {                           // column j, rows k0..k1
-            C* col = H + k1 + 1 + t;
-            C x = col[(long long)k0 * n];
-#pragma unroll 4
-            for (int k = k0; k < k1; k++) {
-                C y = col[(long long)(k + 1) * n];
-                rot_rows(hc[k - k0], hs[k - k0], x, y);
-                col[(long long)k * n] = x;
-                x = y;
-            }
-            col[(long long)k1 * n] = x;
-        } else {                                    // row i of H (above the window) or of Z, columns k0..k1
-            C* row = (t < nright + nabove) ? H + (long long)(t - nright) * n : Z + (long long)(t - nright - nabove) * n;
-            C x = row[k0];
-#pragma unroll 4
-            for (int k = k0; k < k1; k++) {
-                C y = row[k + 1];
-                rot_cols(hc[k - k0], hs[k - k0], x, y);
-                row[k] = x;
-                x = y;
-            }
-            row[k1] = x;
+        const bool right = t < nright;              // column j (rows k0..k1), else a row (columns k0..k1)
+        C* base;
+        long long step;
+        if (right) {
+            base = H + k1 + 1 + t;
+            step = n;
+        } else {
+            base = (t < nright + nabove) ? H + (long long)(t - nright) * n : Z + (long long)(t - nright - nabove) * n;
+            step = 1;
         }
+        C x = base[(long long)k0 * step];
+        for (int kb = k0; kb < k1; kb += kStripe) {
+            const int m = min(kStripe, k1 - kb);
+            C y[kStripe];
+#pragma unroll
+            for (int q = 0; q < kStripe; q++)
+                if (q < m) y[q] = base[(long long)(kb + q + 1) * step];
+#pragma unroll
+            for (int q = 0; q < kStripe; q++) {
+                if (q < m) {
+                    if (right)
+                        rot_rows(hc[kb + q - k0], hs[kb + q - k0], x, y[q]);
+                    else
+                        rot_cols(hc[kb + q - k0], hs[kb + q - k0], x, y[q]);
+                    base[(long long)(kb + q) * step] = x;
+                    x = y[q];
+                }
+            }
+        }
+        base[(long long)k1 * step] = x;
     }
     __syncthreads();
 }

@@ -471,6 +471,8 @@ def batch_leg(args):
     t0 = time.perf_counter()
     b = Batch(ctx, items, lanes=args.batch_lanes, method=args.batch_method)
     t_create = time.perf_counter() - t0
+    print(f"# batch of {len(items)} created (graph recorded and instantiated) in {t_create:.1f} s",
+          file=sys.stderr, flush=True)
     info = b.info()
     if args.batch_warmup:
         b.run()

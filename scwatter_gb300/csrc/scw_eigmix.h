@@ -42,7 +42,9 @@ size_t eigmix_small_bytes(int n, int Z);
 void eigmix_carve_small(EigMixWs& w, char* base, int n, int Z);
 
 struct EigMixParams {
-    int steps = 6;                  // refinement steps (each begins with the residual check)
+    int steps = 10;                 // refinement steps (each begins with the residual check); converged
+                                    // slices skip the rest, and a step costs about 1/50 of the FP64 QR
+                                    // fallback that a slow slice would otherwise take
     double tau_rel = 1e-5;          // cluster threshold relative to ||A||_1
     double deg_rel = 1e-12;         // within a cluster: eigenvalues this close count as equal
     double tol = 1e-14;             // a slice stops refining once its max relative column residual is this small

@@ -1,0 +1,182 @@
+"""Compact factored coefficient files (.cwf) on the host, without a GPU.
+
+The .cwf file holds the separable coefficient set the GEMM-form evaluator reads (written and
+read on the device by ``scw_sep_save`` / ``scw_sep_load``):
+
+    char[8]    "SCWSEP01"
+    int32      M0, M1, Z, J (modes per half), rule (region rule), 0
+    float64    kx[M0], ky[M1], z_boundaries[Z + 1]
+    complex128 exterior[12 MF]   inc[3][MF], refl[3][MF], trans[3][MF], kz_inc, kz_refl, kz_trans
+    complex128 kz[Z][2][Jp]      (Jp = J rounded up to even; entries J..Jp-1 are zero)
+    complex64  Q[Z][2][3][MF][Jp]
+
+Row p = a M1 + b of an MF block is harmonic (kx[a], ky[b]).  Every amplitude is referenced to
+its own plane: E0 exp(i kz z_ref), where the .cw record stores E0 wound to z = 0
+(sCWatter.cpp:469-482).  :func:`factor_cw` builds the set from a volume-solver ``.cw``
+structure (the host restatement of ``scw_sep_from_cw``), :func:`to_cw` rebuilds the wave
+lists from it, and :func:`read_cwf` / :func:`write_cwf` move it to and from a file.  These are
+format tools: evaluation runs on the GPU (``SeparableSet``).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .cw import CoupledWaveStructure, HomogeneousLayer
+
+MAGIC = b"SCWSEP01"
+
+
+@dataclass
+class FactoredSet:
+    M0: int
+    M1: int
+    Z: int
+    J: int
+    rule: int
+    kx: np.ndarray          # [M0] float64
+    ky: np.ndarray          # [M1] float64
+    zb: np.ndarray          # [Z + 1] float64
+    ext: np.ndarray         # [12 MF] complex128
+    kz: np.ndarray          # [Z, 2, Jp] complex128
+    Q: np.ndarray           # [Z, 2, 3, MF, Jp] complex64
+
+    @property
+    def MF(self) -> int:
+        return self.M0 * self.M1
+
+    @property
+    def Jp(self) -> int:
+        return self.J + (self.J & 1)
+
+    def exterior(self, block: str) -> tuple:
+        """(amplitudes [3, MF], kz [MF]) of ``"inc"``, ``"refl"`` or ``"trans"``."""
+        MF = self.MF
+        i = {"inc": 0, "refl": 1, "trans": 2}[block]
+        return self.ext[3 * MF * i:3 * MF * (i + 1)].reshape(3, MF), self.ext[9 * MF + MF * i:9 * MF + MF * (i + 1)]
+
+
+def file_size(M0, M1, Z, J) -> int:
+    MF, Jp = M0 * M1, J + (J & 1)
+    return 8 + 24 + 8 * (M0 + M1 + Z + 1) + 16 * 12 * MF + 16 * Z * 2 * Jp + (8 * Z * 2 * 3 * MF * Jp if J else 0)
+
+
+def write_cwf(path, fs: FactoredSet) -> None:
+    with open(path, "wb") as f:
+        f.write(MAGIC)
+        f.write(np.array([fs.M0, fs.M1, fs.Z, fs.J, fs.rule, 0], dtype="<i4").tobytes())
+        for a in (fs.kx, fs.ky, fs.zb):
+            f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
+        f.write(np.ascontiguousarray(fs.ext, dtype="<c16").tobytes())
+        f.write(np.ascontiguousarray(fs.kz, dtype="<c16").tobytes())
+        if fs.J and fs.Z:
+            f.write(np.ascontiguousarray(fs.Q, dtype="<c8").tobytes())
+
+
+def read_cwf(path) -> FactoredSet:
+    data = open(path, "rb").read()
+    if len(data) < 32 or data[:8] != MAGIC:
+        raise ValueError(f"not a factored coefficient file: {path}")
+    M0, M1, Z, J, rule, _ = (int(v) for v in np.frombuffer(data, "<i4", 6, 8))
+    if M0 <= 0 or M1 <= 0 or Z < 0 or J < 0 or len(data) != file_size(M0, M1, Z, J):
+        raise ValueError("factored file size does not match its header")
+    MF, Jp = M0 * M1, J + (J & 1)
+    off = 32
+
+    def take(dtype, count):
+        nonlocal off
+        a = np.frombuffer(data, dtype, count, off)
+        off += a.nbytes
+        return a.copy()
+
+    kx, ky, zb = take("<f8", M0), take("<f8", M1), take("<f8", Z + 1)
+    ext = take("<c16", 12 * MF)
+    kz = take("<c16", Z * 2 * Jp).reshape(Z, 2, Jp)
+    Q = take("<c8", Z * 2 * 3 * MF * Jp).reshape(Z, 2, 3, MF, Jp) if J else np.zeros((Z, 2, 3, MF, 0), np.complex64)
+    return FactoredSet(M0, M1, Z, J, rule, kx, ky, zb, ext, kz, Q)
+
+
+def factor_cw(cw: CoupledWaveStructure, rule: int = 0) -> FactoredSet:
+    """The separable set of a volume-solver .cw structure (the host form of scw_sep_from_cw):
+    the structure is checked exactly (kx per column, ky per row of the harmonic grid, one kz
+    per mode across harmonics) and every amplitude re-referenced to its plane in FP64."""
+    Pi = np.asarray(cw.Pi, np.complex128).reshape(-1, 6)
+    MF, ZL = len(Pi), len(cw.Layers)
+    if MF == 0 or ZL < 2:
+        raise ValueError("not a volume-solver .cw (needs incident waves and >= 2 boundaries)")
+    Z = ZL - 1
+    M1 = 1
+    while M1 < MF and Pi[M1, 3] == Pi[0, 3]:
+        M1 += 1
+    if MF % M1:
+        raise ValueError("incident block is not an M0 x M1 harmonic grid")
+    M0 = MF // M1
+    kx = Pi[::M1, 3].real.copy()[:M0]
+    ky = Pi[:M1, 4].real.copy()
+    p = np.arange(MF)
+    gx, gy = kx[p // M1], ky[p % M1]
+
+    def grid_ok(w):
+        return (np.array_equal(w[:, 3], gx.astype(np.complex128)) and np.array_equal(w[:, 4], gy.astype(np.complex128)))
+
+    L0, LZ = cw.Layers[0], cw.Layers[-1]
+    blocks = []
+    zb = np.array([L.z for L in cw.Layers], np.float64)
+    for w, zr in ((Pi, 0.0), (np.asarray(L0.Pr).reshape(-1, 6), zb[0]), (np.asarray(LZ.Pt).reshape(-1, 6), zb[-1])):
+        if len(w) != MF or not grid_ok(w):
+            raise ValueError("exterior waves are not separable")
+        f = np.exp(1j * w[:, 5] * zr)
+        blocks.append(((w[:, :3] * f[:, None]).T, w[:, 5]))
+    ext = np.concatenate([b[0].ravel() for b in blocks] + [b[1] for b in blocks])
+    J = len(np.asarray(L0.Pt).reshape(-1, 6)) // MF
+    Jp = J + (J & 1)
+    kz = np.zeros((Z, 2, Jp), np.complex128)
+    Q = np.zeros((Z, 2, 3, MF, Jp), np.complex64)
+    for l in range(Z):
+        for h, (w, zr) in enumerate(((cw.Layers[l].Pt, zb[l]), (cw.Layers[l + 1].Pr, zb[l + 1]))):
+            w = np.asarray(w).reshape(-1, 6)
+            if len(w) != MF * J:
+                raise ValueError(f"slice {l} mode blocks are not MF x J")
+            w = w.reshape(MF, J, 6)
+            kj = w[0, :, 5]
+            if not (np.array_equal(w[:, :, 5], np.broadcast_to(kj, (MF, J))) and
+                    np.array_equal(w[:, :, 3], np.broadcast_to(gx[:, None], (MF, J)).astype(np.complex128)) and
+                    np.array_equal(w[:, :, 4], np.broadcast_to(gy[:, None], (MF, J)).astype(np.complex128))):
+                raise ValueError(f"slice {l} waves are not separable")
+            kz[l, h, :J] = kj
+            f = np.exp(1j * kj * zr)
+            Q[l, h, :, :, :J] = np.moveaxis(w[:, :, :3] * f[None, :, None], 2, 0).astype(np.complex64)
+    return FactoredSet(M0, M1, Z, J, rule, kx, ky, zb, ext, kz, Q)
+
+
+def to_cw(fs: FactoredSet) -> CoupledWaveStructure:
+    """The wave lists of the set in the order the volume solver writes them (harmonic outer,
+    mode inner), each amplitude wound back to z = 0 from its plane."""
+    MF, J = fs.MF, fs.J
+    p = np.arange(MF)
+    gx = fs.kx[p // fs.M1].astype(np.complex128)
+    gy = fs.ky[p % fs.M1].astype(np.complex128)
+
+    def exterior(block, zr):
+        a, kz = fs.exterior(block)
+        f = np.exp(-1j * kz * zr)
+        return np.stack([a[0] * f, a[1] * f, a[2] * f, gx, gy, kz], axis=1)
+
+    def modes(l, h, zr):
+        kj = fs.kz[l, h, :J]
+        a = fs.Q[l, h, :, :, :J].astype(np.complex128) * np.exp(-1j * kj * zr)[None, None, :]
+        out = np.empty((MF, J, 6), np.complex128)
+        out[:, :, 0], out[:, :, 1], out[:, :, 2] = a[0], a[1], a[2]
+        out[:, :, 3], out[:, :, 4], out[:, :, 5] = gx[:, None], gy[:, None], kj[None, :]
+        return out.reshape(-1, 6)
+
+    cw = CoupledWaveStructure()
+    cw.Pi = exterior("inc", 0.0)
+    empty = np.zeros((0, 6), np.complex128)
+    for l in range(fs.Z + 1):
+        zr = fs.zb[l]
+        Pr = exterior("refl", zr) if l == 0 else (modes(l - 1, 1, zr) if J else empty)
+        Pt = exterior("trans", zr) if l == fs.Z else (modes(l, 0, zr) if J else empty)
+        cw.Layers.append(HomogeneousLayer(z=float(zr), Pr=Pr, Pt=Pt))
+    return cw

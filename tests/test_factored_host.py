@@ -1,0 +1,69 @@
+"""The compact factored coefficient file on the host (scwatter_gb300/factored.py): the
+factoring of golden volume-solver .cw structures, the file layout, and the wave lists rebuilt
+from the file against the original .cw records (amplitudes at complex64 precision)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import solve_oracle as so
+from scwatter_gb300 import factored
+from scwatter_gb300.cw import CoupledWaveStructure, HomogeneousLayer
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _load(name):
+    c = so.cw_from_bytes(open(os.path.join(GOLDEN, name), "rb").read())
+    S = CoupledWaveStructure()
+    S.Pi = np.asarray(c.Pi, np.complex128)
+    S.Layers = [HomogeneousLayer(z=c.z[l], Pr=np.asarray(c.Pr[l]), Pt=np.asarray(c.Pt[l])) for l in range(len(c.z))]
+    return S
+
+
+def _close(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    assert np.all(np.abs(a - b) <= 2e-7 * np.abs(b) + 1e-300)
+
+
+@pytest.mark.parametrize("name", ["spheres_2x8x8_c3.cw", "oblique_3x10x12_c3x5.cw"])
+def test_factor_write_read_rebuild(tmp_path, name):
+    S = _load(name)
+    fs = factored.factor_cw(S)
+    MF, Z = fs.MF, fs.Z
+    assert fs.J == 2 * MF and Z == len(S.Layers) - 1
+    f = tmp_path / "c.cwf"
+    factored.write_cwf(f, fs)
+    assert os.path.getsize(f) == factored.file_size(fs.M0, fs.M1, Z, fs.J)
+    raw = f.read_bytes()
+    assert raw[:8] == b"SCWSEP01"
+    assert list(np.frombuffer(raw, "<i4", 6, 8)) == [fs.M0, fs.M1, Z, fs.J, 0, 0]
+    g = factored.read_cwf(f)
+    factored.write_cwf(tmp_path / "d.cwf", g)
+    assert (tmp_path / "d.cwf").read_bytes() == raw
+    R = factored.to_cw(g)
+    # k vectors and z are exact, amplitudes within complex64 rounding
+    assert np.array_equal(R.Pi[:, 3:], S.Pi[:, 3:])
+    _close(R.Pi[:, :3], S.Pi[:, :3])
+    for L0, L1 in zip(R.Layers, S.Layers):
+        assert L0.z == L1.z
+        for a, b in ((L0.Pr, L1.Pr), (L0.Pt, L1.Pt)):
+            b = np.asarray(b).reshape(-1, 6)
+            assert np.array_equal(a[:, 3:], b[:, 3:])
+            _close(a[:, :3], b[:, :3])
+
+
+def test_malformed_inputs(tmp_path):
+    S = _load("spheres_2x8x8_c3.cw")
+    bad = _load("spheres_2x8x8_c3.cw")
+    bad.Layers[1].Pt = bad.Layers[1].Pt[:-1]
+    with pytest.raises(ValueError):
+        factored.factor_cw(bad)
+    f = tmp_path / "c.cwf"
+    factored.write_cwf(f, factored.factor_cw(S))
+    data = f.read_bytes()
+    for blob in (data[:-8], b"SCWSEP02" + data[8:]):
+        (tmp_path / "x.cwf").write_bytes(blob)
+        with pytest.raises(ValueError):
+            factored.read_cwf(tmp_path / "x.cwf")

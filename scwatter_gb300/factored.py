@@ -19,6 +19,8 @@ format tools: evaluation runs on the GPU (``SeparableSet``).
 """
 from __future__ import annotations
 
+import argparse
+import sys
 from dataclasses import dataclass
 
 import numpy as np
@@ -180,3 +182,30 @@ def to_cw(fs: FactoredSet) -> CoupledWaveStructure:
         Pt = exterior("trans", zr) if l == fs.Z else (modes(l, 0, zr) if J else empty)
         cw.Layers.append(HomogeneousLayer(z=float(zr), Pr=Pr, Pt=Pt))
     return cw
+
+
+def main(argv=None) -> int:
+    """``python -m scwatter_gb300.factored in.cw out.cwf`` factors a volume-solver .cw file;
+    ``python -m scwatter_gb300.factored in.cwf out.cw`` writes the wave lists back."""
+    ap = argparse.ArgumentParser(prog="scwatter_gb300.factored", description="convert between .cw and .cwf")
+    ap.add_argument("input")
+    ap.add_argument("output")
+    a = ap.parse_args(argv)
+    if a.input.endswith(".cwf"):
+        to_cw(read_cwf(a.input)).save(a.output)
+    else:
+        S = CoupledWaveStructure()
+        if not S.load(a.input):
+            print(f"ERROR: file {a.input} not found", file=sys.stderr)
+            return 1
+        try:
+            fs = factor_cw(S)
+        except ValueError as e:
+            print(f"ERROR: {a.input}: {e}", file=sys.stderr)
+            return 2
+        write_cwf(a.output, fs)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -67,3 +67,18 @@ def test_malformed_inputs(tmp_path):
         (tmp_path / "x.cwf").write_bytes(blob)
         with pytest.raises(ValueError):
             factored.read_cwf(tmp_path / "x.cwf")
+
+
+def test_command_line_round_trip(tmp_path):
+    from scwatter_gb300.cw import CoupledWaveStructure as CWS
+    src = os.path.join(GOLDEN, "oblique_3x10x12_c3x5.cw")
+    f, back = tmp_path / "g.cwf", tmp_path / "g.cw"
+    assert factored.main([src, str(f)]) == 0
+    assert factored.main([str(f), str(back)]) == 0
+    A, B = CWS(), CWS()
+    assert A.load(src) and B.load(str(back))
+    assert np.array_equal(A.Pi[:, 3:], B.Pi[:, 3:]) and len(A.Layers) == len(B.Layers)
+    for L0, L1 in zip(A.Layers, B.Layers):
+        assert L0.z == L1.z and L0.Pr.shape == L1.Pr.shape and L0.Pt.shape == L1.Pt.shape
+        _close(L1.Pt[:, :3], L0.Pt[:, :3])
+    assert factored.main([str(tmp_path / "missing.cw"), str(f)]) == 1

@@ -184,6 +184,102 @@ def to_cw(fs: FactoredSet) -> CoupledWaveStructure:
     return cw
 
 
+def _cw_layout(path):
+    """Byte offsets of a .cw file (CoupledWaveStructure.h:72-100): (Pi offset, nPi, [(z, Pr
+    offset, nPr, Pt offset, nPt) per layer]), from the counts alone."""
+    size = __import__("os").path.getsize(path)
+    with open(path, "rb") as f:
+        def u64():
+            b = f.read(8)
+            if len(b) != 8:
+                raise ValueError("truncated .cw file")
+            return int(np.frombuffer(b, "<u8")[0])
+        u64()                                   # sizeof(T)
+        npi = u64()
+        pi_off = f.tell()
+        f.seek(96 * npi, 1)
+        nl = u64()
+        layers = []
+        for _ in range(nl):
+            b = f.read(8)
+            if len(b) != 8:
+                raise ValueError("truncated .cw layer")
+            z = float(np.frombuffer(b, "<f8")[0])
+            npr = u64()
+            pr_off = f.tell()
+            f.seek(96 * npr, 1)
+            npt = u64()
+            pt_off = f.tell()
+            f.seek(96 * npt, 1)
+            layers.append((z, pr_off, npr, pt_off, npt))
+        if f.tell() > size:
+            raise ValueError("truncated .cw file")
+    return pi_off, npi, layers
+
+
+def convert_cw_file(src, dst, rule: int = 0) -> FactoredSet:
+    """Factors a volume-solver .cw file into a .cwf file, streaming: the .cw is memory-mapped
+    and read one slice's two mode blocks at a time, so host memory stays at one slice however
+    large the file (about 63 GB at config 2).  Returns the set with an empty Q."""
+    pi_off, npi, layers = _cw_layout(src)
+    mm = np.memmap(src, dtype=np.uint8, mode="r")
+
+    def block(off, n):
+        return np.frombuffer(mm, "<c16", 6 * n, off).reshape(n, 6)
+
+    head = CoupledWaveStructure()
+    head.Pi = block(pi_off, npi)
+    ZL = len(layers)
+    if ZL < 2:
+        raise ValueError("not a volume-solver .cw (needs incident waves and >= 2 boundaries)")
+    # exterior blocks and the harmonic grid from a structure holding only the exterior waves
+    z0, pr0, npr0, pt0, npt0 = layers[0]
+    zZ, prZ, nprZ, ptZ, nptZ = layers[-1]
+    head.Layers = [HomogeneousLayer(z=z0, Pr=block(pr0, npr0), Pt=np.zeros((0, 6), np.complex128)),
+                   HomogeneousLayer(z=zZ, Pr=np.zeros((0, 6), np.complex128), Pt=block(ptZ, nptZ))]
+    fs = factor_cw(head, rule)                  # J = 0 here: exterior only
+    MF = fs.MF
+    J = npt0 // MF
+    Jp = J + (J & 1)
+    Z = ZL - 1
+    zb = np.array([L[0] for L in layers], np.float64)
+    p = np.arange(MF)
+    gx, gy = fs.kx[p // fs.M1].astype(np.complex128), fs.ky[p % fs.M1].astype(np.complex128)
+
+    def modes(off, n, zr, l):
+        if n != MF * J:
+            raise ValueError(f"slice {l} mode blocks are not MF x J")
+        w = block(off, n).reshape(MF, J, 6)
+        kj = w[0, :, 5].copy()
+        if not (np.array_equal(w[:, :, 5], np.broadcast_to(kj, (MF, J))) and
+                np.array_equal(w[:, :, 3], np.broadcast_to(gx[:, None], (MF, J))) and
+                np.array_equal(w[:, :, 4], np.broadcast_to(gy[:, None], (MF, J)))):
+            raise ValueError(f"slice {l} waves are not separable")
+        q = np.zeros((3, MF, Jp), np.complex64)
+        q[:, :, :J] = np.moveaxis(w[:, :, :3] * np.exp(1j * kj * zr)[None, :, None], 2, 0).astype(np.complex64)
+        return kj, q
+
+    kz = np.zeros((Z, 2, Jp), np.complex128)
+    for l in range(Z):                          # kz of every slice first (the file order)
+        for h, (off, n, zr) in enumerate(((layers[l][3], layers[l][4], zb[l]), (layers[l + 1][1], layers[l + 1][2], zb[l + 1]))):
+            if n != MF * J:
+                raise ValueError(f"slice {l} mode blocks are not MF x J")
+            kz[l, h, :J] = block(off, J)[:, 5]
+    with open(dst, "wb") as f:
+        f.write(MAGIC)
+        f.write(np.array([fs.M0, fs.M1, Z, J, rule, 0], dtype="<i4").tobytes())
+        for a in (fs.kx, fs.ky, zb):
+            f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
+        f.write(np.ascontiguousarray(fs.ext, dtype="<c16").tobytes())
+        f.write(kz.astype("<c16").tobytes())
+        if J:
+            for l in range(Z):
+                for off, n, zr in ((layers[l][3], layers[l][4], zb[l]), (layers[l + 1][1], layers[l + 1][2], zb[l + 1])):
+                    kj, q = modes(off, n, zr, l)
+                    f.write(q.astype("<c8").tobytes())
+    return FactoredSet(fs.M0, fs.M1, Z, J, rule, fs.kx, fs.ky, zb, fs.ext, kz, np.zeros((Z, 2, 3, MF, 0), np.complex64))
+
+
 def main(argv=None) -> int:
     """``python -m scwatter_gb300.factored in.cw out.cwf`` factors a volume-solver .cw file;
     ``python -m scwatter_gb300.factored in.cwf out.cw`` writes the wave lists back."""
@@ -194,16 +290,15 @@ def main(argv=None) -> int:
     if a.input.endswith(".cwf"):
         to_cw(read_cwf(a.input)).save(a.output)
     else:
-        S = CoupledWaveStructure()
-        if not S.load(a.input):
+        import os
+        if not os.path.exists(a.input):
             print(f"ERROR: file {a.input} not found", file=sys.stderr)
             return 1
         try:
-            fs = factor_cw(S)
+            convert_cw_file(a.input, a.output)
         except ValueError as e:
             print(f"ERROR: {a.input}: {e}", file=sys.stderr)
             return 2
-        write_cwf(a.output, fs)
     return 0
 
 

@@ -82,3 +82,14 @@ def test_command_line_round_trip(tmp_path):
         assert L0.z == L1.z and L0.Pr.shape == L1.Pr.shape and L0.Pt.shape == L1.Pt.shape
         _close(L1.Pt[:, :3], L0.Pt[:, :3])
     assert factored.main([str(tmp_path / "missing.cw"), str(f)]) == 1
+
+
+@pytest.mark.parametrize("name", ["spheres_2x8x8_c3.cw", "oblique_3x10x12_c3x5.cw"])
+def test_streaming_conversion_matches_in_memory(tmp_path, name):
+    a, b = tmp_path / "stream.cwf", tmp_path / "memory.cwf"
+    factored.convert_cw_file(os.path.join(GOLDEN, name), a)
+    factored.write_cwf(b, factored.factor_cw(_load(name)))
+    assert a.read_bytes() == b.read_bytes()
+    (tmp_path / "t.cw").write_bytes(open(os.path.join(GOLDEN, name), "rb").read()[:-50])
+    with pytest.raises(ValueError):
+        factored.convert_cw_file(tmp_path / "t.cw", tmp_path / "t.cwf")

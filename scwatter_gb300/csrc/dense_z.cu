@@ -299,8 +299,7 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
     A += sA * blockIdx.x;
     Q += sA * blockIdx.x;
     C* v = work + (long long)blockIdx.x * 3 * n;      // Householder vector (rows k+1..n-1)
-    C* w = v + n;                                       // v^H A (row vector) / A v (column)
-    C* y = w + n;
+    C* y = v + 2 * n;                                   // tau A v / tau Q v (the work keeps 3 n per matrix)
     __shared__ R sh[32];
     __shared__ C s_tau, s_beta;
     // FP32 (first stage of the mixed solver): a column whose part below the diagonal is under
@@ -355,7 +354,6 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
         // then left: A[k+1:, k+1:] -= conj(tau) v (v^H A[k+1:, k+1:]).  Both act on one column
         // at a time, so each thread owns its columns: right update (all rows) while summing
         // v^H of the updated column, then the left update of that column.
-        (void)w;
         for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) {
             const C vc = CT<C>::mk(v[j].x, -v[j].y);
             C s = CT<C>::mk(0, 0);

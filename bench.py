@@ -18,8 +18,9 @@ point's region (waves_end[l] - waves_begin[l], cpuEvaluator.cpp:34-53) -- the sa
 the plain and the separable form.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-Multi-GPU (torchrun): every rank evaluates its own copy of the workload (weak scaling, no
-data exchange); value = all ranks' units / max-over-ranks time.
+Multi-GPU (torchrun): the grid is split into z-slabs, one per rank (strong scaling: the total
+work is fixed), each evaluated by the slab entry points with no exchange of data; value = the
+whole grid's units / max-over-ranks time.
 """
 from __future__ import annotations
 
@@ -183,6 +184,38 @@ def run_reference(args):
                       "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def link_peaks(torch, nbytes=2 << 30):
+    """Pinned host <-> device copy bandwidth of this machine (best of 3 single cudaMemcpyAsync of
+    nbytes each way, and both directions at once on two streams)."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h2 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def best(fn):
+        ts = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    def both():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+    out = {"h2d_gbs": nbytes / best(lambda: d.copy_(h, non_blocking=True)) / 1e9,
+           "d2h_gbs": nbytes / best(lambda: h.copy_(d, non_blocking=True)) / 1e9,
+           "bidirectional_gbs": 2 * nbytes / best(both) / 1e9, "bytes_per_copy": nbytes}
+    del h, h2, d, d2
+    torch.cuda.empty_cache()
+    return out
+
+
 def rel_l2(got, ref):
     got = np.asarray(got).reshape(-1, 3).astype(np.complex128)
     ref = np.asarray(ref).reshape(-1, 3).astype(np.complex128)
@@ -199,6 +232,7 @@ def run_ours(args):
     from scwatter_gb300 import _lib
     from scwatter_gb300 import evaluator as ev
     from scwatter_gb300 import separable as sp
+    from scwatter_gb300 import shard
     from scwatter_gb300 import synthetic
 
     cfg = CFG2
@@ -224,12 +258,11 @@ def run_ours(args):
                       ctypes.c_void_p(Qu_src[l].data_ptr()))
     upload(Qd, Qu)
     ctx.synchronize()
-    hQd = hQu = None
-    if not args.no_e2e:        # pinned host copy of the coefficients for the host-buffer leg
-        hQd = torch.empty(Qd.shape, dtype=torch.complex64, pin_memory=True)
-        hQu = torch.empty(Qu.shape, dtype=torch.complex64, pin_memory=True)
-        hQd.copy_(Qd)
-        hQu.copy_(Qu)
+    hQ = None
+    if not args.no_e2e:        # pinned host copy of the coefficients ([Z][2][3][MF][J]) for the host-buffer leg
+        hQ = torch.empty((Z, 2) + tuple(Qd.shape[1:]), dtype=torch.complex64, pin_memory=True)
+        hQ[:, 0].copy_(Qd)
+        hQ[:, 1].copy_(Qu)
     # keep the one slice needed for the plain / CPU samples, free the rest of the generator output
     Qd_s = Qd[CPU_SLICE].cpu().numpy()
     Qu_s = Qu[CPU_SLICE].cpu().numpy()
@@ -239,12 +272,19 @@ def run_ours(args):
 
     dx, dy, dz, z0 = grid_params(cfg)
     Nx, Ny, Nz = cfg["Nx"], cfg["Ny"], cfg["Nz"]
-    units = Nx * Ny * Nz * 2 * (2 * MF) * MF          # every point is interior: 4 MF^2 waves
-    out = torch.empty((Nz, Ny, Nx, 3), dtype=torch.complex64, device="cuda")
+    # this rank's z-slab of the grid (the whole grid at N = 1), balanced by points x modes per plane
+    waves_per_region = [2 * MF] + [4 * MF * MF] * Z + [MF]
+    w = shard.plane_weights(z0, dz, Nz, fs.z, waves_per_region)
+    k0, k1 = shard.slab_bounds(Nz, ws, rank, w)
+    nz_local = k1 - k0
+    units = int(Nx * Ny * w.sum())                      # whole job; every point is interior: 4 MF^2 waves
+    units_local = int(Nx * Ny * w[k0:k1].sum())
+    out = torch.empty((max(nz_local, 1), Ny, Nx, 3), dtype=torch.complex64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def step(method=sp.TF32X3):
-        sep.eval_volume_device(cfg["x0"], cfg["y0"], z0, dx, dy, dz, Nx, Ny, Nz, out.data_ptr(), method=method)
+        if nz_local > 0:
+            sep.eval_slab_device(cfg["x0"], cfg["y0"], z0, dx, dy, dz, Nx, Ny, k0, k1, out.data_ptr(), method=method)
 
     for _ in range(args.warmup):
         step()
@@ -274,7 +314,7 @@ def run_ours(args):
         tt = torch.tensor([t_step], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_step = float(tt.item())
-    value = units * ws / t_step
+    value = units / t_step
 
     # per-kernel times of one step (CUDA events around each launch, on the launching stream)
     ctx.set_timing(True)
@@ -292,8 +332,9 @@ def run_ours(args):
         ctx.set_timing(False)
         ms = sum(v[0] for v in r.values())
         forms[name] = {"ms_per_step": ms, "synth_ms": sum(v[0] for k, v in r.items() if "synth" in k),
-                       "value": units / (ms / 1e3),
-                       "rel_l2_vs_tf32x3": rel_l2(out[Nz // 2].cpu().numpy(), sep_field_all[Nz // 2].cpu().numpy())}
+                       "value": units_local / (ms / 1e3),
+                       "rel_l2_vs_tf32x3": rel_l2(out[nz_local // 2].cpu().numpy(),
+                                                  sep_field_all[nz_local // 2].cpu().numpy())}
 
     # dominant kernel: the stage-1 coefficient contraction streams every Q block once
     contract_ms = kt.get("sep_contract_kernel", (0.0, 0))[0]
@@ -331,7 +372,7 @@ def run_ours(args):
     plain_v = plain_units / (plain_ms / 1e3)
     plain_field = pout.cpu().numpy()
     # the separable form at the same points: the first P x P corner of grid plane kz_mid
-    sep_field = sep_field_all[kz_mid, :P, :P, :].cpu().numpy() if kz_mid < Nz else None
+    sep_field = sep_field_all[kz_mid - k0, :P, :P, :].cpu().numpy() if k0 <= kz_mid < k1 else None
     del wset
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
 
@@ -344,10 +385,12 @@ def run_ours(args):
                   "cpu_f32_vs_separable_rel_l2": (rel_l2(cpu_out, sep_field[:rows, :cw_])
                                                   if sep_field is not None else None)}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+                "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "strong",
                 "vs_baseline": None, "dtype": "c64", "data": "synthetic",
                 "config": {"workload": cfg["name"], "form": "separable, tcgen05 3xTF32 output GEMM",
                            "points_modes_per_step": units, "l2": "flushed between timed steps; Q (15.7 GB) > L2",
+                           "parallelism": f"z-slabs over {ws} process(es), one GPU each, no collective on the "
+                                          f"data path (rank 0: planes {k0}..{k1 - 1} of {Nz})",
                            "wall_s_timed_region": t_wall},
                 "roofline": {"bound": "hbm", "kernel": "sep_contract_kernel (streams every Q block once)",
                              "achieved": contract_gbs, "peak": hbm_peak, "unit": "GB/s",
@@ -371,23 +414,46 @@ def run_ours(args):
                 "gpu_launches": int(launches), "clocks": clocks}
     del sep_field_all
 
-    # e2e through the host-buffer API: upload Q from pinned host memory, evaluate, read back
+    # e2e through the host-buffer API (scw_sep_eval_volume_host): Q uploaded from pinned host
+    # memory slice by slice while earlier slices are evaluated, planes read back as they finish
     if not args.no_e2e:
-        host_out = torch.empty((Nz, Ny, Nx, 3), dtype=torch.complex64, pin_memory=True)
+        del out
+        torch.cuda.empty_cache()
+        host_out = torch.empty((max(nz_local, 1), Ny, Nx, 3), dtype=torch.complex64, pin_memory=True)
         e2e_t = []
+        # Q bytes this rank uploads per step: the slices its planes lie in
+        regions = shard.region_of_z(shard.plane_z(z0, dz, Nz)[k0:k1], fs.z)
+        h2d_local = int(len({int(r) for r in regions if 1 <= r <= Z}) * q_bytes // Z)
         for i in range(max(2, min(args.steps, 3)) + 1):
             ctx.synchronize()
+            if ws > 1:
+                torch.distributed.barrier()
             t0 = time.perf_counter()
-            upload(hQd, hQu)
-            step()
-            host_out.copy_(out, non_blocking=True)
-            ctx.synchronize()
-            torch.cuda.synchronize()
+            if nz_local > 0:
+                sep.eval_slab_host(hQ, cfg["x0"], cfg["y0"], z0, dx, dy, dz, Nx, Ny, k0, k1, out=host_out,
+                                   method=sp.TF32X3)
             if i > 0:
                 e2e_t.append(time.perf_counter() - t0)
+        t_e2e = float(np.mean(e2e_t))
+        h2d_total, d2h_total = h2d_local, nz_local * Ny * Nx * 24
+        if ws > 1:
+            tt = torch.tensor([t_e2e], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(tt.item())
+            bb = torch.tensor([h2d_total, d2h_total], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(bb)
+            h2d_total, d2h_total = int(bb[0].item()), int(bb[1].item())
+        link = link_peaks(torch)
         if line is not None:
-            line["e2e"] = {"value": units / float(np.mean(e2e_t)), "unit": UNIT, "h2d_bytes_per_step": int(q_bytes),
-                           "d2h_bytes_per_step": int(out_bytes), "ms_per_step": float(np.mean(e2e_t)) * 1e3}
+            t_bound = max(h2d_local / (link["h2d_gbs"] * 1e9), nz_local * Ny * Nx * 24 / (link["d2h_gbs"] * 1e9))
+            line["e2e"] = {"value": units / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d_total,
+                           "d2h_bytes_per_step": d2h_total, "ms_per_step": t_e2e * 1e3,
+                           "api": "scw_sep_eval_slab_host (the whole volume at N = 1; pinned host Q in, pinned host planes out)",
+                           "roofline": {"bound": "host link", "achieved": (h2d_local + nz_local * Ny * Nx * 24) / t_e2e / 1e9,
+                                        "unit": "GB/s", "link_peaks_GBs": link,
+                                        "t_link_bound_ms": t_bound * 1e3, "frac": t_bound / t_e2e,
+                                        "note": "frac = time the measured link needs for the step's H2D and D2H "
+                                                "bytes (the two directions overlap) / e2e time"}}
     if line is not None and not args.no_solve:
         line["solve"] = solve_leg(ctx)
     if line is not None:

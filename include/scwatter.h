@@ -143,8 +143,9 @@ SCW_API scw_status scw_eval_volume_device(scw_waves waves, float x_start, float 
  * GPU that loads it until exit) and its region table travels as kernel parameters.
  * Limits: N <= 16384 and at most 160 layers (SCW_ERR_ARG beyond either); planes of more
  * than 1024 tiles of 16 x 32 points run without the split.
- * The first call on a device looks up the array's device address (and may load the library's
- * GPU module there); make that first call before any stream capture on that device.
+ * The first call through a context looks up the array's address on the context's device (and may
+ * load the library's GPU module there) and keeps it in the context; make that first call before
+ * any stream capture on that device.  After a cudaDeviceReset, create a new context.
  * All calls share the one array per device: calls that overlap on the GPU (other streams,
  * other contexts on the same device) race.  Calls on one stream are ordered and safe; each
  * call writes every scratch element it reads, so nothing needs clearing between calls. */
@@ -182,10 +183,38 @@ SCW_API scw_status scw_sep_from_cw(scw_ctx ctx, scw_cw cw, scw_sep* out);
 SCW_API scw_status scw_sep_save(scw_sep s, const char* path);
 SCW_API scw_status scw_sep_load(scw_ctx ctx, const char* path, scw_sep* out);
 SCW_API scw_status scw_sep_info(scw_sep s, int* M0, int* M1, int* n_slices, int* modes_per_half);
+/* kx [M0], ky [M1] (the separable harmonic grid) and the Z + 1 slice boundaries; any may be NULL. */
+SCW_API scw_status scw_sep_get_grid(scw_sep s, double* kx, double* ky, double* z_boundaries);
 SCW_API scw_status scw_sep_set_region_rule(scw_sep s, int rule);
 SCW_API scw_status scw_sep_eval_volume_device(scw_sep s, float x_start, float y_start, float z_start,
                                               float dx, float dy, float dz, int Nx, int Ny, int Nz,
                                               float* dE, int method);
+/* The same volume from HOST amplitudes, end to end (no reference counterpart; the reference
+ * uploads its wave table once in gpu_initialize, gpuEvaluator.cu:15-26, and reads each plane back
+ * in gpu_cw_evaluate, :131-165).  Q_host: [Z][2][3][MF][J] complex64 (per slice the downward then
+ * the upward block, as in the .cwf file but without the even padding); E_host: [Nz][Ny][Nx][3]
+ * complex64.  Slices go up on one stream while the planes of the slices already up are evaluated
+ * on the context stream, and finished planes come back on a third stream; use page-locked host
+ * buffers for full link speed.  The set's device copy of each slice that a grid plane lies in is
+ * overwritten (after the work already queued on the context stream); blocks until E_host is
+ * written. */
+SCW_API scw_status scw_sep_eval_volume_host(scw_sep s, const void* Q_host, float x_start, float y_start,
+                                            float z_start, float dx, float dy, float dz, int Nx, int Ny, int Nz,
+                                            float* E_host, int method);
+/* Planes k_begin .. k_end-1 of the volume above (plane k at z = z_start + dz*k, the value the whole
+ * volume gives it): output [k_end - k_begin][Ny][Nx][3] complex64.  One process per GPU evaluates
+ * its own z-slab this way; the slabs put together are the whole volume.  The host form reads only
+ * the slices its planes lie in from Q_host (still the whole [Z][2][3][MF][J] array). */
+SCW_API scw_status scw_sep_eval_slab_device(scw_sep s, float x_start, float y_start, float z_start, float dx,
+                                            float dy, float dz, int Nx, int Ny, int k_begin, int k_end, float* dE,
+                                            int method);
+SCW_API scw_status scw_sep_eval_slab_host(scw_sep s, const void* Q_host, float x_start, float y_start,
+                                          float z_start, float dx, float dy, float dz, int Nx, int Ny, int k_begin,
+                                          int k_end, float* E_host, int method);
+/* Granularity of scw_sep_eval_volume_host: Q bytes per upload (whole slices, at least one; default
+ * 192 MiB) and output bytes per read-back slab (whole planes, at least one; default 64 MiB; three
+ * slabs are kept on the device).  0 restores a default. */
+SCW_API scw_status scw_sep_set_streaming(scw_sep s, int64_t chunk_bytes, int64_t slab_bytes);
 SCW_API scw_status scw_sep_eval_plane_device(scw_sep s, int axis, float a_start, float b_start, float c,
                                              float d, int N, float* dE, int method);
 SCW_API scw_status scw_sep_gpu_cw_evaluate(scw_sep s, float* E_xy, float* E_xz, float* E_yz,

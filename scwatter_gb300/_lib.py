@@ -108,7 +108,12 @@ _SIGS = {
     "scw_sep_from_cw": [P, P, PP],
     "scw_sep_info": [P, ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32)],
     "scw_sep_set_region_rule": [P, I32],
+    "scw_sep_get_grid": [P, P, P, P],
     "scw_sep_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
+    "scw_sep_eval_volume_host": [P, P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
+    "scw_sep_set_streaming": [P, I64, I64],
+    "scw_sep_eval_slab_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, I32, P, I32],
+    "scw_sep_eval_slab_host": [P, P, F32, F32, F32, F32, F32, F32, I32, I32, I32, I32, P, I32],
     "scw_sep_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P, I32],
     "scw_sep_gpu_cw_evaluate": [P, P, P, P, F32, F32, F32, F32, F32, F32, F32, I32, I32, I32],
     "scw_zgemm": [P, I32, I32, I32, P, P, P, P, P, I32],

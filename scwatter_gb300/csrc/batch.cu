@@ -77,7 +77,7 @@ struct scw_batch_s {
     int tuned = 0;
     std::vector<double> tune_log;  // lanes, method, ms per candidate
     ~scw_batch_s() {
-        if (ctx) cudaSetDevice(ctx->device);
+        ::scw::DeviceScope dev_scope_(ctx ? ctx->device : -1);
         g.reset();
         for (auto c : lane_ctx) scw_ctx_destroy(c);
         for (auto s : lane_stream) cudaStreamDestroy(s);
@@ -271,7 +271,7 @@ scw_status scw_batch_create(scw_ctx ctx, const scw_batch_item* items, int count,
     if (!ctx || !items || count < 1 || !out || lanes < 0 || lanes > 64 || method < 0 || method > 3)
         return fail(SCW_ERR_ARG, "scw_batch_create: bad arguments");
     *out = nullptr;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     std::unique_ptr<scw_batch_s> b(new (std::nothrow) scw_batch_s());
     if (!b) return fail(SCW_ERR_NOMEM, "host allocation");
     b->ctx = ctx;
@@ -431,7 +431,7 @@ scw_status scw_batch_create(scw_ctx ctx, const scw_batch_item* items, int count,
 // One graph launch on the context's stream: every item solved and evaluated.
 scw_status scw_batch_run(scw_batch b) {
     if (!b || !b->g.exec) return fail(SCW_ERR_STATE, "scw_batch_run: no graph");
-    SCW_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    SCW_ON_DEVICE(b->ctx->device);
     SCW_CUDA_TRY(cudaGraphLaunch(b->g.exec, b->ctx->stream));
     b->ctx->launches += b->kernels;
     return SCW_OK;
@@ -441,7 +441,7 @@ scw_status scw_batch_run(scw_batch b) {
 // SCW_ERR_TIMEOUT (a tensor-core wait of the item's lane gave up).
 scw_status scw_batch_wait(scw_batch b, int* item_status) {
     if (!b) return fail(SCW_ERR_ARG, "null batch");
-    SCW_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    SCW_ON_DEVICE(b->ctx->device);
     SCW_CUDA_TRY(cudaStreamSynchronize(b->ctx->stream));
     std::vector<int> lane_err(b->lane_ctx.size(), 0);
     for (size_t l = 0; l < b->lane_ctx.size(); l++)
@@ -470,7 +470,7 @@ scw_status scw_batch_wait(scw_batch b, int* item_status) {
 scw_status scw_batch_get(scw_batch b, int i, double* x, double* gamma, float* field_host, float** field_device) {
     if (!b || i < 0 || i >= (int)b->items.size()) return fail(SCW_ERR_ARG, "scw_batch_get: item out of range");
     const Item& it = b->items[i];
-    SCW_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    SCW_ON_DEVICE(b->ctx->device);
     if (x) SCW_CUDA_TRY(cudaMemcpy(x, it.out.x, sizeof(double2) * 6 * it.sp.MF, cudaMemcpyDeviceToHost));
     if (gamma)
         SCW_CUDA_TRY(cudaMemcpy(gamma, it.out.gam, sizeof(double2) * (size_t)it.sp.Z * it.sp.n, cudaMemcpyDeviceToHost));
@@ -513,7 +513,7 @@ scw_status scw_batch_item_eig(scw_batch b, int i, int* mixed, int* accepted, int
     std::vector<int> st(2 * Z, 0);
     std::vector<double> res(Z, 0.0);
     if (it.out.eig) {
-        SCW_CUDA_TRY(cudaSetDevice(b->ctx->device));
+        SCW_ON_DEVICE(b->ctx->device);
         SCW_CUDA_TRY(cudaMemcpy(st.data(), it.out.eig, sizeof(int) * 2 * Z, cudaMemcpyDeviceToHost));
         SCW_CUDA_TRY(cudaMemcpy(res.data(), it.out.eig_res, sizeof(double) * Z, cudaMemcpyDeviceToHost));
     }

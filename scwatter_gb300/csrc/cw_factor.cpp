@@ -11,6 +11,7 @@
 // M1 x M0 mesh, so kx depends on a = p / M1 and ky on b = p % M1) and kz = gamma_j k.
 // This file checks that structure exactly (equal kx per a, ky per b, kz per j across p)
 // and re-references every amplitude to its own plane in FP64 before rounding to complex64.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -35,6 +36,14 @@ scw_status scw_sep_info(scw_sep s, int* M0, int* M1, int* n_slices, int* modes_p
     if (M1) *M1 = s->M1;
     if (n_slices) *n_slices = s->Z;
     if (modes_per_half) *modes_per_half = s->J;
+    return SCW_OK;
+}
+
+scw_status scw_sep_get_grid(scw_sep s, double* kx, double* ky, double* z_boundaries) {
+    if (!s) return fail(SCW_ERR_ARG, "null separable set");
+    if (kx) std::copy(s->kx.begin(), s->kx.end(), kx);
+    if (ky) std::copy(s->ky.begin(), s->ky.end(), ky);
+    if (z_boundaries) std::copy(s->zb.begin(), s->zb.end(), z_boundaries);
     return SCW_OK;
 }
 

@@ -115,7 +115,7 @@ scw_status scw_ctx_create(int device, void* stream, scw_ctx* out) {
     int n = 0;
     SCW_CUDA_TRY(cudaGetDeviceCount(&n));
     if (device < 0 || device >= n) return fail(SCW_ERR_ARG, "scw_ctx_create: device out of range");
-    SCW_CUDA_TRY(cudaSetDevice(device));
+    SCW_ON_DEVICE(device);
     scw_ctx c = new (std::nothrow) scw_ctx_s();
     if (!c) return fail(SCW_ERR_NOMEM, "scw_ctx_create: host allocation");
     c->device = device;
@@ -148,7 +148,7 @@ scw_status scw_ctx_create(int device, void* stream, scw_ctx* out) {
 
 scw_status scw_ctx_destroy(scw_ctx c) {
     if (!c) return SCW_OK;
-    cudaSetDevice(c->device);
+    ::scw::DeviceScope dev_scope_(c->device);
     cudaStreamSynchronize(c->stream);
     c->scratch.release();
     c->desc.release();

@@ -831,7 +831,7 @@ scw_status scw_zgemm(scw_ctx ctx, int M, int N, int K, const double* alpha, cons
                      const double* beta, void* C, int batch) {
     if (!ctx || !A || !B || !C || !alpha || !beta || M < 0 || N < 0 || K < 0 || batch < 1)
         return fail(SCW_ERR_ARG, "scw_zgemm: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     ctx->launches++;
     return scw::zgemm(ctx->stream, M, N, K, make_double2(alpha[0], alpha[1]), (const double2*)A, K, (long long)M * K,
                       (const double2*)B, N, (long long)K * N, make_double2(beta[0], beta[1]), (double2*)C, N,
@@ -840,7 +840,7 @@ scw_status scw_zgemm(scw_ctx ctx, int M, int N, int K, const double* alpha, cons
 
 scw_status scw_zgesv(scw_ctx ctx, int n, int nrhs, void* A, void* B, int batch, int* info_host) {
     if (!ctx || !A || !B || n < 1 || nrhs < 1 || batch < 1) return fail(SCW_ERR_ARG, "scw_zgesv: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     int* dpiv = nullptr;
     int* dinfo = nullptr;
     if (cudaMalloc(&dpiv, sizeof(int) * (size_t)n * batch) != cudaSuccess ||
@@ -872,7 +872,7 @@ scw_status scw_zgesv(scw_ctx ctx, int n, int nrhs, void* A, void* B, int batch, 
 
 scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* status_host) {
     if (!ctx || !A || !W || !V || n < 1 || batch < 1) return fail(SCW_ERR_ARG, "scw_zgeev: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     double2* work = nullptr;
     int* dst = nullptr;
     const size_t wbytes = sizeof(double2) * ((size_t)n * n + 3 * (size_t)n) * batch;
@@ -901,7 +901,7 @@ scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, i
 
 scw_status scw_cgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* status_host) {
     if (!ctx || !A || !W || !V || n < 1 || batch < 1) return fail(SCW_ERR_ARG, "scw_cgeev: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     float2* work = nullptr;
     int* dst = nullptr;
     const size_t wbytes = sizeof(float2) * ((size_t)n * n + 3 * (size_t)n) * batch;

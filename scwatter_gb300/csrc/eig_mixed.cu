@@ -681,7 +681,7 @@ extern "C" scw_status scw_zgeev_mixed(scw_ctx ctx, int n, void* A, void* W, void
     using namespace scw;
     if (!ctx || !A || !W || !V || n < 1 || batch < 1) return fail(SCW_ERR_ARG, "scw_zgeev_mixed: bad arguments");
     if (n > mx::kMaxN) return fail(SCW_ERR_ARG, "scw_zgeev_mixed: n above 4096");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const size_t nn = (size_t)n * n;
     // FP64 fallback work (>= 2 Z n^2 + 4 Z n float2 for S0, S1, hw, lam32), W region (S2, S3), small buffers
     const size_t pbytes = sizeof(double2) * (nn + 3 * (size_t)n) * batch;

@@ -387,7 +387,7 @@ static void plan_planes(const scw_waves_s* w, const std::vector<PlaneGeom>& plan
 
 static scw_status launch_planes(scw_waves w, std::vector<PlaneGeom>& planes) {
     scw_ctx ctx = w->ctx;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     Plan P;
     plan_planes(w, planes, ctx->sm_count, P);
     if (P.items.empty()) return SCW_OK;
@@ -443,7 +443,7 @@ static scw_status launch_planes(scw_waves w, std::vector<PlaneGeom>& planes) {
 scw_status waves_upload(scw_waves w, const std::vector<double>& kre, const std::vector<double>& kim,
                         const std::vector<double>& zref, const std::vector<float2>& amp) {
     scw_ctx ctx = w->ctx;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const size_t n = (size_t)w->n;
     if (n == 0) return SCW_OK;
     if (cudaMalloc(&w->kre, 3 * n * sizeof(double)) != cudaSuccess ||
@@ -465,7 +465,7 @@ using scw::fail;
 
 static void free_waves(scw_waves w) {
     if (!w) return;
-    if (w->ctx) cudaSetDevice(w->ctx->device);
+    ::scw::DeviceScope dev_scope_(w->ctx ? w->ctx->device : -1);
     if (w->kre) cudaFree(w->kre);
     if (w->kim) cudaFree(w->kim);
     if (w->zref) cudaFree(w->zref);
@@ -629,7 +629,7 @@ scw_status scw_gpu_cw_evaluate(scw_waves w, float* E_xy, float* E_xz, float* E_y
     scw_ctx ctx = w->ctx;
     if (device != ctx->device)
         return fail(SCW_ERR_ARG, "scw_gpu_cw_evaluate: device differs from the wave set's device");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const size_t plane_floats = (size_t)N * N * 6;
     scw_status st = ctx->planes_out.reserve(3 * plane_floats * sizeof(float));
     if (st != SCW_OK) return st;
@@ -662,7 +662,6 @@ scw_status scw_gpu_cw_evaluate(scw_waves w, float* E_xy, float* E_xz, float* E_y
 // parameters, and calls no cudaMalloc, cudaMallocHost, cudaFree or allocating library
 // routine.
 // ------------------------------------------------------------------------------------
-#include <mutex>
 
 namespace scw {
 
@@ -852,26 +851,19 @@ plain_reduce_static_kernel(PlaneGeom g, int tiles_i, int split, const float* __r
     }
 }
 
-// Device address of g_static_partials, looked up once per device with that device current.
-// The first lookup on a device may load this library's GPU module there.
-constexpr int kStaticMaxDevices = 64;
-static std::mutex g_static_mu;
-static float* g_static_ptr[kStaticMaxDevices] = {};
-
-static scw_status static_scratch(int device, float** out) {
-    if (device < 0 || device >= kStaticMaxDevices)
-        return fail(SCW_ERR_ARG, "scw_eval_plane_device_static: device ordinal beyond " +
-                                     std::to_string(kStaticMaxDevices - 1));
-    std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_ptr[device]) {
+// Device address of g_static_partials as seen from the context's device, looked up once per
+// context with that device current (the first lookup may load this library's GPU module
+// there) and kept in the context.  A context made after a cudaDeviceReset looks it up afresh.
+static scw_status static_scratch(scw_ctx ctx, float** out) {
+    if (!ctx->static_scratch) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_static_partials);
         if (e != cudaSuccess || !p)
             return fail(SCW_ERR_CUDA, std::string("cudaGetSymbolAddress of the static scratch array: ") +
                                           cudaGetErrorString(e));
-        g_static_ptr[device] = (float*)p;
+        ctx->static_scratch = p;
     }
-    *out = g_static_ptr[device];
+    *out = (float*)ctx->static_scratch;
     return SCW_OK;
 }
 
@@ -891,9 +883,9 @@ scw_status scw_eval_plane_device_static(scw_waves w, int axis, float a_start, fl
         return fail(SCW_ERR_ARG, "scw_eval_plane_device_static: " + std::to_string(w->layers) +
                                      " layers exceed the maximum of " + std::to_string(kStaticMaxLayers));
     scw_ctx ctx = w->ctx;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     float* scratch = nullptr;
-    scw_status st = static_scratch(ctx->device, &scratch);
+    scw_status st = static_scratch(ctx, &scratch);
     if (st != SCW_OK) return st;
 
     StaticRegions R;

@@ -512,10 +512,30 @@ scw_status sep_synth(scw_ctx ctx, const float2* T, const float2* F, int nrows, i
     return SCW_OK;
 }
 
-// One evaluation "sheet" family: a volume of xy planes, or an xz / yz plane.  Host-only plan.
-scw_status sep_eval_plan(const scw_sep_s* s, int kind, float a0, float b0, float c, float da, float db, float dz,
-                         int Na, int Nb, int Nz, int method, SepEvalPlan& p) {
+// Sizes and stage-1 grouping of a plan whose kind, geometry and z-list are set.
+static scw_status sep_plan_finish(const scw_sep_s* s, SepEvalPlan& p) {
     const int M0 = s->M0, M1 = s->M1, MF = s->MF;
+    const int nz = (int)p.zlist.size();
+    if (p.kind == 0) { p.nrows = p.Nz * p.Nb; p.ncols = p.Na; p.Mk = M0; }
+    else if (p.kind == 1) { p.nrows = p.Nb; p.ncols = p.Na; p.Mk = M0; }
+    else { p.nrows = p.Nb; p.ncols = p.Na; p.Mk = M1; }
+    if (p.kind == 0) {
+        const size_t smem = (size_t)(3 * M0 * M1 + kRowsBlk * M1) * sizeof(float2);
+        if (smem > 200 * 1024) return fail(SCW_ERR_UNSUPPORTED, "harmonic grid too large for the row stage");
+    }
+    // phases for the PGroups: at most nz groups
+    p.phi_bytes = align256((size_t)nz * 2 * (size_t)s->Jp * kMaxGroup * sizeof(float2));
+    p.c_bytes = align256((size_t)nz * 3 * MF * sizeof(float2));
+    // slack past the last row: the tensor-core producer reads whole 16-row tiles of T
+    p.t_bytes = align256((size_t)p.nrows * 3 * p.Mk * sizeof(float2) + 16 * 3 * 64 * sizeof(float2) + 4096);
+    p.tab_bytes = align256((size_t)(M0 + M1) * (p.Na + p.Nb + 2) * sizeof(float2));
+    p.scratch_bytes = p.phi_bytes + p.c_bytes + p.t_bytes + 2 * p.tab_bytes;
+    stage1_plan(s, p);
+    return SCW_OK;
+}
+
+static void sep_plan_geom(SepEvalPlan& p, int kind, float a0, float b0, float c, float da, float db, float dz, int Na,
+                          int Nb, int Nz, int method) {
     p.kind = kind;
     p.a0 = a0;
     p.b0 = b0;
@@ -528,29 +548,32 @@ scw_status sep_eval_plan(const scw_sep_s* s, int kind, float a0, float b0, float
     p.Nz = Nz;
     p.method = method;
     p.zlist.clear();
+}
+
+// One evaluation "sheet" family: a volume of xy planes, or an xz / yz plane.  Host-only plan.
+scw_status sep_eval_plan(const scw_sep_s* s, int kind, float a0, float b0, float c, float da, float db, float dz,
+                         int Na, int Nb, int Nz, int method, SepEvalPlan& p) {
+    sep_plan_geom(p, kind, a0, b0, c, da, db, dz, Na, Nb, Nz, method);
     if (kind == 0) {            // volume: Nz xy planes at z = c + dz*k; a = x (Na), b = y (Nb)
         for (int k = 0; k < Nz; k++) p.zlist.push_back(host_coord(c, dz, k));
     } else {                    // kind 1: xz plane at y = c (a = x, rows = z); kind 2: yz plane at x = c (a = y)
         for (int k = 0; k < Nb; k++) p.zlist.push_back(host_coord(b0, db, k));
     }
-    const int nz = (int)p.zlist.size();
-    if (kind == 0) { p.nrows = Nz * Nb; p.ncols = Na; p.Mk = M0; }
-    else if (kind == 1) { p.nrows = Nb; p.ncols = Na; p.Mk = M0; }
-    else { p.nrows = Nb; p.ncols = Na; p.Mk = M1; }
-    if (kind == 0) {
-        const size_t smem = (size_t)(3 * M0 * M1 + kRowsBlk * M1) * sizeof(float2);
-        if (smem > 200 * 1024) return fail(SCW_ERR_UNSUPPORTED, "harmonic grid too large for the row stage");
-    }
-    // phases for the PGroups: at most nz groups
-    p.phi_bytes = align256((size_t)nz * 2 * (size_t)s->Jp * kMaxGroup * sizeof(float2));
-    p.c_bytes = align256((size_t)nz * 3 * MF * sizeof(float2));
-    // slack past the last row: the tensor-core producer reads whole 16-row tiles of T
-    p.t_bytes = align256((size_t)p.nrows * 3 * p.Mk * sizeof(float2) + 16 * 3 * 64 * sizeof(float2) + 4096);
-    p.tab_bytes = align256((size_t)(M0 + M1) * (Na + Nb + 2) * sizeof(float2));
-    p.scratch_bytes = p.phi_bytes + p.c_bytes + p.t_bytes + 2 * p.tab_bytes;
-    stage1_plan(s, p);
-    return SCW_OK;
+    return sep_plan_finish(s, p);
 }
+
+// Plan of the xy planes k0 .. k1-1 of the volume (x_start, y_start, z_start, dx, dy, dz): the
+// planes keep the z-values the whole volume's plan gives them.
+static scw_status sep_eval_plan_planes(const scw_sep_s* s, float a0, float b0, float z_start, float da, float db,
+                                       float dz, int Na, int Nb, int k0, int k1, int method, SepEvalPlan& p) {
+    sep_plan_geom(p, 0, a0, b0, z_start, da, db, dz, Na, Nb, k1 - k0, method);
+    for (int k = k0; k < k1; k++) p.zlist.push_back(host_coord(z_start, dz, k));
+    return sep_plan_finish(s, p);
+}
+
+// Planes k_begin .. k_end-1 of a volume into device memory, with the z-values the whole volume has.
+scw_status sep_eval_slab(scw_sep s, float x0, float y0, float z0, float dx, float dy, float dz, int Nx, int Ny,
+                         int k_begin, int k_end, float* dE, int method);
 
 // Launches of one planned evaluation (no allocation, no host synchronisation).
 scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, char* scratch, float* dE) {
@@ -601,12 +624,162 @@ scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, 
 scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, float db, float dz, int Na, int Nb,
                     int Nz, float* dE, int method) {
     scw_ctx ctx = s->ctx;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     SepEvalPlan p;
     scw_status st = sep_eval_plan(s, kind, a0, b0, c, da, db, dz, Na, Nb, Nz, method, p);
     if (st != SCW_OK) return st;
     if ((st = ctx->sep_scratch.reserve(p.scratch_bytes)) != SCW_OK) return st;
     // descriptors to the device (pinned staging, guarded by the context's event)
+    SCW_CUDA_TRY(cudaEventSynchronize(ctx->desc_done));
+    if ((st = ctx->host_desc.reserve(p.desc_bytes)) != SCW_OK) return st;
+    if ((st = ctx->desc.reserve(p.desc_bytes)) != SCW_OK) return st;
+    sep_eval_desc(p, (char*)ctx->host_desc.ptr);
+    SCW_CUDA_TRY(cudaMemcpyAsync(ctx->desc.ptr, ctx->host_desc.ptr, p.desc_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    SCW_CUDA_TRY(cudaEventRecord(ctx->desc_done, ctx->stream));
+    return sep_eval_record(s, p, (const char*)ctx->desc.ptr, (char*)ctx->sep_scratch.ptr, dE);
+}
+
+
+// ------------------------------------------------------------------------------------
+// Host-streamed volume evaluation: the interior amplitudes come from host memory on every
+// call.  Three streams overlap the link and the kernels: slices go up on the set's upload
+// stream, each run of planes is evaluated on the context stream as soon as its slices are
+// in, and each finished slab of planes goes down on the set's download stream.
+// ------------------------------------------------------------------------------------
+constexpr int kSlabSlots = 3;                         // output slabs in flight
+constexpr size_t kSlabTarget = 64ull << 20;           // default bytes of output per run (at least one plane)
+constexpr size_t kChunkTarget = 192ull << 20;         // default bytes of Q per upload chunk (at least one slice)
+
+static scw_status stream_res(scw_sep s, size_t n_events, size_t slab_bytes) {
+    if (!s->up_stream) SCW_CUDA_TRY(cudaStreamCreateWithFlags(&s->up_stream, cudaStreamNonBlocking));
+    if (!s->down_stream) SCW_CUDA_TRY(cudaStreamCreateWithFlags(&s->down_stream, cudaStreamNonBlocking));
+    while (s->events.size() < n_events) {
+        cudaEvent_t e;
+        SCW_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        s->events.push_back(e);
+    }
+    if (s->slab_bytes < slab_bytes) {
+        if (s->dslab) cudaFree(s->dslab);
+        s->dslab = nullptr;
+        s->slab_bytes = 0;
+        if (cudaMalloc(&s->dslab, slab_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SCW_ERR_NOMEM, "cudaMalloc of the output slabs");
+        }
+        s->slab_bytes = slab_bytes;
+    }
+    return SCW_OK;
+}
+
+struct StreamRun {
+    int k0, k1;      // planes of the volume
+    int chunk;       // upload chunk the run waits for (-1: exterior planes, no amplitudes needed)
+};
+
+// planes k_begin .. k_end-1 of the volume into Eh (plane k at Eh + (k - k_begin) planes)
+scw_status sep_eval_volume_host(scw_sep s, const float2* Qh, float x0, float y0, float z0, float dx, float dy,
+                                float dz, int Nx, int Ny, int k_begin, int k_end, float* Eh, int method) {
+    scw_ctx ctx = s->ctx;
+    SCW_ON_DEVICE(ctx->device);
+    const size_t plane_bytes = (size_t)Nx * Ny * 6 * sizeof(float);
+    const size_t J = (size_t)s->J, Jp = (size_t)s->Jp, MF = (size_t)s->MF;
+    const size_t slice_bytes = 2 * 3 * MF * J * sizeof(float2);          // host layout [2][3][MF][J]
+    const size_t chunk_target = s->chunk_bytes > 0 ? s->chunk_bytes : kChunkTarget;
+    const size_t slab_target = s->slab_target > 0 ? s->slab_target : kSlabTarget;
+    const int per_chunk = (int)std::max<size_t>(1, chunk_target / std::max<size_t>(slice_bytes, 1));
+    const int max_run = (int)std::max<size_t>(1, slab_target / plane_bytes);
+    // runs: consecutive planes in the same upload chunk, at most max_run planes each
+    std::vector<StreamRun> runs;
+    for (int k = k_begin; k < k_end; k++) {
+        const int64_t r = sep_region(s, host_coord(z0, dz, k));
+        const int ch = (r == 0 || r == s->Z + 1 || J == 0) ? -1 : (int)((r - 1) / per_chunk);
+        if (!runs.empty() && runs.back().chunk == ch && runs.back().k1 == k && k - runs.back().k0 < max_run)
+            runs.back().k1 = k + 1;
+        else
+            runs.push_back(StreamRun{k, k + 1, ch});
+    }
+    // chunks in the order the runs first need them
+    const int n_chunks = s->Z > 0 ? (s->Z + per_chunk - 1) / per_chunk : 0;
+    std::vector<int> order, ev_up(n_chunks, -1);
+    for (const auto& rn : runs)
+        if (rn.chunk >= 0 && ev_up[rn.chunk] < 0) {
+            ev_up[rn.chunk] = (int)order.size();
+            order.push_back(rn.chunk);
+        }
+    // plans and their descriptors (all uploaded at once, before the first launch)
+    std::vector<SepEvalPlan> plans(runs.size());
+    std::vector<size_t> desc_off(runs.size());
+    size_t desc_total = 0, scratch = 0;
+    int max_planes = 1;
+    for (size_t i = 0; i < runs.size(); i++) {
+        scw_status st = sep_eval_plan_planes(s, x0, y0, z0, dx, dy, dz, Nx, Ny, runs[i].k0, runs[i].k1, method,
+                                             plans[i]);
+        if (st != SCW_OK) return st;
+        desc_off[i] = desc_total;
+        desc_total += align256(plans[i].desc_bytes);
+        scratch = std::max(scratch, plans[i].scratch_bytes);
+        max_planes = std::max(max_planes, runs[i].k1 - runs[i].k0);
+    }
+    const size_t slab = align256((size_t)max_planes * plane_bytes);
+    // events: [0] start, then one per chunk upload, then computed / downloaded per run
+    const size_t n_ev = 1 + order.size() + 2 * runs.size();
+    scw_status st = stream_res(s, n_ev, kSlabSlots * slab);
+    if (st != SCW_OK) return st;
+    if ((st = ctx->sep_scratch.reserve(scratch)) != SCW_OK) return st;
+    SCW_CUDA_TRY(cudaEventSynchronize(ctx->desc_done));
+    if ((st = ctx->host_desc.reserve(desc_total)) != SCW_OK) return st;
+    if ((st = ctx->desc.reserve(desc_total)) != SCW_OK) return st;
+    for (size_t i = 0; i < runs.size(); i++) sep_eval_desc(plans[i], (char*)ctx->host_desc.ptr + desc_off[i]);
+    SCW_CUDA_TRY(cudaMemcpyAsync(ctx->desc.ptr, ctx->host_desc.ptr, desc_total, cudaMemcpyHostToDevice, ctx->stream));
+    SCW_CUDA_TRY(cudaEventRecord(ctx->desc_done, ctx->stream));
+    cudaEvent_t* ev = s->events.data();
+    cudaEvent_t* ev_chunk = ev + 1;
+    cudaEvent_t* ev_comp = ev + 1 + order.size();
+    cudaEvent_t* ev_down = ev_comp + runs.size();
+    // the amplitudes on the device are overwritten only after the work queued before this call
+    SCW_CUDA_TRY(cudaEventRecord(ev[0], ctx->stream));
+    SCW_CUDA_TRY(cudaStreamWaitEvent(s->up_stream, ev[0], 0));
+    SCW_CUDA_TRY(cudaStreamWaitEvent(s->down_stream, ev[0], 0));
+    for (size_t c = 0; c < order.size(); c++) {
+        const int l0 = order[c] * per_chunk, l1 = std::min(s->Z, l0 + per_chunk);
+        for (int l = l0; l < l1; l++) {
+            const float2* src = Qh + (size_t)l * 2 * 3 * MF * J;
+            float2* dst = s->dQ + (size_t)l * 2 * 3 * MF * Jp;
+            if (J == Jp)
+                SCW_CUDA_TRY(cudaMemcpyAsync(dst, src, slice_bytes, cudaMemcpyHostToDevice, s->up_stream));
+            else
+                SCW_CUDA_TRY(cudaMemcpy2DAsync(dst, Jp * sizeof(float2), src, J * sizeof(float2), J * sizeof(float2),
+                                               2 * 3 * MF, cudaMemcpyHostToDevice, s->up_stream));
+        }
+        SCW_CUDA_TRY(cudaEventRecord(ev_chunk[c], s->up_stream));
+    }
+    const char* d_desc = (const char*)ctx->desc.ptr;
+    for (size_t i = 0; i < runs.size(); i++) {
+        if (runs[i].chunk >= 0) SCW_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ev_chunk[ev_up[runs[i].chunk]], 0));
+        if (i >= (size_t)kSlabSlots) SCW_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ev_down[i - kSlabSlots], 0));
+        float* slot = (float*)((char*)s->dslab + (i % kSlabSlots) * slab);
+        if ((st = sep_eval_record(s, plans[i], d_desc + desc_off[i], (char*)ctx->sep_scratch.ptr, slot)) != SCW_OK)
+            return st;
+        SCW_CUDA_TRY(cudaEventRecord(ev_comp[i], ctx->stream));
+        SCW_CUDA_TRY(cudaStreamWaitEvent(s->down_stream, ev_comp[i], 0));
+        SCW_CUDA_TRY(cudaMemcpyAsync((char*)Eh + (size_t)(runs[i].k0 - k_begin) * plane_bytes, slot,
+                                     (size_t)(runs[i].k1 - runs[i].k0) * plane_bytes, cudaMemcpyDeviceToHost,
+                                     s->down_stream));
+        SCW_CUDA_TRY(cudaEventRecord(ev_down[i], s->down_stream));
+    }
+    SCW_CUDA_TRY(cudaStreamSynchronize(s->down_stream));
+    SCW_CUDA_TRY(cudaStreamSynchronize(s->up_stream));
+    return scw_ctx_synchronize(ctx);
+}
+
+scw_status sep_eval_slab(scw_sep s, float x0, float y0, float z0, float dx, float dy, float dz, int Nx, int Ny,
+                         int k_begin, int k_end, float* dE, int method) {
+    scw_ctx ctx = s->ctx;
+    SCW_ON_DEVICE(ctx->device);
+    SepEvalPlan p;
+    scw_status st = sep_eval_plan_planes(s, x0, y0, z0, dx, dy, dz, Nx, Ny, k_begin, k_end, method, p);
+    if (st != SCW_OK) return st;
+    if ((st = ctx->sep_scratch.reserve(p.scratch_bytes)) != SCW_OK) return st;
     SCW_CUDA_TRY(cudaEventSynchronize(ctx->desc_done));
     if ((st = ctx->host_desc.reserve(p.desc_bytes)) != SCW_OK) return st;
     if ((st = ctx->desc.reserve(p.desc_bytes)) != SCW_OK) return st;
@@ -625,13 +798,17 @@ using scw::fail;
 // ------------------------------------------------------------------------------------
 static void sep_free(scw_sep s) {
     if (!s) return;
-    if (s->ctx) cudaSetDevice(s->ctx->device);
+    ::scw::DeviceScope dev_scope_(s->ctx ? s->ctx->device : -1);
     if (s->dQ && s->own_Q) cudaFree(s->dQ);
     if (s->dKz) cudaFree(s->dKz);
     if (s->dExt) cudaFree(s->dExt);
     if (s->dkx) cudaFree(s->dkx);
     if (s->dky) cudaFree(s->dky);
     if (s->dzb) cudaFree(s->dzb);
+    if (s->dslab) cudaFree(s->dslab);
+    for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+    if (s->up_stream) cudaStreamDestroy(s->up_stream);
+    if (s->down_stream) cudaStreamDestroy(s->down_stream);
     delete s;
 }
 
@@ -642,7 +819,7 @@ scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_p
     if (!ctx || !out || M0 <= 0 || M1 <= 0 || n_slices < 0 || modes_per_half < 0 || !kx || !ky || !z_boundaries)
         return fail(SCW_ERR_ARG, "scw_sep_create: bad arguments");
     *out = nullptr;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     scw_sep s = new (std::nothrow) scw_sep_s();
     if (!s) return fail(SCW_ERR_NOMEM, "host allocation");
     s->ctx = ctx;
@@ -703,7 +880,7 @@ scw_status scw_sep_set_exterior(scw_sep s, const double* inc, const double* kz_i
     std::memcpy(h.data() + 18 * MF, kz_inc, 2 * MF * 8);
     std::memcpy(h.data() + 20 * MF, kz_refl, 2 * MF * 8);
     std::memcpy(h.data() + 22 * MF, kz_trans, 2 * MF * 8);
-    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    SCW_ON_DEVICE(s->ctx->device);
     SCW_CUDA_TRY(cudaMemcpy(s->dExt, h.data(), 24 * MF * 8, cudaMemcpyHostToDevice));
     return SCW_OK;
 }
@@ -743,7 +920,7 @@ scw_status scw_sep_set_slice(scw_sep s, int l, const double* kz_dn, const double
     const size_t J = (size_t)s->J, MF = (size_t)s->MF;
     if (J == 0) return SCW_OK;
     if (!kz_dn || !Q_dn || !kz_up || !Q_up) return fail(SCW_ERR_ARG, "scw_sep_set_slice: null argument");
-    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    SCW_ON_DEVICE(s->ctx->device);
     scw_status st = upload_kz(s, l, kz_dn, kz_up);
     if (st != SCW_OK) return st;
     std::vector<float2> q(3 * MF * J);
@@ -760,7 +937,7 @@ scw_status scw_sep_set_slice_device(scw_sep s, int l, const double* kz_dn, const
     if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_sep_set_slice_device: slice out of range");
     if (s->J == 0) return SCW_OK;
     if (!kz_dn || !Q_dn_c64 || !kz_up || !Q_up_c64) return fail(SCW_ERR_ARG, "scw_sep_set_slice_device: null argument");
-    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    SCW_ON_DEVICE(s->ctx->device);
     scw_status st = upload_kz(s, l, kz_dn, kz_up);
     if (st != SCW_OK) return st;
     if ((st = upload_q(s, l, 0, Q_dn_c64, cudaMemcpyDefault, true)) != SCW_OK) return st;
@@ -779,6 +956,37 @@ scw_status scw_sep_eval_volume_device(scw_sep s, float x_start, float y_start, f
     return scw::sep_eval(s, 0, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, Nz, dE, method);
 }
 
+scw_status scw_sep_eval_volume_host(scw_sep s, const void* Q_host, float x_start, float y_start, float z_start,
+                                    float dx, float dy, float dz, int Nx, int Ny, int Nz, float* E_host, int method) {
+    if (!s || !E_host || Nx <= 0 || Ny <= 0 || Nz <= 0 || (s->J > 0 && !Q_host))
+        return fail(SCW_ERR_ARG, "scw_sep_eval_volume_host: bad arguments");
+    return scw::sep_eval_volume_host(s, (const float2*)Q_host, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, 0, Nz,
+                                     E_host, method);
+}
+
+scw_status scw_sep_eval_slab_host(scw_sep s, const void* Q_host, float x_start, float y_start, float z_start, float dx,
+                                  float dy, float dz, int Nx, int Ny, int k_begin, int k_end, float* E_host,
+                                  int method) {
+    if (!s || !E_host || Nx <= 0 || Ny <= 0 || k_begin < 0 || k_end <= k_begin || (s->J > 0 && !Q_host))
+        return fail(SCW_ERR_ARG, "scw_sep_eval_slab_host: bad arguments");
+    return scw::sep_eval_volume_host(s, (const float2*)Q_host, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, k_begin,
+                                     k_end, E_host, method);
+}
+
+scw_status scw_sep_eval_slab_device(scw_sep s, float x_start, float y_start, float z_start, float dx, float dy,
+                                    float dz, int Nx, int Ny, int k_begin, int k_end, float* dE, int method) {
+    if (!s || !dE || Nx <= 0 || Ny <= 0 || k_begin < 0 || k_end <= k_begin)
+        return fail(SCW_ERR_ARG, "scw_sep_eval_slab_device: bad arguments");
+    return scw::sep_eval_slab(s, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, k_begin, k_end, dE, method);
+}
+
+scw_status scw_sep_set_streaming(scw_sep s, int64_t chunk_bytes, int64_t slab_bytes) {
+    if (!s || chunk_bytes < 0 || slab_bytes < 0) return fail(SCW_ERR_ARG, "scw_sep_set_streaming: bad arguments");
+    s->chunk_bytes = (size_t)chunk_bytes;
+    s->slab_target = (size_t)slab_bytes;
+    return SCW_OK;
+}
+
 scw_status scw_sep_eval_plane_device(scw_sep s, int axis, float a_start, float b_start, float c, float d, int N,
                                      float* dE, int method) {
     if (!s || !dE || N <= 0 || axis < 0 || axis > 2) return fail(SCW_ERR_ARG, "scw_sep_eval_plane_device: bad arguments");
@@ -792,7 +1000,7 @@ scw_status scw_sep_gpu_cw_evaluate(scw_sep s, float* E_xy, float* E_xz, float* E
     if (!s || !E_xy || !E_xz || !E_yz || N <= 0) return fail(SCW_ERR_ARG, "scw_sep_gpu_cw_evaluate: bad arguments");
     scw_ctx ctx = s->ctx;
     if (device != ctx->device) return fail(SCW_ERR_ARG, "scw_sep_gpu_cw_evaluate: device differs from the set's device");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const size_t plane = (size_t)N * N * 6;
     scw_status st = ctx->planes_out.reserve(3 * plane * sizeof(float));
     if (st != SCW_OK) return st;

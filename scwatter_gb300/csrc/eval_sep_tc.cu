@@ -523,7 +523,8 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     if (!ctx->tc_err) {
         if (cudaMalloc(&ctx->tc_err, sizeof(int)) != cudaSuccess) return fail(SCW_ERR_NOMEM, "cudaMalloc error flag");
     }
-    SCW_CUDA_TRY(cudaMemsetAsync(ctx->tc_err, 0, sizeof(int), ctx->stream));
+    // cleared once per synchronisation: a flag raised by an earlier launch stays raised
+    if (!ctx->tc_pending_check) SCW_CUDA_TRY(cudaMemsetAsync(ctx->tc_err, 0, sizeof(int), ctx->stream));
     const int xt = (ncols + tc::kM - 1) / tc::kM;
     const int ntiles = (nrows + tc::kRows - 1) / tc::kRows;
     int yt = std::max(1, ctx->sm_count / xt);

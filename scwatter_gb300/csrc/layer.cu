@@ -207,7 +207,7 @@ scw_status scw_layer_solve(scw_ctx ctx, int L, const double* ri, const double* z
                            const double* waves, double* x, int* info) {
     if (!ctx || L < 2 || L > 16 || !ri || !z || count < 1 || !waves || !x || !info)
         return fail(SCW_ERR_ARG, "scw_layer_solve: bad arguments (2 <= L <= 16)");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const int N = 6 * L;
     // sub-buffers at 256-byte offsets (double2 needs 16-byte alignment whatever L is)
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };

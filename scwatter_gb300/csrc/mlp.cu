@@ -146,7 +146,7 @@ struct scw_mlp_s {
     float *H1 = nullptr, *H2 = nullptr, *Y = nullptr, *dY = nullptr, *dH2 = nullptr, *dH1 = nullptr;
     double* sums = nullptr;
     ~scw_mlp_s() {
-        if (ctx) cudaSetDevice(ctx->device);
+        ::scw::DeviceScope dev_scope_(ctx ? ctx->device : -1);
         for (void* p : {(void*)P, (void*)G, (void*)Mv, (void*)Vv, (void*)H1, (void*)H2, (void*)Y, (void*)dY,
                         (void*)dH2, (void*)dH1, (void*)sums})
             cudaFree(p);
@@ -252,7 +252,7 @@ extern "C" {
 scw_status scw_mlp_create(scw_ctx ctx, int n_in, int width, int n_out, uint64_t seed, scw_mlp* out) {
     if (!ctx || !out || n_in < 1 || width < 1 || n_out < 1) return fail(SCW_ERR_ARG, "scw_mlp_create: bad arguments");
     *out = nullptr;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     scw_mlp m = new (std::nothrow) scw_mlp_s();
     if (!m) return fail(SCW_ERR_NOMEM, "host allocation");
     m->ctx = ctx;
@@ -307,7 +307,7 @@ scw_status scw_mlp_info(scw_mlp m, int* n_in, int* width, int* n_out, int64_t* n
 // parameters as one host vector: W1 [width][n_in], b1, W2 [width][width], b2, W3 [n_out][width], b3
 scw_status scw_mlp_get_params(scw_mlp m, float* host) {
     if (!m || !host) return fail(SCW_ERR_ARG, "null argument");
-    SCW_CUDA_TRY(cudaSetDevice(m->ctx->device));
+    SCW_ON_DEVICE(m->ctx->device);
     SCW_CUDA_TRY(cudaStreamSynchronize(m->ctx->stream));
     SCW_CUDA_TRY(cudaMemcpy(host, m->P, sizeof(float) * m->n_par, cudaMemcpyDeviceToHost));
     return SCW_OK;
@@ -315,7 +315,7 @@ scw_status scw_mlp_get_params(scw_mlp m, float* host) {
 
 scw_status scw_mlp_set_params(scw_mlp m, const float* host) {
     if (!m || !host) return fail(SCW_ERR_ARG, "null argument");
-    SCW_CUDA_TRY(cudaSetDevice(m->ctx->device));
+    SCW_ON_DEVICE(m->ctx->device);
     SCW_CUDA_TRY(cudaStreamSynchronize(m->ctx->stream));
     SCW_CUDA_TRY(cudaMemcpy(m->P, host, sizeof(float) * m->n_par, cudaMemcpyHostToDevice));
     return SCW_OK;
@@ -324,7 +324,7 @@ scw_status scw_mlp_set_params(scw_mlp m, const float* host) {
 // Y (device, [B][n_out]) from X (device, [B][n_in]); asynchronous
 scw_status scw_mlp_forward(scw_mlp m, const float* X, int B, float* Y) {
     if (!m || !X || !Y || B < 1) return fail(SCW_ERR_ARG, "scw_mlp_forward: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(m->ctx->device));
+    SCW_ON_DEVICE(m->ctx->device);
     scw_status s = reserve(m, B);
     if (s != SCW_OK) return s;
     return forward(m, X, B, Y);
@@ -333,7 +333,7 @@ scw_status scw_mlp_forward(scw_mlp m, const float* X, int B, float* Y) {
 // gradients of the mean squared error over the batch (device X, T) into host grad (n_params)
 scw_status scw_mlp_gradients(scw_mlp m, const float* X, const float* T, int B, float* grad_host, double* loss) {
     if (!m || !X || !T || B < 1) return fail(SCW_ERR_ARG, "scw_mlp_gradients: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(m->ctx->device));
+    SCW_ON_DEVICE(m->ctx->device);
     scw_status s = reserve(m, B);
     if (s != SCW_OK) return s;
     if ((s = backward(m, X, T, B, loss)) != SCW_OK) return s;
@@ -347,7 +347,7 @@ scw_status scw_mlp_gradients(scw_mlp m, const float* X, const float* T, int B, f
 // one Adam step on the batch; loss (before the step) to *loss if not null
 scw_status scw_mlp_train_step(scw_mlp m, const float* X, const float* T, int B, float lr, double* loss) {
     if (!m || !X || !T || B < 1 || !(lr > 0)) return fail(SCW_ERR_ARG, "scw_mlp_train_step: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(m->ctx->device));
+    SCW_ON_DEVICE(m->ctx->device);
     scw_status s = reserve(m, B);
     if (s != SCW_OK) return s;
     if ((s = backward(m, X, T, B, loss)) != SCW_OK) return s;

@@ -116,7 +116,7 @@ scw_status scw_gen_spheres(scw_ctx ctx, int Z, int Y, int X, int n_spheres, cons
     if (!ctx || Z < 1 || Y < 1 || X < 1 || n_spheres < 0 || (n_spheres > 0 && !spheres) || !n_background ||
         !n_sphere || !out)
         return fail(SCW_ERR_ARG, "scw_gen_spheres: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     double* d = nullptr;
     SCW_CUDA_TRY(cudaMallocAsync(&d, sizeof(double) * 4 * (size_t)(n_spheres + 1), ctx->stream));
     if (n_spheres > 0)
@@ -137,7 +137,7 @@ scw_status scw_gen_grf(scw_ctx ctx, int Z, int Y, int X, double corr_px, double 
                        uint64_t seed, void* out) {
     if (!ctx || Z < 1 || Y < 1 || X < 1 || !(corr_px > 0.0) || !out)
         return fail(SCW_ERR_ARG, "scw_gen_grf: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const long long total = (long long)Z * Y * X;
     const int R = (int)std::ceil(4.0 * corr_px);
     std::vector<double> w(2 * R + 1);
@@ -227,7 +227,7 @@ scw_status scw_npy_read(scw_ctx ctx, const char* path, int* dims, void* out) {
     dims[2] = (int)shp[2];
     if (!out) return SCW_OK;
     if (!ctx) return fail(SCW_ERR_ARG, "scw_npy_read: null context");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const long long total = shp[0] * shp[1] * shp[2];
     const size_t esz = c16 ? 16 : 8;
     if (fortran) {                                     // 2-D: read whole, transpose on the host

@@ -21,6 +21,39 @@ scw_status fail(scw_status st, const std::string& msg);
             return ::scw::fail(SCW_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// Makes `device` current for the enclosing scope and gives the caller's current device back
+// when the scope ends, so no entry point changes the calling thread's device as a side effect.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceScope(int device) {
+        if (device < 0) return;
+        int cur = -1;
+        if (cudaGetDevice(&cur) != cudaSuccess) {
+            cudaGetLastError();
+            cur = -1;
+        }
+        if (cur != device) {
+            err = cudaSetDevice(device);
+            if (err == cudaSuccess) prev = cur;
+        }
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
+#define SCW_CAT2_(a, b) a##b
+#define SCW_CAT_(a, b) SCW_CAT2_(a, b)
+// the device of a context current until the end of the enclosing scope; returns on failure
+#define SCW_ON_DEVICE(dev)                                                                          \
+    ::scw::DeviceScope SCW_CAT_(scw_dev_scope_, __LINE__)(dev);                                     \
+    if (SCW_CAT_(scw_dev_scope_, __LINE__).err != cudaSuccess)                                      \
+    return ::scw::fail(SCW_ERR_CUDA, std::string("cudaSetDevice: ") +                               \
+                                         cudaGetErrorString(SCW_CAT_(scw_dev_scope_, __LINE__).err))
+
 // Device buffer (of a context or a call); grows on demand, never shrinks, freed on destruction.
 struct DevBuf {
     void* ptr = nullptr;
@@ -65,6 +98,7 @@ struct scw_ctx_s {
     scw::DevBuf sep_scratch;    // separable evaluator: phases, coefficients C, row products T, tables
     scw::PinnedBuf host_desc;   // pinned staging of the descriptors
     cudaEvent_t desc_done = nullptr;  // the last descriptor upload has been consumed
+    void* static_scratch = nullptr;   // device address of the allocation-free entry point's array
     int* tc_err = nullptr;            // device flag: a tensor-core kernel's bounded wait gave up
     bool tc_pending_check = false;    // a tensor-core kernel ran since the flag was last read
     bool timing = false;

@@ -60,4 +60,10 @@ struct scw_sep_s {
     double2* dKz = nullptr;                // [Z][2][Jp] kz of the downward / upward modes
     float2* dQ = nullptr;                  // [Z][2][3][MF][Jp] amplitudes at the modes' reference planes
     bool own_Q = false;
+    // host-streamed evaluation (scw_sep_eval_volume_host): copy streams, events, output slabs
+    cudaStream_t up_stream = nullptr, down_stream = nullptr;
+    std::vector<cudaEvent_t> events;
+    void* dslab = nullptr;                 // output slab ring (device)
+    size_t slab_bytes = 0;
+    size_t chunk_bytes = 0, slab_target = 0;   // scw_sep_set_streaming (0: defaults)
 };

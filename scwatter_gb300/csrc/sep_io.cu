@@ -49,7 +49,7 @@ extern "C" {
 
 scw_status scw_sep_save(scw_sep s, const char* path) {
     if (!s || !path) return fail(SCW_ERR_ARG, "scw_sep_save: null argument");
-    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    SCW_ON_DEVICE(s->ctx->device);
     SCW_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
     File out;
     out.f = fopen(path, "wb");
@@ -102,6 +102,7 @@ scw_status scw_sep_load(scw_ctx ctx, const char* path, scw_sep* out) {
     if (fread(kx.data(), 8, M0, in.f) != (size_t)M0 || fread(ky.data(), 8, M1, in.f) != (size_t)M1 ||
         fread(zb.data(), 8, Z + 1, in.f) != (size_t)Z + 1)
         return fail(SCW_ERR_FORMAT, "truncated factored file");
+    SCW_ON_DEVICE(ctx->device);
     scw_sep s = nullptr;
     scw_status st = scw_sep_create(ctx, M0, M1, Z, J, kx.data(), ky.data(), zb.data(), &s);
     if (st != SCW_OK) return st;

@@ -54,7 +54,7 @@ struct scw_solution_s {
     std::vector<double> eig_res;
     ~scw_solution_s() {
         if (dQ) {
-            cudaSetDevice(ctx->device);
+            ::scw::DeviceScope dev_scope_(ctx->device);
             cudaFree(dQ);
         }
     }
@@ -796,7 +796,7 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
     SolvePlan p;
     scw_status st = plan_solve(prm, Zs, Y, X, p);
     if (st != SCW_OK) return st;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     std::unique_ptr<scw_solution_s> sol(new (std::nothrow) scw_solution_s());
     if (!sol) return fail(SCW_ERR_NOMEM, "host allocation");
     sol->ctx = ctx;
@@ -883,7 +883,7 @@ scw_status scw_layer_problem(scw_ctx ctx, const double* sample, int Zs, int Y, i
     if (M1) *M1 = p.M1;
     if (!coef && !PQ) return SCW_OK;
     if (!sample) return fail(SCW_ERR_ARG, "scw_layer_problem: null sample");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     SolveIn in{};
     SolveWs ws{};
     Carver sz;
@@ -958,7 +958,7 @@ scw_status scw_solution_get_modes(scw_solution s, int l, double* Q_check, double
     if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_solution_get_modes: slice out of range");
     if (!s->dQ) return fail(SCW_ERR_STATE, "scw_solution_get_modes: no mode amplitudes (external solve)");
     const size_t blk = (size_t)3 * s->MF * 2 * s->MF;
-    SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    SCW_ON_DEVICE(s->ctx->device);
     if (Q_check)
         SCW_CUDA_TRY(cudaMemcpy(Q_check, s->dQ + (size_t)l * 2 * blk, sizeof(double2) * blk, cudaMemcpyDeviceToHost));
     if (Q_hat)
@@ -971,7 +971,7 @@ scw_status scw_solution_to_sep(scw_solution s, scw_sep* out) {
     if (!s || !out) return fail(SCW_ERR_ARG, "null argument");
     *out = nullptr;
     scw_ctx ctx = s->ctx;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const int MF = s->MF, n = 2 * MF, M0 = s->M0, M1 = s->M1, Z = s->Z;
     const double k = s->k;
     std::vector<double> kx(M0), ky(M1);
@@ -1103,7 +1103,7 @@ scw_status scw_solution_to_cw(scw_solution s, scw_cw* out) {
         return fail(SCW_ERR_NOMEM, "host allocation of the mode amplitudes");
     }
     if (!s->external) {
-        SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+        SCW_ON_DEVICE(s->ctx->device);
         SCW_CUDA_TRY(cudaMemcpy(Qh.data(), s->dQ, sizeof(double2) * Qh.size(), cudaMemcpyDeviceToHost));
     }
     std::unique_ptr<scw_cw_s> cw(new (std::nothrow) scw_cw_s());
@@ -1173,7 +1173,7 @@ scw_status scw_solution_write_cw(scw_solution s, const char* path) {
     }
     flush();
     put(&nL, 8);
-    if (!s->external) SCW_CUDA_TRY(cudaSetDevice(s->ctx->device));
+    SCW_ON_DEVICE(s->external ? -1 : s->ctx->device);
     for (int l = 0; l < ZL && ok; l++) {
         const bool up = !s->external && l > 0, dn = !s->external && l < ZL - 1;
         if (up)

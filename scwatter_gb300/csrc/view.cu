@@ -96,7 +96,7 @@ extern "C" {
 scw_status scw_view_scalar(scw_ctx ctx, const float* E, int64_t n, int mode, float* S) {
     if (!ctx || !E || !S || n < 0 || mode < 0 || mode > 3) return fail(SCW_ERR_ARG, "scw_view_scalar: bad arguments");
     if (n == 0) return SCW_OK;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     scw::vw::scalar_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>((const float2*)E, n, mode, (float2*)S);
     SCW_CUDA_TRY(cudaGetLastError());
     ctx->launches++;
@@ -105,7 +105,7 @@ scw_status scw_view_scalar(scw_ctx ctx, const float* E, int64_t n, int mode, flo
 
 scw_status scw_view_minmax(scw_ctx ctx, const float* S, int64_t n, float* out4) {
     if (!ctx || !S || !out4 || n < 1) return fail(SCW_ERR_ARG, "scw_view_minmax: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     const int blocks = (int)std::min<int64_t>(1024, (n + 255) / 256);
     scw_status st = ctx->scratch.reserve(sizeof(float4) * blocks);
     if (st != SCW_OK) return st;
@@ -134,7 +134,7 @@ scw_status scw_view_minmax(scw_ctx ctx, const float* S, int64_t n, float* out4) 
 scw_status scw_view_color(scw_ctx ctx, const float* S, int64_t n, const float* params, unsigned char* rgb) {
     if (!ctx || !S || !params || !rgb || n < 0) return fail(SCW_ERR_ARG, "scw_view_color: bad arguments");
     if (n == 0) return SCW_OK;
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     scw::vw::ColorParams p{};
     p.real_low = params[0];
     p.real_high = params[1];

@@ -319,7 +319,7 @@ scw_status scw_eig_warm(scw_ctx ctx, int n, const void* A_, int batch, const voi
     using namespace scw::wm;
     if (!ctx || n < 1 || !A_ || batch < 1 || !shifts_ || !W_ || !V_ || max_it < 1 || !(tol > 0))
         return fail(SCW_ERR_ARG, "scw_eig_warm: bad arguments");
-    SCW_CUDA_TRY(cudaSetDevice(ctx->device));
+    SCW_ON_DEVICE(ctx->device);
     cudaStream_t st = ctx->stream;
     const double2* A = (const double2*)A_;
     const double2* shifts = (const double2*)shifts_;

@@ -25,6 +25,17 @@ def _c(a):
     return a, ctypes.c_void_p(a.ctypes.data)
 
 
+def _host_ptr(a, name):
+    """Address of a C-contiguous complex64 host array (numpy) or CPU tensor (torch)."""
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.complex64 or not a.flags.c_contiguous:
+            raise ValueError(f"{name} must be a C-contiguous complex64 array")
+        return a.ctypes.data
+    if getattr(a, "is_cuda", True) or str(getattr(a, "dtype", "")) != "torch.complex64" or not a.is_contiguous():
+        raise ValueError(f"{name} must be a contiguous complex64 host array or CPU tensor")
+    return a.data_ptr()
+
+
 class SeparableSet:
     def __init__(self, ctx: Context, handle):
         self.ctx = ctx
@@ -84,12 +95,69 @@ class SeparableSet:
         _lib.call("scw_sep_info", self.handle, *[ctypes.byref(x) for x in v])
         return tuple(x.value for x in v)
 
+    def grid(self):
+        """(kx [M0], ky [M1], z boundaries [Z + 1]) of the set."""
+        M0, M1, Z, _ = self.info()
+        kx, ky, zb = np.zeros(M0), np.zeros(M1), np.zeros(Z + 1)
+        _lib.call("scw_sep_get_grid", self.handle, *(ctypes.c_void_p(a.ctypes.data) for a in (kx, ky, zb)))
+        return kx, ky, zb
+
     def set_region_rule(self, rule: int):
         _lib.call("scw_sep_set_region_rule", self.handle, int(rule))
 
     def eval_volume_device(self, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, Nz, dE_ptr: int, method=FP32):
         _lib.call("scw_sep_eval_volume_device", self.handle, x_start, y_start, z_start, dx, dy, dz, int(Nx), int(Ny),
                   int(Nz), ctypes.c_void_p(dE_ptr), int(method))
+
+    def eval_volume_host(self, Q_host, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, Nz, out=None,
+                         method=TF32X3):
+        """End-to-end volume evaluation from HOST amplitudes (``scw_sep_eval_volume_host``):
+        ``Q_host`` [Z, 2, 3, MF, J] complex64 (numpy array or CPU torch tensor, page-locked for
+        full link speed) is uploaded slice by slice while earlier slices are evaluated, and the
+        planes come back into ``out`` ([Nz, Ny, Nx, 3] complex64 host array or CPU tensor,
+        allocated when None) as they finish.  Returns ``out``."""
+        M0, M1, Z, J = self.info()
+        shape = (Z, 2, 3, M0 * M1, J)
+        if tuple(Q_host.shape) != shape:
+            raise ValueError(f"Q_host must be {shape}, got {tuple(Q_host.shape)}")
+        qptr = _host_ptr(Q_host, "Q_host")
+        if out is None:
+            out = np.empty((Nz, Ny, Nx, 3), np.complex64)
+        if tuple(out.shape) != (Nz, Ny, Nx, 3):
+            raise ValueError("out must be [Nz, Ny, Nx, 3]")
+        optr = _host_ptr(out, "out")
+        _lib.call("scw_sep_eval_volume_host", self.handle, ctypes.c_void_p(qptr), x_start, y_start, z_start, dx, dy,
+                  dz, int(Nx), int(Ny), int(Nz), ctypes.c_void_p(optr), int(method))
+        return out
+
+    def eval_slab_device(self, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, k_begin, k_end, dE_ptr: int,
+                         method=TF32X3):
+        """Planes ``k_begin .. k_end-1`` of the volume (same z-values as the whole volume) into
+        device memory [k_end - k_begin, Ny, Nx, 3] (``scw_sep_eval_slab_device``)."""
+        _lib.call("scw_sep_eval_slab_device", self.handle, x_start, y_start, z_start, dx, dy, dz, int(Nx), int(Ny),
+                  int(k_begin), int(k_end), ctypes.c_void_p(dE_ptr), int(method))
+
+    def eval_slab_host(self, Q_host, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, k_begin, k_end, out=None,
+                       method=TF32X3):
+        """Host-buffer form of :meth:`eval_slab_device` (``scw_sep_eval_slab_host``): only the
+        slices the slab's planes lie in are read from ``Q_host`` [Z, 2, 3, MF, J]."""
+        M0, M1, Z, J = self.info()
+        if tuple(Q_host.shape) != (Z, 2, 3, M0 * M1, J):
+            raise ValueError(f"Q_host must be {(Z, 2, 3, M0 * M1, J)}, got {tuple(Q_host.shape)}")
+        n = int(k_end) - int(k_begin)
+        if out is None:
+            out = np.empty((n, Ny, Nx, 3), np.complex64)
+        if tuple(out.shape) != (n, Ny, Nx, 3):
+            raise ValueError("out must be [k_end - k_begin, Ny, Nx, 3]")
+        _lib.call("scw_sep_eval_slab_host", self.handle, ctypes.c_void_p(_host_ptr(Q_host, "Q_host")), x_start,
+                  y_start, z_start, dx, dy, dz, int(Nx), int(Ny), int(k_begin), int(k_end),
+                  ctypes.c_void_p(_host_ptr(out, "out")), int(method))
+        return out
+
+    def set_streaming(self, chunk_bytes: int = 0, slab_bytes: int = 0):
+        """Upload chunk (Q bytes, whole slices) and read-back slab (output bytes, whole planes)
+        of :meth:`eval_volume_host`; 0 keeps the defaults (192 MiB, 64 MiB)."""
+        _lib.call("scw_sep_set_streaming", self.handle, ctypes.c_int64(chunk_bytes), ctypes.c_int64(slab_bytes))
 
     def eval_plane_device(self, axis, a_start, b_start, c, d, N, dE_ptr: int, method=FP32):
         _lib.call("scw_sep_eval_plane_device", self.handle, int(axis), a_start, b_start, c, d, int(N),

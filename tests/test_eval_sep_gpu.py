@@ -110,3 +110,71 @@ def test_not_separable_is_rejected(ctx):
     with pytest.raises(_lib.ScwError) as ei:
         SeparableSet.from_cw(ctx, S)
     assert ei.value.status == 9
+
+
+def _trimmed(fs, J):
+    """The factored sample with only the first J modes per half (odd J exercises the padded
+    device rows)."""
+    import dataclasses
+    return dataclasses.replace(fs, gamma_dn=fs.gamma_dn[:, :J], gamma_up=fs.gamma_up[:, :J],
+                               Q_dn=fs.Q_dn[..., :J], Q_up=fs.Q_up[..., :J])
+
+
+@pytest.mark.parametrize("odd", [False, True])
+def test_volume_from_host_amplitudes(ctx, odd):
+    """scw_sep_eval_volume_host (slices uploaded while earlier ones are evaluated, planes read
+    back as they finish) against the device-resident evaluation of the same set; the set it
+    runs on starts with zero amplitudes, so every interior value must come from Q_host.  The
+    grid reaches above and below the sample (exterior planes need no upload) and is long
+    enough for several output slabs per slice."""
+    import torch
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import SeparableSet, TF32X3
+    fs = synthetic.make_factored(M0=6, M1=4, Z=5, size=(12.0, 10.0, 5.0), seed=11)
+    if odd:
+        fs = _trimmed(fs, 2 * fs.MF - 3)
+    J = fs.gamma_dn.shape[1]
+    ref_set = SeparableSet.from_factored(ctx, fs)
+    zero = dataclasses_zero(fs)
+    set_ = SeparableSet.from_factored(ctx, zero)
+    Nx, Ny, Nz = 45, 23, 70
+    args = (np.float32(-7), np.float32(-6), np.float32(-3.5), np.float32(0.3), np.float32(0.5), np.float32(0.1),
+            Nx, Ny, Nz)
+    ref = torch.zeros((Nz, Ny, Nx, 3), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ref_set.eval_volume_device(*args, ref.data_ptr(), method=TF32X3)
+    ctx.synchronize()
+    ref = ref.cpu().numpy()
+    Qh = torch.empty((fs.Z, 2, 3, fs.MF, J), dtype=torch.complex64, pin_memory=True)
+    Qh[:, 0] = torch.from_numpy(np.ascontiguousarray(fs.Q_dn, dtype=np.complex64))
+    Qh[:, 1] = torch.from_numpy(np.ascontiguousarray(fs.Q_up, dtype=np.complex64))
+    # one slice per upload, 3 planes per read-back slab: many slabs cycle through the 3 slots
+    set_.set_streaming(chunk_bytes=1, slab_bytes=3 * Nx * Ny * 24)
+    for out in (None, torch.empty((Nz, Ny, Nx, 3), dtype=torch.complex64, pin_memory=True)):
+        got = set_.eval_volume_host(Qh, *args, out=out, method=TF32X3)
+        got = got.numpy() if hasattr(got, "numpy") and not isinstance(got, np.ndarray) else got
+        assert np.isfinite(got).all()
+        assert max(rel_l2(got, ref, floor=0.0)) < 1e-6
+    set_.set_streaming()                 # defaults: every slice in one upload chunk here
+    got = set_.eval_volume_host(Qh, *args, method=TF32X3)
+    assert max(rel_l2(got, ref, floor=0.0)) < 1e-6
+    # the set's own device copy now holds the uploaded amplitudes
+    again = torch.zeros((Nz, Ny, Nx, 3), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    set_.eval_volume_device(*args, again.data_ptr(), method=TF32X3)
+    ctx.synchronize()
+    assert max(rel_l2(again.cpu().numpy(), ref, floor=0.0)) < 1e-6
+
+
+def dataclasses_zero(fs):
+    import dataclasses
+    return dataclasses.replace(fs, Q_dn=np.zeros_like(fs.Q_dn), Q_up=np.zeros_like(fs.Q_up))
+
+
+def test_volume_from_host_rejects_wrong_shape(ctx):
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import SeparableSet
+    fs = synthetic.make_factored(M0=4, M1=4, Z=2, size=(8.0, 8.0, 2.0), seed=1)
+    s = SeparableSet.from_factored(ctx, fs)
+    with pytest.raises(ValueError):
+        s.eval_volume_host(np.zeros((2, 2, 3, 16, 31), np.complex64), 0, 0, 0, 1, 1, 1, 4, 4, 4)

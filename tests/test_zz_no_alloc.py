@@ -91,3 +91,30 @@ def test_static_rejects_oversized_plane(waves):
         _lib.call("scw_eval_plane_device_static", ws.handle, 0, ctypes.c_float(0), ctypes.c_float(0),
                   ctypes.c_float(0), ctypes.c_float(1), 16385, ctypes.c_void_p(16))
     assert e.value.status == 1 and "maximum" in str(e.value)
+
+
+def test_static_allocates_no_device_memory(waves):
+    """The entry point's one promise: after a first call (which may load the library's GPU
+    module on the device), further calls with caller-allocated outputs leave the device's free
+    memory exactly where it was."""
+    import torch
+    from scwatter_gb300 import _lib
+    ctx, ws = waves
+    axis, a0, b0, c, d, N = PLANES[0]                    # a split-K plane: both kernels run
+    outs = [torch.zeros((N, N, 3), dtype=torch.complex64, device="cuda") for _ in range(4)]
+
+    def call(o):
+        _lib.call("scw_eval_plane_device_static", ws.handle, int(axis), ctypes.c_float(a0), ctypes.c_float(b0),
+                  ctypes.c_float(c), ctypes.c_float(d), int(N), ctypes.c_void_p(o.data_ptr()))
+
+    call(outs[0])
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for o in outs[1:]:
+        call(o)
+    ctx.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    for o in outs[1:]:
+        assert torch.equal(o, outs[0])

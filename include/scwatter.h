@@ -162,6 +162,20 @@ SCW_API scw_status scw_eval_plane_device_static(scw_waves waves, int axis, float
 SCW_API scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half,
                                   const double* kx, const double* ky, const double* z_boundaries, scw_sep* out);
 SCW_API scw_status scw_sep_destroy(scw_sep s);
+/* Paired set (no reference counterpart): per slice ONE block V [3][MF][J] and the mode amplitudes
+ * beta_dn, beta_up [J], standing for Q_dn = V diag(beta_dn) and Q_up = diag(1, 1, -1) V diag(beta_up).
+ * That is the structure of the solver's modes (sCWatter.cpp:781-871: the E rows of a mode are the
+ * same eigenvector for the roots +gamma and -gamma, its H rows -- hence Ez -- change sign), so the
+ * evaluator streams one block per slice instead of two: half the coefficient bytes.  The amplitudes
+ * are folded into the FP64 mode phases. */
+SCW_API scw_status scw_sep_create_paired(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half,
+                                         const double* kx, const double* ky, const double* z_boundaries,
+                                         scw_sep* out);
+/* kz_dn, kz_up, beta_dn, beta_up: [J] complex (HOST); V: [3][MF][J] complex64 in host or device memory. */
+SCW_API scw_status scw_sep_set_slice_paired(scw_sep s, int l, const double* kz_dn, const double* kz_up,
+                                            const void* V_c64, const double* beta_dn, const double* beta_up);
+/* 2: two-half set (scw_sep_create), 1: paired set (scw_sep_create_paired). */
+SCW_API scw_status scw_sep_form(scw_sep s, int* halves);
 /* incident (referenced at z = 0), reflected (at z_0), transmitted (at z_Z): [3][MF] complex;
  * kz_*: [MF] complex. */
 SCW_API scw_status scw_sep_set_exterior(scw_sep s, const double* inc, const double* kz_inc, const double* refl,
@@ -178,8 +192,9 @@ SCW_API scw_status scw_sep_from_cw(scw_ctx ctx, scw_cw cw, scw_sep* out);
 /* Compact factored coefficient file (.cwf; no reference counterpart): the separable set as it is
  * -- "SCWSEP01", int32 M0, M1, Z, J, region rule, 0; float64 kx[M0], ky[M1], z[Z+1];
  * complex128 exterior[12 MF], kz[Z][2][Jp]; complex64 Q[Z][2][3][MF][Jp] (Jp = J rounded up to
- * even), little-endian -- streamed one slice at a time.  Load checks the magic and that the
- * file size matches the header (SCW_ERR_FORMAT otherwise). */
+ * even), little-endian -- streamed one slice at a time.  A paired set is written as "SCWSEP02":
+ * the same header and blocks up to kz, then complex128 beta[Z][2][Jp] and complex64 V[Z][3][MF][Jp].
+ * Load checks the magic and that the file size matches the header (SCW_ERR_FORMAT otherwise). */
 SCW_API scw_status scw_sep_save(scw_sep s, const char* path);
 SCW_API scw_status scw_sep_load(scw_ctx ctx, const char* path, scw_sep* out);
 SCW_API scw_status scw_sep_info(scw_sep s, int* M0, int* M1, int* n_slices, int* modes_per_half);
@@ -192,7 +207,8 @@ SCW_API scw_status scw_sep_eval_volume_device(scw_sep s, float x_start, float y_
 /* The same volume from HOST amplitudes, end to end (no reference counterpart; the reference
  * uploads its wave table once in gpu_initialize, gpuEvaluator.cu:15-26, and reads each plane back
  * in gpu_cw_evaluate, :131-165).  Q_host: [Z][2][3][MF][J] complex64 (per slice the downward then
- * the upward block, as in the .cwf file but without the even padding); E_host: [Nz][Ny][Nx][3]
+ * the upward block, as in the .cwf file but without the even padding; a paired set takes its one block
+ * per slice, [Z][3][MF][J], and keeps its kz and beta from scw_sep_set_slice_paired); E_host: [Nz][Ny][Nx][3]
  * complex64.  Slices go up on one stream while the planes of the slices already up are evaluated
  * on the context stream, and finished planes come back on a third stream; use page-locked host
  * buffers for full link speed.  The set's device copy of each slice that a grid plane lies in is
@@ -304,6 +320,10 @@ SCW_API scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_sl
  * products (one n x n x n GEMM each) summed over the slices. */
 SCW_API scw_status scw_solution_eig_info(scw_solution s, int* mixed, int* accepted, int* max_steps,
                                          double* max_residual, int* residual_checks);
+/* Per slice (Z entries each, any may be NULL): state 1 = the mixed eigen-solver's refined result
+ * was accepted, else the reason code of scw_zgeev_mixed for the FP64 fallback; refinement steps;
+ * last relative residual.  SCW_ERR_STATE when the FP64 solver ran for every slice. */
+SCW_API scw_status scw_solution_eig_slices(scw_solution s, int* state, int* steps, double* residual);
 /* gamma: Z x 2MF complex downward roots (the reference's even-slot eigenvalues); x: 6MF
  * complex reflected / transmitted amplitudes (sCWatter.cpp:722); ef: 3MF incident Fourier
  * amplitudes; z_boundaries: Z + 1.  Any pointer may be NULL. */
@@ -410,6 +430,14 @@ SCW_API scw_status scw_view_color(scw_ctx ctx, const float* S, int64_t n, const 
  * amplitude, xyz); info: count ints (1 = singular system).  2 <= L <= 16. */
 SCW_API scw_status scw_layer_solve(scw_ctx ctx, int L, const double* ri, const double* z, double n0, double k,
                                    int count, const double* waves, double* x, int* info);
+
+/* ---------------------------------------------------------------------------------- */
+/* Diagnostics (no reference counterpart)                                              */
+/* ---------------------------------------------------------------------------------- */
+/* Measured issue peaks of this GPU (any output may be NULL): MUFU operations per second for the
+ * plain evaluator's mix (one sin.approx, cos.approx and ex2.approx each), FP32 and FP64 FMA
+ * FLOP/s; independent dependency chains on every SM, event-timed; synchronises. */
+SCW_API scw_status scw_measure_peaks(scw_ctx ctx, double* mufu_ops_per_s, double* fp32_flops, double* fp64_flops);
 
 #ifdef __cplusplus
 }

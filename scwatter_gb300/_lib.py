@@ -70,6 +70,7 @@ _SIGS = {
     "scw_solve": [P, P, I32, I32, I32, P, PP],
     "scw_solution_destroy": [P],
     "scw_solution_info": [P, P, P, P, P],
+    "scw_solution_eig_slices": [P, P, P, P],
     "scw_solution_eig_info": [P, P, P, P, P, P],
     "scw_solution_get": [P, P, P, P, P],
     "scw_solution_get_modes": [P, I32, P, P],
@@ -108,6 +109,10 @@ _SIGS = {
     "scw_sep_from_cw": [P, P, PP],
     "scw_sep_info": [P, ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32)],
     "scw_sep_set_region_rule": [P, I32],
+    "scw_sep_create_paired": [P, I32, I32, I32, I32, P, P, P, PP],
+    "scw_sep_set_slice_paired": [P, I32, P, P, P, P, P],
+    "scw_sep_form": [P, ctypes.POINTER(I32)],
+    "scw_measure_peaks": [P, P, P, P],
     "scw_sep_get_grid": [P, P, P, P],
     "scw_sep_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
     "scw_sep_eval_volume_host": [P, P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],

@@ -36,34 +36,60 @@ __device__ __forceinline__ float2 phase_fp64(double kr, double ki, double dz) {
     return make_float2(m * c, m * s);
 }
 
-// Phi[g][j][kk] (kk < nks) = exp(i kz_j (z_kk - zref_j)) for the group's planes, zero past g.nk
+// Phase table of one group of planes, Phi[g][h][j][kk] (h = 0, 1; kk < nks; zero past g.nk):
+//   two-half sets: h = 0: exp(i kz_dn_j (z_kk - z_l)), h = 1: exp(i kz_up_j (z_kk - z_{l+1}));
+//   paired sets (beta != null): the mode amplitudes folded in, in FP64,
+//     h = 0 (rows Ex, Ey): beta_dn_j exp(i kz_dn_j (z - z_l)) + beta_up_j exp(i kz_up_j (z - z_{l+1}))
+//     h = 1 (rows Ez):     beta_dn_j exp(i kz_dn_j (z - z_l)) - beta_up_j exp(i kz_up_j (z - z_{l+1}))
 __global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float* __restrict__ zlist,
-                                 const double2* __restrict__ kz, const double* __restrict__ zb, int J, int nks,
-                                 float2* __restrict__ Phi) {
+                                 const double2* __restrict__ kz, const double2* __restrict__ beta,
+                                 const double* __restrict__ zb, int J, int nks, float2* __restrict__ Phi) {
     const PGroup g = groups[blockIdx.y];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= 2 * J) return;
     const int l = g.region - 1;
-    const int half = j / J;
-    const double2 k = kz[((long long)l * 2 + half) * J + (j - half * J)];
-    const double zref = half == 0 ? zb[l] : zb[l + 1];
+    const int half = j / J, jj = j - half * J;
     float2* out = Phi + ((long long)blockIdx.y * 2 * J + j) * nks;
+    if (!beta) {
+        const double2 k = kz[((long long)l * 2 + half) * J + jj];
+        const double zref = half == 0 ? zb[l] : zb[l + 1];
+        for (int kk = 0; kk < nks; kk++) {
+            if (kk < g.nk) {
+                const double dz = (double)zlist[g.zi[kk]] - zref;
+                out[kk] = phase_fp64(k.x, k.y, dz);
+            } else {
+                out[kk] = make_float2(0.f, 0.f);
+            }
+        }
+        return;
+    }
+    const double2 kd = kz[(long long)l * 2 * J + jj], ku = kz[((long long)l * 2 + 1) * J + jj];
+    const double2 bd = beta[(long long)l * 2 * J + jj], bu = beta[((long long)l * 2 + 1) * J + jj];
+    const double su = half == 0 ? 1.0 : -1.0;
     for (int kk = 0; kk < nks; kk++) {
         if (kk < g.nk) {
-            const double dz = (double)zlist[g.zi[kk]] - zref;
-            out[kk] = phase_fp64(k.x, k.y, dz);
+            const double z = (double)zlist[g.zi[kk]];
+            const float2 fd = phase_fp64(kd.x, kd.y, z - zb[l]);
+            const float2 fu = phase_fp64(ku.x, ku.y, z - zb[l + 1]);
+            const double re = bd.x * fd.x - bd.y * fd.y + su * (bu.x * fu.x - bu.y * fu.y);
+            const double im = bd.x * fd.y + bd.y * fd.x + su * (bu.x * fu.y + bu.y * fu.x);
+            out[kk] = make_float2((float)re, (float)im);
         } else {
             out[kk] = make_float2(0.f, 0.f);
         }
     }
 }
 
-// C[zi][c][p] = sum over the slice's 2J modes of Q[l][half][c][p][j] * Phi[g][half*J + j][kk]
+// C[zi][c][p] = sum over the slice's modes of Q[l][h][c][p][j] * Phi[g][h'][j][kk]:
+//   two-half sets (H = 2): h = h' = 0, 1 (downward and upward modes, 2J terms);
+//   paired sets (H = 1): the one block V, h' = 0 for rows Ex, Ey and 1 for rows Ez (J terms).
 //
 // HBM-streaming contraction: one warp owns RW rows (c, p) at a time; its lanes read 2
 // consecutive complex Q entries each (512 contiguous bytes per warp and row per step) and
 // multiply them with the group's phases, staged in shared memory per chunk of kChunk modes
-// and shared by the CTA's 8 warps.  Lane partial sums are reduced with warp shuffles.
+// and shared by the CTA's 8 warps.  Every CTA works on one component c (blockIdx.x / nbp),
+// so its phase rows are the same for all its warps.  Lane partial sums are reduced with warp
+// shuffles.
 constexpr int kCtrWarps = 8;
 constexpr int kCtrChunk = 1024;
 
@@ -85,7 +111,7 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 template <int NK, int RW>
 __global__ void __launch_bounds__(kCtrWarps * 32, 2)
 sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict__ Phi,
-                    const float2* __restrict__ Q, int MF, int J, float2* __restrict__ C) {
+                    const float2* __restrict__ Q, int MF, int J, int H, float2* __restrict__ C) {
     constexpr int S = CtrCfg<RW, NK>::kStages;
     extern __shared__ float4 smem4[];
     // (phi[j][kk], phi[j+1][kk]) pairs per plane; then per lane S x RW private Q slots
@@ -94,20 +120,22 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
     const int l = g.region - 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* qs = smem4 + NK * (kCtrChunk / 2) + (size_t)warp * S * RW * 32 + lane;   // slot (s, r): qs[(s*RW + r)*32]
-    const int row0 = (blockIdx.x * kCtrWarps + warp) * RW;
+    const int nbp = gridDim.x / 3;                       // CTAs per component
+    const int c = blockIdx.x / nbp;
+    const int p0 = ((blockIdx.x - c * nbp) * kCtrWarps + warp) * RW;
     float acc[RW][NK][2];
 #pragma unroll
     for (int r = 0; r < RW; r++)
 #pragma unroll
         for (int kk = 0; kk < NK; kk++) acc[r][kk][0] = acc[r][kk][1] = 0.f;
     const float2* Pg = Phi + (long long)blockIdx.y * 2 * J * NK;
-    for (int half = 0; half < 2; half++) {
+    for (int half = 0; half < H; half++) {
+        const int ph_half = H == 2 ? half : (c == 2 ? 1 : 0);
         const float4* qrow[RW];
 #pragma unroll
         for (int r = 0; r < RW; r++) {
-            const int row = min(row0 + r, 3 * MF - 1);    // rows past the end repeat the last (not written)
-            const int c = row / MF, p = row % MF;
-            qrow[r] = reinterpret_cast<const float4*>(Q + ((((long long)l * 2 + half) * 3 + c) * MF + p) * (long long)J);
+            const int p = min(p0 + r, MF - 1);            // rows past the end repeat the last (not written)
+            qrow[r] = reinterpret_cast<const float4*>(Q + ((((long long)l * H + half) * 3 + c) * MF + p) * (long long)J);
         }
         for (int j0 = 0; j0 < J; j0 += kCtrChunk) {
             const int nj = min(kCtrChunk, J - j0);
@@ -115,8 +143,8 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
             // consecutive threads fill consecutive pairs of one plane (conflict-free stores)
             for (int e = threadIdx.x; e < (nj / 2) * NK; e += blockDim.x) {
                 const int kk = e / (nj / 2), jp = e % (nj / 2);
-                const float2 a = Pg[((long long)half * J + j0 + 2 * jp) * NK + kk];
-                const float2 b = Pg[((long long)half * J + j0 + 2 * jp + 1) * NK + kk];
+                const float2 a = Pg[((long long)ph_half * J + j0 + 2 * jp) * NK + kk];
+                const float2 b = Pg[((long long)ph_half * J + j0 + 2 * jp + 1) * NK + kk];
                 ph[kk][jp] = make_float4(a.x, a.y, b.x, b.y);
             }
             __syncthreads();
@@ -163,7 +191,7 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
     }
 #pragma unroll
     for (int r = 0; r < RW; r++) {
-        const int row = row0 + r;
+        const int p = p0 + r;
 #pragma unroll
         for (int kk = 0; kk < NK; kk++) {
             float vr = acc[r][kk][0], vi = acc[r][kk][1];
@@ -172,10 +200,7 @@ sep_contract_kernel(const PGroup* __restrict__ groups, const float2* __restrict_
                 vr += __shfl_xor_sync(0xffffffffu, vr, o);
                 vi += __shfl_xor_sync(0xffffffffu, vi, o);
             }
-            if (lane == 0 && row < 3 * MF && kk < g.nk) {
-                const int c = row / MF, p = row % MF;
-                C[((long long)g.zi[kk] * 3 + c) * MF + p] = make_float2(vr, vi);
-            }
+            if (lane == 0 && p < MF && kk < g.nk) C[((long long)g.zi[kk] * 3 + c) * MF + p] = make_float2(vr, vi);
         }
     }
 }
@@ -429,15 +454,19 @@ static scw_status stage1_record(scw_sep s, const SepEvalPlan& p, const char* d_d
             dim3 gp((2 * J + 255) / 256, (unsigned)groups.size());
             {
                 LaunchTimer lt(ctx, "sep_phase_kernel");
-                sep_phase_kernel<<<gp, 256, 0, ctx->stream>>>(dg, dz, s->dKz, s->dzb, J, nks, dPhi);
+                sep_phase_kernel<<<gp, 256, 0, ctx->stream>>>(dg, dz, s->dKz, s->halves == 1 ? s->dBeta : nullptr,
+                                                              s->dzb, J, nks, dPhi);
             }
             SCW_CUDA_TRY(cudaGetLastError());
             ctx->launches++;
-            auto grid_for = [&](int rw) { return dim3((3 * MF + kCtrWarps * rw - 1) / (kCtrWarps * rw), (unsigned)groups.size()); };
+            // per component c, ceil(MF / (warps x rows per warp)) CTAs
+            auto grid_for = [&](int rw) {
+                return dim3(3 * ((MF + kCtrWarps * rw - 1) / (kCtrWarps * rw)), (unsigned)groups.size());
+            };
             LaunchTimer lt(ctx, "sep_contract_kernel");
             auto launch = [&](auto kernel, int rw, size_t smem) -> scw_status {
                 SCW_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                kernel<<<grid_for(rw), kCtrWarps * 32, smem, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, dC);
+                kernel<<<grid_for(rw), kCtrWarps * 32, smem, ctx->stream>>>(dg, dPhi, s->dQ, MF, J, s->halves, dC);
                 return SCW_OK;
             };
             scw_status ls;
@@ -683,7 +712,8 @@ scw_status sep_eval_volume_host(scw_sep s, const float2* Qh, float x0, float y0,
     SCW_ON_DEVICE(ctx->device);
     const size_t plane_bytes = (size_t)Nx * Ny * 6 * sizeof(float);
     const size_t J = (size_t)s->J, Jp = (size_t)s->Jp, MF = (size_t)s->MF;
-    const size_t slice_bytes = 2 * 3 * MF * J * sizeof(float2);          // host layout [2][3][MF][J]
+    const size_t H = (size_t)s->halves;
+    const size_t slice_bytes = H * 3 * MF * J * sizeof(float2);          // host layout [H][3][MF][J]
     const size_t chunk_target = s->chunk_bytes > 0 ? s->chunk_bytes : kChunkTarget;
     const size_t slab_target = s->slab_target > 0 ? s->slab_target : kSlabTarget;
     const int per_chunk = (int)std::max<size_t>(1, chunk_target / std::max<size_t>(slice_bytes, 1));
@@ -743,13 +773,13 @@ scw_status sep_eval_volume_host(scw_sep s, const float2* Qh, float x0, float y0,
     for (size_t c = 0; c < order.size(); c++) {
         const int l0 = order[c] * per_chunk, l1 = std::min(s->Z, l0 + per_chunk);
         for (int l = l0; l < l1; l++) {
-            const float2* src = Qh + (size_t)l * 2 * 3 * MF * J;
-            float2* dst = s->dQ + (size_t)l * 2 * 3 * MF * Jp;
+            const float2* src = Qh + (size_t)l * H * 3 * MF * J;
+            float2* dst = s->dQ + (size_t)l * H * 3 * MF * Jp;
             if (J == Jp)
                 SCW_CUDA_TRY(cudaMemcpyAsync(dst, src, slice_bytes, cudaMemcpyHostToDevice, s->up_stream));
             else
                 SCW_CUDA_TRY(cudaMemcpy2DAsync(dst, Jp * sizeof(float2), src, J * sizeof(float2), J * sizeof(float2),
-                                               2 * 3 * MF, cudaMemcpyHostToDevice, s->up_stream));
+                                               H * 3 * MF, cudaMemcpyHostToDevice, s->up_stream));
         }
         SCW_CUDA_TRY(cudaEventRecord(ev_chunk[c], s->up_stream));
     }
@@ -805,6 +835,7 @@ static void sep_free(scw_sep s) {
     if (s->dkx) cudaFree(s->dkx);
     if (s->dky) cudaFree(s->dky);
     if (s->dzb) cudaFree(s->dzb);
+    if (s->dBeta) cudaFree(s->dBeta);
     if (s->dslab) cudaFree(s->dslab);
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     if (s->up_stream) cudaStreamDestroy(s->up_stream);
@@ -814,8 +845,10 @@ static void sep_free(scw_sep s) {
 
 extern "C" {
 
-scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half, const double* kx,
-                          const double* ky, const double* z_boundaries, scw_sep* out) {
+}  // extern "C"
+
+static scw_status sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half, const double* kx,
+                             const double* ky, const double* z_boundaries, int halves, scw_sep* out) {
     if (!ctx || !out || M0 <= 0 || M1 <= 0 || n_slices < 0 || modes_per_half < 0 || !kx || !ky || !z_boundaries)
         return fail(SCW_ERR_ARG, "scw_sep_create: bad arguments");
     *out = nullptr;
@@ -829,12 +862,13 @@ scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_p
     s->Z = n_slices;
     s->J = modes_per_half;
     s->Jp = modes_per_half + (modes_per_half & 1);
+    s->halves = halves;
     s->kx.assign(kx, kx + M0);
     s->ky.assign(ky, ky + M1);
     s->zb.assign(z_boundaries, z_boundaries + n_slices + 1);
     s->z_layers.resize(n_slices + 1);
     for (int l = 0; l <= n_slices; l++) s->z_layers[l] = (float)z_boundaries[l];
-    const size_t nQ = (size_t)n_slices * 2 * 3 * s->MF * (size_t)s->Jp;
+    const size_t nQ = (size_t)n_slices * halves * 3 * s->MF * (size_t)s->Jp;
     bool ok = cudaMalloc(&s->dkx, M0 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&s->dky, M1 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&s->dzb, (n_slices + 1) * sizeof(double)) == cudaSuccess &&
@@ -844,6 +878,8 @@ scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_p
         ok = cudaMalloc(&s->dQ, nQ * sizeof(float2)) == cudaSuccess;
         s->own_Q = true;
     }
+    const size_t nB = (size_t)n_slices * 2 * s->Jp + 1;
+    if (ok && halves == 1) ok = cudaMalloc(&s->dBeta, nB * sizeof(double2)) == cudaSuccess;
     if (!ok) {
         sep_free(s);
         return fail(SCW_ERR_NOMEM, "cudaMalloc of the separable coefficient set");
@@ -854,12 +890,31 @@ scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_p
     cudaMemset(s->dExt, 0, 12 * (size_t)s->MF * sizeof(double2));
     if (nQ) cudaMemset(s->dQ, 0, nQ * sizeof(float2));
     cudaMemset(s->dKz, 0, ((size_t)n_slices * 2 * s->Jp + 1) * sizeof(double2));
+    if (s->dBeta) cudaMemset(s->dBeta, 0, nB * sizeof(double2));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         sep_free(s);
         return fail(SCW_ERR_CUDA, cudaGetErrorString(e));
     }
     *out = s;
+    return SCW_OK;
+}
+
+extern "C" {
+
+scw_status scw_sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half, const double* kx,
+                          const double* ky, const double* z_boundaries, scw_sep* out) {
+    return sep_create(ctx, M0, M1, n_slices, modes_per_half, kx, ky, z_boundaries, 2, out);
+}
+
+scw_status scw_sep_create_paired(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half, const double* kx,
+                                 const double* ky, const double* z_boundaries, scw_sep* out) {
+    return sep_create(ctx, M0, M1, n_slices, modes_per_half, kx, ky, z_boundaries, 1, out);
+}
+
+scw_status scw_sep_form(scw_sep s, int* halves) {
+    if (!s || !halves) return fail(SCW_ERR_ARG, "scw_sep_form: null argument");
+    *halves = s->halves;
     return SCW_OK;
 }
 
@@ -917,6 +972,7 @@ static scw_status upload_q(scw_sep s, int l, int half, const void* src, cudaMemc
 scw_status scw_sep_set_slice(scw_sep s, int l, const double* kz_dn, const double* Q_dn, const double* kz_up,
                              const double* Q_up) {
     if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_sep_set_slice: slice out of range");
+    if (s->halves != 2) return fail(SCW_ERR_STATE, "scw_sep_set_slice: a paired set takes scw_sep_set_slice_paired");
     const size_t J = (size_t)s->J, MF = (size_t)s->MF;
     if (J == 0) return SCW_OK;
     if (!kz_dn || !Q_dn || !kz_up || !Q_up) return fail(SCW_ERR_ARG, "scw_sep_set_slice: null argument");
@@ -935,6 +991,8 @@ scw_status scw_sep_set_slice(scw_sep s, int l, const double* kz_dn, const double
 scw_status scw_sep_set_slice_device(scw_sep s, int l, const double* kz_dn, const void* Q_dn_c64, const double* kz_up,
                                     const void* Q_up_c64) {
     if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_sep_set_slice_device: slice out of range");
+    if (s->halves != 2)
+        return fail(SCW_ERR_STATE, "scw_sep_set_slice_device: a paired set takes scw_sep_set_slice_paired");
     if (s->J == 0) return SCW_OK;
     if (!kz_dn || !Q_dn_c64 || !kz_up || !Q_up_c64) return fail(SCW_ERR_ARG, "scw_sep_set_slice_device: null argument");
     SCW_ON_DEVICE(s->ctx->device);
@@ -942,6 +1000,30 @@ scw_status scw_sep_set_slice_device(scw_sep s, int l, const double* kz_dn, const
     if (st != SCW_OK) return st;
     if ((st = upload_q(s, l, 0, Q_dn_c64, cudaMemcpyDefault, true)) != SCW_OK) return st;
     return upload_q(s, l, 1, Q_up_c64, cudaMemcpyDefault, true);
+}
+
+scw_status scw_sep_set_slice_paired(scw_sep s, int l, const double* kz_dn, const double* kz_up, const void* V_c64,
+                                    const double* beta_dn, const double* beta_up) {
+    if (!s || l < 0 || l >= s->Z) return fail(SCW_ERR_ARG, "scw_sep_set_slice_paired: slice out of range");
+    if (s->halves != 1) return fail(SCW_ERR_STATE, "scw_sep_set_slice_paired: not a paired set");
+    if (s->J == 0) return SCW_OK;
+    if (!kz_dn || !kz_up || !V_c64 || !beta_dn || !beta_up)
+        return fail(SCW_ERR_ARG, "scw_sep_set_slice_paired: null argument");
+    SCW_ON_DEVICE(s->ctx->device);
+    scw_status st = upload_kz(s, l, kz_dn, kz_up);
+    if (st != SCW_OK) return st;
+    const size_t J = (size_t)s->J, Jp = (size_t)s->Jp, MF = (size_t)s->MF;
+    std::vector<double> b(4 * Jp, 0.0);
+    std::memcpy(b.data(), beta_dn, 2 * J * 8);
+    std::memcpy(b.data() + 2 * Jp, beta_up, 2 * J * 8);
+    SCW_CUDA_TRY(cudaMemcpy(s->dBeta + (size_t)l * 2 * Jp, b.data(), 4 * Jp * 8, cudaMemcpyHostToDevice));
+    float2* dst = s->dQ + (size_t)l * 3 * MF * Jp;
+    if (J == Jp)
+        SCW_CUDA_TRY(cudaMemcpyAsync(dst, V_c64, 3 * MF * J * sizeof(float2), cudaMemcpyDefault, s->ctx->stream));
+    else
+        SCW_CUDA_TRY(cudaMemcpy2DAsync(dst, Jp * sizeof(float2), V_c64, J * sizeof(float2), J * sizeof(float2), 3 * MF,
+                                       cudaMemcpyDefault, s->ctx->stream));
+    return SCW_OK;
 }
 
 scw_status scw_sep_set_region_rule(scw_sep s, int rule) {

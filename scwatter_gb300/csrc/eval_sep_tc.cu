@@ -18,10 +18,11 @@
 //
 // Pipeline (one CTA per SM, persistent over the row tiles of one 128-column x tile), warp
 // specialised with mbarrier hand-offs:
-//   warps 0-3  epilogue: TMEM lane quarter w -> registers -> global (accumulator full/empty)
-//   warps 4-7  producers: build B (hi, lo) of the next tile into one of two shared buffers,
-//              writing whole 16-byte core rows in address order (no bank conflicts)
-//   warp 8     one thread issues the MMAs into one of two TMEM accumulators and commits them
+//   warps 0-7   epilogue: warp w reads TMEM lane quarter w % 4 (32 x-values) for the tile's
+//               rows 8 (w / 4) .. 8 (w / 4) + 7 -> registers -> global (accumulator full/empty)
+//   warps 8-14  producers: build B (hi, lo) of the next tile into one of two shared buffers,
+//               writing whole 16-byte core rows in address order (no bank conflicts)
+//   warp 15     one thread issues the MMAs into one of two TMEM accumulators and commits them
 // A (hi, lo) is built once by all warps before the roles split.  Operands use the SWIZZLE_NONE
 // K-major canonical layout: 8-row x 16-byte core matrices stored contiguously, LBO = 128 B
 // between core matrices along K, SBO = (K bytes / 16) * 128 B between 8-row groups.
@@ -103,6 +104,16 @@ __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t b
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
+}
+
+// 32 lanes x 16 consecutive columns of 32-bit values
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
 }
 
 // 32 lanes x 32 consecutive columns of 32-bit values
@@ -192,7 +203,8 @@ __device__ __forceinline__ uint4 pack4<1>(const __nv_bfloat16* v) { // 8 bf16 va
     return r;
 }
 
-constexpr int kEpiWarps = 4, kProdWarps = 8;
+constexpr int kEpiWarps = 8, kProdWarps = 7;      // 16 warps with the MMA warp: 128 registers each
+constexpr int kEpiRows = kRows * 4 / kEpiWarps;     // output rows per epilogue warp and tile (8)
 
 // OR of v over the producer warps (named barrier 1): keeps their loop decisions uniform so
 // every producer thread reaches the same named barriers
@@ -456,7 +468,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue (warps 0-3, TMEM lanes 32 w .. 32 w + 31) ----------------
+        // -------- epilogue (warp w: TMEM lanes 32 (w % 4) .. + 31, rows kEpiRows (w / 4) ..) --------
         for (int i = 0; i < n_my; i++) {
             if (*abort_flag) break;
             const int a = i & 1;
@@ -467,20 +479,21 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                 break;
             }
             tc_fence_after();
-            const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
-            const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * 128);
-            // TMEM -> registers (16 rows x 6 floats per lane) -> per-row staging in shared memory
+            const int quarter = warp & 3, part = warp >> 2;
+            const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows + part * kEpiRows;
+            const uint32_t tbase =
+                tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 128) + (uint32_t)(part * kEpiRows * 6);
+            // TMEM -> registers (8 rows x 6 floats per lane) -> per-row staging in shared memory
             // (lane l at float offset 6 l) -> 768 contiguous bytes per row with 16-byte stores
-            uint32_t v[kN];
-            tmem_ld32(tbase + 0u, *reinterpret_cast<uint32_t(*)[32]>(&v[0]));
-            tmem_ld32(tbase + 32u, *reinterpret_cast<uint32_t(*)[32]>(&v[32]));
-            tmem_ld32(tbase + 64u, *reinterpret_cast<uint32_t(*)[32]>(&v[64]));
+            uint32_t v[kEpiRows * 6];
+#pragma unroll
+            for (int c16 = 0; c16 < kEpiRows * 6 / 16; c16++) tmem_ld16(tbase + (uint32_t)(16 * c16), &v[16 * c16]);
             tmem_ld_wait();
             float* stage = sOut + warp * 192;
-            const int xw = x0 + warp * 32;                     // first x of this warp
+            const int xw = x0 + quarter * 32;                  // first x of this warp
             const int nx = min(32, ncols - xw);               // valid x of this warp
 #pragma unroll
-            for (int r = 0; r < kRows; r++) {
+            for (int r = 0; r < kEpiRows; r++) {
                 const int row = r0 + r;
                 if (row >= nrows || nx <= 0) break;           // warp-uniform
                 reinterpret_cast<float2*>(stage)[3 * lane + 0] = make_float2(__uint_as_float(v[6 * r + 0]), __uint_as_float(v[6 * r + 1]));

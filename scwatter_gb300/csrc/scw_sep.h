@@ -58,7 +58,15 @@ struct scw_sep_s {
     double* dzb = nullptr;
     double2* dExt = nullptr;               // inc[3][MF], refl[3][MF], trans[3][MF], kz_inc, kz_refl, kz_trans
     double2* dKz = nullptr;                // [Z][2][Jp] kz of the downward / upward modes
-    float2* dQ = nullptr;                  // [Z][2][3][MF][Jp] amplitudes at the modes' reference planes
+    // Interior amplitudes, in one of two forms:
+    //   halves = 2: dQ [Z][2][3][MF][Jp], the downward and upward blocks Q_dn, Q_up as given;
+    //   halves = 1 ("paired"): dQ [Z][3][MF][Jp] holds one block V and dBeta [Z][2][Jp] the mode
+    //     amplitudes, with Q_dn = V diag(beta_dn) and Q_up = S V diag(beta_up), S = diag(+1, +1, -1)
+    //     over (Ex, Ey, Ez) -- the structure of the solver's modes, whose E rows are the same
+    //     eigenvector for the two roots +-gamma and whose H rows (hence Ez) change sign.
+    int halves = 2;
+    float2* dQ = nullptr;
+    double2* dBeta = nullptr;
     bool own_Q = false;
     // host-streamed evaluation (scw_sep_eval_volume_host): copy streams, events, output slabs
     cudaStream_t up_stream = nullptr, down_stream = nullptr;

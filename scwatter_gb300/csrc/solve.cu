@@ -48,14 +48,18 @@ struct scw_solution_s {
     std::vector<cd> Sz0, Sz1, EF, x;       // MF, MF, 3MF incident, 6MF boundary solution
     std::vector<cd> gam;                   // Z x 2MF downward roots
     double2* dQ = nullptr;                 // device [Z][2][3MF][2MF]: Q_check, Q_hat (FP64)
+    float2* dV = nullptr;                  // device [Z][3][MF][2MF] complex64: the paired set's block V
+    double2* dBeta = nullptr;              // device [Z][2][2MF]: beta_dn, beta_up
     // mixed eigen-solver per slice: state (1 accepted, else FP64 fallback), refinement steps
     // used, last relative residual; empty when the FP64 solver ran throughout
     std::vector<int> eig_state, eig_steps;
     std::vector<double> eig_res;
     ~scw_solution_s() {
-        if (dQ) {
+        if (dQ || dV || dBeta) {
             ::scw::DeviceScope dev_scope_(ctx->device);
-            cudaFree(dQ);
+            if (dQ) cudaFree(dQ);
+            if (dV) cudaFree(dV);
+            if (dBeta) cudaFree(dBeta);
         }
     }
 };
@@ -256,7 +260,8 @@ __global__ void kn_kernel(const double2* __restrict__ NiF, int M0, int M1, doubl
 }
 
 // rows Ex, Ey of Q_check / Q_hat: U diag(beta);  Hm = sign (up_m Hy - wq_m Hx) for the Ez step,
-// with Hx, Hy = rows of W diag(beta) (sign -1 for the upward modes, whose H rows are -W)
+// with Hx, Hy = rows of W diag(beta) (sign -1 for the upward modes, whose H rows are -W).
+// beta == null: unit amplitudes (the paired set's block V = [U; Kn (up W_y - wq W_x)])
 __global__ void q_rows_kernel(const double2* __restrict__ U, const double2* __restrict__ Wm,
                               const double2* __restrict__ beta, int MF, double sign, const double* __restrict__ up_pz,
                               const double* __restrict__ wq_pz, double2* __restrict__ Qout, double2* __restrict__ Hm) {
@@ -264,7 +269,7 @@ __global__ void q_rows_kernel(const double2* __restrict__ U, const double2* __re
     const int n = 2 * MF;
     if (e >= (long long)n * n) return;
     const int r = (int)(e / n), j = (int)(e % n);
-    const double2 b = beta[j];
+    const double2 b = beta ? beta[j] : make_double2(1.0, 0.0);
     Qout[e] = cmul(U[e], b);
     if (Hm && r < MF) {
         const double2 hx = cmul(Wm[e], b);
@@ -754,6 +759,22 @@ scw_status record_solve(const SolvePlan& p, const SolveIn& in, const SolveWs& ws
             }
             L += 2;
         }
+        if (out.Vsep) {      // the paired set: V = [U; Kn (up W_y - wq W_x)] and beta_dn, beta_up
+            q_rows_kernel<<<nblk(nn), 256, 0, st>>>(ws.U + o, ws.W + o, nullptr, MF, 1.0, in.uppz, in.wqpz, ws.Qtmp,
+                                                   p.pz ? ws.Hm : nullptr);
+            SCW_CUDA_TRY(cudaGetLastError());
+            if (p.pz) {
+                SCW_TRY(zgemm(st, MF, n, MF, kOne, ws.Kn, MF, 0, ws.Hm, n, 0, kZero, ws.Qtmp + (size_t)n * n, n, 0, 1));
+            } else {
+                SCW_CUDA_TRY(cudaMemsetAsync(ws.Qtmp + (size_t)n * n, 0, sizeof(double2) * MF * n, st));
+            }
+            const long long cnt = (long long)M3 * n;
+            to_c64_kernel<<<nblk(cnt), 256, 0, st>>>(ws.Qtmp, out.Vsep + (size_t)l * M3 * n, cnt);
+            SCW_CUDA_TRY(cudaGetLastError());
+            SCW_CUDA_TRY(cudaMemcpyAsync(out.sepBeta + (size_t)l * 2 * n, ws.beta + (size_t)l * N4,
+                                         sizeof(double2) * 2 * n, cudaMemcpyDeviceToDevice, st));
+            L += 3;
+        }
     }
     if (out.sepKz) {
         sep_kz_kernel<<<nblk((long long)Zs * n), 256, 0, st>>>(out.gam, Zs, n, k, out.sepKz);
@@ -841,6 +862,14 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
             return fail(SCW_ERR_NOMEM, "scw_solve: cudaMalloc of the mode amplitudes");
         }
         o.Q64 = sol->dQ;
+        const size_t vbytes = sizeof(float2) * (size_t)Zs * 3 * p.MF * p.n;
+        const size_t bbytes = sizeof(double2) * (size_t)Zs * 2 * p.n;
+        if (cudaMalloc(&sol->dV, vbytes) != cudaSuccess || cudaMalloc(&sol->dBeta, bbytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SCW_ERR_NOMEM, "scw_solve: cudaMalloc of the paired mode blocks");
+        }
+        o.Vsep = sol->dV;
+        o.sepBeta = sol->dBeta;
     }
     cudaStream_t s = ctx->stream;
     if ((st = upload_inputs(p, sample, in, s)) != SCW_OK) return st;
@@ -932,6 +961,16 @@ scw_status scw_solution_info(scw_solution s, int* M0, int* M1, int* n_slices, do
     return SCW_OK;
 }
 
+scw_status scw_solution_eig_slices(scw_solution s, int* state, int* steps, double* residual) {
+    if (!s) return fail(SCW_ERR_ARG, "null solution");
+    if (s->eig_state.empty()) return fail(SCW_ERR_STATE, "scw_solution_eig_slices: the FP64 eigen-solver ran throughout");
+    const size_t Z = s->eig_state.size();
+    if (state) std::copy(s->eig_state.begin(), s->eig_state.end(), state);
+    if (steps) std::copy(s->eig_steps.begin(), s->eig_steps.begin() + Z, steps);
+    if (residual) std::copy(s->eig_res.begin(), s->eig_res.begin() + Z, residual);
+    return SCW_OK;
+}
+
 scw_status scw_solution_eig_info(scw_solution s, int* mixed, int* accepted, int* max_steps, double* max_residual,
                                  int* residual_checks) {
     if (!s) return fail(SCW_ERR_ARG, "null solution");
@@ -981,7 +1020,11 @@ scw_status scw_solution_to_sep(scw_solution s, scw_sep* out) {
     if (s->external)      // interior layers of an external-only structure sit at z = 0 with no waves
         for (int l = 1; l < Z; l++) zb[l] = 0.0;
     scw_sep sp = nullptr;
-    scw_status st = scw_sep_create(ctx, M0, M1, Z, s->external ? 0 : n, kx.data(), ky.data(), zb.data(), &sp);
+    // interior modes as a paired set: one block V per slice and the amplitudes beta (half the
+    // coefficient bytes of the two blocks Q_check, Q_hat)
+    const bool paired = !s->external && s->dV && s->dBeta;
+    scw_status st = paired ? scw_sep_create_paired(ctx, M0, M1, Z, n, kx.data(), ky.data(), zb.data(), &sp)
+                           : scw_sep_create(ctx, M0, M1, Z, s->external ? 0 : n, kx.data(), ky.data(), zb.data(), &sp);
     if (st != SCW_OK) return st;
     std::unique_ptr<scw_sep_s, scw_status (*)(scw_sep)> guard(sp, scw_sep_destroy);
     std::vector<cd> inc(3 * MF), refl(3 * MF), trans(3 * MF), kzi(MF), kzr(MF), kzt(MF);
@@ -998,7 +1041,22 @@ scw_status scw_solution_to_sep(scw_solution s, scw_sep* out) {
     st = scw_sep_set_exterior(sp, (const double*)inc.data(), (const double*)kzi.data(), (const double*)refl.data(),
                               (const double*)kzr.data(), (const double*)trans.data(), (const double*)kzt.data());
     if (st != SCW_OK) return st;
-    if (!s->external) {
+    if (paired) {
+        std::vector<cd> kzd(n), kzu(n), beta(2 * (size_t)n);
+        for (int l = 0; l < Z && st == SCW_OK; l++) {
+            for (int j = 0; j < n; j++) {
+                kzd[j] = s->gam[(size_t)l * n + j] * k;
+                kzu[j] = -s->gam[(size_t)l * n + j] * k;
+            }
+            SCW_CUDA_TRY(cudaMemcpy(beta.data(), s->dBeta + (size_t)l * 2 * n, sizeof(double2) * 2 * n,
+                                    cudaMemcpyDeviceToHost));
+            st = scw_sep_set_slice_paired(sp, l, (const double*)kzd.data(), (const double*)kzu.data(),
+                                          s->dV + (size_t)l * 3 * MF * n, (const double*)beta.data(),
+                                          (const double*)(beta.data() + n));
+        }
+        if (st != SCW_OK) return st;
+        SCW_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    } else if (!s->external) {
         const size_t blk = (size_t)3 * MF * n;
         float2* tmp = nullptr;
         if (cudaMalloc(&tmp, sizeof(float2) * 2 * blk) != cudaSuccess) {

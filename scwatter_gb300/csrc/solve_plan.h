@@ -73,6 +73,8 @@ struct SolveOut {                           // results
     float2* Qsep;                           // [Z][2][3][MF][2MF] complex64 (separable layout), or null
     double2* sepKz;                         // [Z][2][2MF] kz = +-gamma k for the separable set, or null
     double2* sepExt;                        // [12 MF] exterior blocks of the separable set, or null
+    float2* Vsep = nullptr;                 // [Z][3][MF][2MF] complex64 mode block V of the paired set, or null
+    double2* sepBeta = nullptr;             // [Z][2][2MF] its amplitudes beta_dn, beta_up (with Vsep)
     int* eig;                               // mixed eigen-solver per slice: [0, Z) state, [Z, 2Z) steps, or null
     double* eig_res;                        // [Z] last relative residual, or null
 };

@@ -10,6 +10,11 @@ read on the device by ``scw_sep_save`` / ``scw_sep_load``):
     complex128 kz[Z][2][Jp]      (Jp = J rounded up to even; entries J..Jp-1 are zero)
     complex64  Q[Z][2][3][MF][Jp]
 
+A paired set (the solver's own output, ``scw_sep_create_paired``) is written as "SCWSEP02": the
+same blocks up to kz, then complex128 beta[Z][2][Jp] and complex64 V[Z][3][MF][Jp] with
+Q_dn = V diag(beta_dn), Q_up = diag(1, 1, -1) V diag(beta_up).  :func:`read_cwf` reads both and
+returns the two-half blocks.
+
 Row p = a M1 + b of an MF block is harmonic (kx[a], ky[b]).  Every amplitude is referenced to
 its own plane: E0 exp(i kz z_ref), where the .cw record stores E0 wound to z = 0
 (sCWatter.cpp:469-482).  :func:`factor_cw` builds the set from a volume-solver ``.cw``
@@ -28,6 +33,7 @@ import numpy as np
 from .cw import CoupledWaveStructure, HomogeneousLayer
 
 MAGIC = b"SCWSEP01"
+MAGIC_PAIRED = b"SCWSEP02"
 
 
 @dataclass
@@ -59,9 +65,12 @@ class FactoredSet:
         return self.ext[3 * MF * i:3 * MF * (i + 1)].reshape(3, MF), self.ext[9 * MF + MF * i:9 * MF + MF * (i + 1)]
 
 
-def file_size(M0, M1, Z, J) -> int:
+def file_size(M0, M1, Z, J, paired=False) -> int:
     MF, Jp = M0 * M1, J + (J & 1)
-    return 8 + 24 + 8 * (M0 + M1 + Z + 1) + 16 * 12 * MF + 16 * Z * 2 * Jp + (8 * Z * 2 * 3 * MF * Jp if J else 0)
+    head = 8 + 24 + 8 * (M0 + M1 + Z + 1) + 16 * 12 * MF + 16 * Z * 2 * Jp
+    if paired:
+        return head + 16 * Z * 2 * Jp + (8 * Z * 3 * MF * Jp if J else 0)
+    return head + (8 * Z * 2 * 3 * MF * Jp if J else 0)
 
 
 def write_cwf(path, fs: FactoredSet) -> None:
@@ -78,10 +87,11 @@ def write_cwf(path, fs: FactoredSet) -> None:
 
 def read_cwf(path) -> FactoredSet:
     data = open(path, "rb").read()
-    if len(data) < 32 or data[:8] != MAGIC:
+    if len(data) < 32 or data[:8] not in (MAGIC, MAGIC_PAIRED):
         raise ValueError(f"not a factored coefficient file: {path}")
+    paired = data[:8] == MAGIC_PAIRED
     M0, M1, Z, J, rule, _ = (int(v) for v in np.frombuffer(data, "<i4", 6, 8))
-    if M0 <= 0 or M1 <= 0 or Z < 0 or J < 0 or len(data) != file_size(M0, M1, Z, J):
+    if M0 <= 0 or M1 <= 0 or Z < 0 or J < 0 or len(data) != file_size(M0, M1, Z, J, paired):
         raise ValueError("factored file size does not match its header")
     MF, Jp = M0 * M1, J + (J & 1)
     off = 32
@@ -95,7 +105,18 @@ def read_cwf(path) -> FactoredSet:
     kx, ky, zb = take("<f8", M0), take("<f8", M1), take("<f8", Z + 1)
     ext = take("<c16", 12 * MF)
     kz = take("<c16", Z * 2 * Jp).reshape(Z, 2, Jp)
-    Q = take("<c8", Z * 2 * 3 * MF * Jp).reshape(Z, 2, 3, MF, Jp) if J else np.zeros((Z, 2, 3, MF, 0), np.complex64)
+    if paired:
+        beta = take("<c16", Z * 2 * Jp).reshape(Z, 2, Jp)
+        Q = np.zeros((Z, 2, 3, MF, Jp if J else 0), np.complex64)
+        if J:
+            V = take("<c8", Z * 3 * MF * Jp).reshape(Z, 3, MF, Jp)
+            sign = np.array([1.0, 1.0, -1.0])[:, None, None]
+            for l in range(Z):
+                v = V[l].astype(np.complex128)
+                Q[l, 0] = v * beta[l, 0][None, None, :]
+                Q[l, 1] = sign * v * beta[l, 1][None, None, :]
+    else:
+        Q = take("<c8", Z * 2 * 3 * MF * Jp).reshape(Z, 2, 3, MF, Jp) if J else np.zeros((Z, 2, 3, MF, 0), np.complex64)
     return FactoredSet(M0, M1, Z, J, rule, kx, ky, zb, ext, kz, Q)
 
 

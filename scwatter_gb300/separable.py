@@ -53,6 +53,61 @@ class SeparableSet:
         return cls(ctx, h)
 
     @classmethod
+    def create_paired(cls, ctx: Context, kx, ky, z_boundaries, modes_per_half: int) -> "SeparableSet":
+        """Empty paired set (``scw_sep_create_paired``): per slice one block V and the mode
+        amplitudes, Q_dn = V diag(beta_dn), Q_up = diag(1, 1, -1) V diag(beta_up)."""
+        kx = np.ascontiguousarray(kx, dtype=np.float64)
+        ky = np.ascontiguousarray(ky, dtype=np.float64)
+        zb = np.ascontiguousarray(z_boundaries, dtype=np.float64)
+        h = ctypes.c_void_p()
+        _lib.call("scw_sep_create_paired", ctx.handle, len(kx), len(ky), len(zb) - 1, int(modes_per_half),
+                  kx.ctypes.data_as(ctypes.c_void_p), ky.ctypes.data_as(ctypes.c_void_p),
+                  zb.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
+        return cls(ctx, h)
+
+    @classmethod
+    def from_paired(cls, ctx: Context, ps, V=None) -> "SeparableSet":
+        """From a :class:`scwatter_gb300.synthetic.PairedSample`; ``V`` (host array or device
+        tensor, [Z, 3, MF, J] complex64) overrides ``ps.V``."""
+        b = ps.base
+        V = ps.V if V is None else V
+        s = cls.create_paired(ctx, b.kx, b.ky, b.z, ps.beta_dn.shape[1])
+        keep = [_c(b.inc), _c(b.kz_inc), _c(b.refl), _c(b.kz_refl), _c(b.trans), _c(b.kz_trans)]
+        _lib.call("scw_sep_set_exterior", s.handle, *[p for _, p in keep])
+        for l in range(b.Z):
+            s.set_slice_paired(l, b.gamma_dn[l] * b.k, b.gamma_up[l] * b.k, V[l], ps.beta_dn[l], ps.beta_up[l])
+            ctx.synchronize()
+        return s
+
+    def set_slice_paired(self, l, kz_dn, kz_up, V_l, beta_dn, beta_up):
+        """Slice l of a paired set: kz and amplitudes [J] complex, V_l [3, MF, J] complex64 (host
+        array or device tensor; the copy is asynchronous on the context stream)."""
+        kd, pkd = _c(kz_dn)
+        ku, pku = _c(kz_up)
+        bd, pbd = _c(beta_dn)
+        bu, pbu = _c(beta_up)
+        if hasattr(V_l, "data_ptr"):
+            vptr, keep = V_l.data_ptr(), V_l
+        else:
+            keep = np.ascontiguousarray(V_l, dtype=np.complex64)
+            vptr = keep.ctypes.data
+        _lib.call("scw_sep_set_slice_paired", self.handle, int(l), pkd, pku, ctypes.c_void_p(vptr), pbd, pbu)
+        if not hasattr(V_l, "data_ptr"):
+            self.ctx.synchronize()      # host source: finished before it goes out of scope
+
+    def form(self) -> int:
+        """2 for a two-half set, 1 for a paired set."""
+        h = ctypes.c_int()
+        _lib.call("scw_sep_form", self.handle, ctypes.byref(h))
+        return h.value
+
+    def host_block_shape(self):
+        """Shape of the amplitude array the host-buffer evaluations take: [Z, 2, 3, MF, J] for a
+        two-half set, [Z, 3, MF, J] for a paired set."""
+        M0, M1, Z, J = self.info()
+        return (Z, 2, 3, M0 * M1, J) if self.form() == 2 else (Z, 3, M0 * M1, J)
+
+    @classmethod
     def from_factored(cls, ctx: Context, fs) -> "SeparableSet":
         """From a :class:`scwatter_gb300.synthetic.FactoredSample`-like object."""
         s = cls.create(ctx, fs.kx, fs.ky, fs.z, fs.gamma_dn.shape[1])
@@ -112,12 +167,13 @@ class SeparableSet:
     def eval_volume_host(self, Q_host, x_start, y_start, z_start, dx, dy, dz, Nx, Ny, Nz, out=None,
                          method=TF32X3):
         """End-to-end volume evaluation from HOST amplitudes (``scw_sep_eval_volume_host``):
-        ``Q_host`` [Z, 2, 3, MF, J] complex64 (numpy array or CPU torch tensor, page-locked for
-        full link speed) is uploaded slice by slice while earlier slices are evaluated, and the
+        ``Q_host`` (:meth:`host_block_shape`: [Z, 2, 3, MF, J] for a two-half set, [Z, 3, MF, J]
+        for a paired set; complex64 numpy array or CPU torch tensor, page-locked for full link
+        speed) is uploaded slice by slice while earlier slices are evaluated, and the
         planes come back into ``out`` ([Nz, Ny, Nx, 3] complex64 host array or CPU tensor,
         allocated when None) as they finish.  Returns ``out``."""
         M0, M1, Z, J = self.info()
-        shape = (Z, 2, 3, M0 * M1, J)
+        shape = self.host_block_shape()
         if tuple(Q_host.shape) != shape:
             raise ValueError(f"Q_host must be {shape}, got {tuple(Q_host.shape)}")
         qptr = _host_ptr(Q_host, "Q_host")
@@ -141,9 +197,8 @@ class SeparableSet:
                        method=TF32X3):
         """Host-buffer form of :meth:`eval_slab_device` (``scw_sep_eval_slab_host``): only the
         slices the slab's planes lie in are read from ``Q_host`` [Z, 2, 3, MF, J]."""
-        M0, M1, Z, J = self.info()
-        if tuple(Q_host.shape) != (Z, 2, 3, M0 * M1, J):
-            raise ValueError(f"Q_host must be {(Z, 2, 3, M0 * M1, J)}, got {tuple(Q_host.shape)}")
+        if tuple(Q_host.shape) != self.host_block_shape():
+            raise ValueError(f"Q_host must be {self.host_block_shape()}, got {tuple(Q_host.shape)}")
         n = int(k_end) - int(k_begin)
         if out is None:
             out = np.empty((n, Ny, Nx, 3), np.complex64)

@@ -96,6 +96,15 @@ class Solution:
                     else self.Z, "max_steps": steps.value, "max_residual": res.value,
                     "residual_checks": checks.value}
 
+    def eig_slices(self):
+        """Per-slice record of the mixed eigen-solver: (state, steps, residual) arrays, state 1 =
+        refined result accepted, else the fallback's reason code; None when the FP64 solver ran."""
+        if not self.eig["mixed"]:
+            return None
+        st, steps, res = np.zeros(self.Z, np.int32), np.zeros(self.Z, np.int32), np.zeros(self.Z)
+        _lib.call("scw_solution_eig_slices", self.handle, *(ctypes.c_void_p(a.ctypes.data) for a in (st, steps, res)))
+        return st, steps, res
+
     def modes(self, l: int):
         """(Q_check, Q_hat) of slice ``l``: [3MF, 2MF] complex128 each."""
         qc = np.zeros((3 * self.MF, 2 * self.MF), np.complex128)

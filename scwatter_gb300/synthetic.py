@@ -161,3 +161,71 @@ def device_factored(M0, M1, Z, size, lam=1.0, z_center=0.0, seed=0, device="cuda
     fs = FactoredSample(M0, M1, k, kx, ky, z, gamma_dn, gamma_up, None, None, inc, refl, trans,
                         sz * k, -sz * k, sz * k)
     return fs, Q_dn, Q_up
+
+
+@dataclass
+class PairedSample:
+    """Paired form of a factored sample (the solver's mode structure): per slice one block
+    V [Z, 3, MF, J] and amplitudes beta_dn, beta_up [Z, J], with Q_dn = V diag(beta_dn) and
+    Q_up = diag(1, 1, -1) V diag(beta_up); gamma_up = -gamma_dn.  Exterior blocks as in
+    :class:`FactoredSample`."""
+    base: FactoredSample          # k grids, z, gamma, exterior blocks (its Q_dn / Q_up unused)
+    V: np.ndarray
+    beta_dn: np.ndarray
+    beta_up: np.ndarray
+
+    def to_factored(self) -> FactoredSample:
+        """The same coefficients as a two-half :class:`FactoredSample` (for the FP64 oracle)."""
+        import dataclasses
+        s = np.array([1.0, 1.0, -1.0])[None, :, None, None]
+        V = self.V.astype(np.complex128)
+        return dataclasses.replace(self.base, Q_dn=V * self.beta_dn[:, None, None, :],
+                                   Q_up=s * V * self.beta_up[:, None, None, :])
+
+
+def _paired_meta(M0, M1, Z, size, lam, z_center, rng):
+    k = 2 * PI_REF / lam
+    MF = M0 * M1
+    J = 2 * MF
+    p = np.arange(M0) - M0 // 2
+    q = np.arange(M1) - M1 // 2
+    kx = 2 * PI_REF * p / size[0]
+    ky = 2 * PI_REF * q / size[1]
+    z = z_center - size[2] / 2 + np.arange(Z + 1) * (size[2] / Z)
+    re = rng.uniform(1.0, 1.4, size=(Z, J))
+    im = rng.uniform(0.0, 0.02, size=(Z, J))
+    gamma_dn = (re + 1j * im).astype(np.complex128)
+    # eigenvector columns normalised to 1 (entries ~ 1/sqrt(3 MF)); amplitudes ~ 1/sqrt(2 MF)
+    bd = (rng.standard_normal((Z, J)) + 1j * rng.standard_normal((Z, J))) / np.sqrt(2 * J)
+    bu = 0.3 * (rng.standard_normal((Z, J)) + 1j * rng.standard_normal((Z, J))) / np.sqrt(2 * J)
+    sz = np.sqrt((1.0 + 0j) - (np.repeat(kx, M1) / k) ** 2 - (np.tile(ky, M0) / k) ** 2)
+    inc = np.zeros((3, MF), np.complex128)
+    inc[0, (M0 // 2) * M1 + M1 // 2] = 1.0
+    refl = (rng.standard_normal((3, MF)) + 1j * rng.standard_normal((3, MF))) * 0.05
+    trans = (rng.standard_normal((3, MF)) + 1j * rng.standard_normal((3, MF))) * 0.5
+    base = FactoredSample(M0, M1, k, kx, ky, z, gamma_dn, -gamma_dn, None, None, inc, refl, trans,
+                          sz * k, -sz * k, sz * k)
+    return base, bd, bu
+
+
+def make_paired(M0=20, M1=20, Z=20, size=(64.0, 64.0, 20.0), lam=1.0, z_center=0.0, seed=0) -> PairedSample:
+    """Seeded paired sample on the host (V complex64)."""
+    rng = np.random.default_rng(seed)
+    base, bd, bu = _paired_meta(M0, M1, Z, size, lam, z_center, rng)
+    MF, J = M0 * M1, 2 * M0 * M1
+    shp = (Z, 3, MF, J)
+    V = ((rng.standard_normal(shp) + 1j * rng.standard_normal(shp)) / np.sqrt(6 * MF)).astype(np.complex64)
+    return PairedSample(base, V, bd, bu)
+
+
+def device_paired(M0, M1, Z, size, lam=1.0, z_center=0.0, seed=0, device="cuda"):
+    """Paired sample with the large block V drawn on the GPU (torch, seeded) as a complex64
+    [Z, 3, MF, 2MF] tensor.  Returns (PairedSample with V None, V)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    base, bd, bu = _paired_meta(M0, M1, Z, size, lam, z_center, rng)
+    MF = M0 * M1
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    V = torch.randn((Z, 3, MF, 2 * MF), dtype=torch.complex64, device=device, generator=g) / float(np.sqrt(3 * MF))
+    return PairedSample(base, None, bd, bu), V

@@ -178,3 +178,98 @@ def test_volume_from_host_rejects_wrong_shape(ctx):
     s = SeparableSet.from_factored(ctx, fs)
     with pytest.raises(ValueError):
         s.eval_volume_host(np.zeros((2, 2, 3, 16, 31), np.complex64), 0, 0, 0, 1, 1, 1, 4, 4, 4)
+
+
+def _volume_oracle(fs, grid):
+    from scwatter_gb300 import synthetic
+    Pi, zsl, Pr, Pt = synthetic.to_cw_arrays(fs)
+    W, b, e, zl = so.unpack(so.CW(Pi=Pi, z=zsl, Pr=Pr, Pt=Pt))
+    x0, y0, z0, dx, dy, dz, Nx, Ny, Nz = grid
+    ix = (x0 + dx * np.arange(Nx, dtype=np.float32)).astype(np.float32)
+    iy = (y0 + dy * np.arange(Ny, dtype=np.float32)).astype(np.float32)
+    iz = (z0 + dz * np.arange(Nz, dtype=np.float32)).astype(np.float32)
+    P = np.stack(np.meshgrid(iz, iy, ix, indexing="ij"), -1)[..., ::-1]
+    return ol.eval_points_f64(W, b, e, ol.thresholds(zl, "gpu"), P.reshape(-1, 3)).reshape(Nz, Ny, Nx, 3)
+
+
+def _eval_device(ctx, sep, grid, method):
+    import torch
+    *geo, Nx, Ny, Nz = grid
+    o = torch.zeros((Nz, Ny, Nx, 3), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    sep.eval_volume_device(*geo, Nx, Ny, Nz, o.data_ptr(), method=method)
+    ctx.synchronize()
+    return o.cpu().numpy()
+
+
+PAIRED_GRID = (np.float32(-7), np.float32(-6), np.float32(-2.5), np.float32(0.4), np.float32(0.55), np.float32(0.5),
+               37, 21, 11)
+
+
+@pytest.mark.parametrize("method", [1, 2, 3])
+def test_paired_set_volume(ctx, method):
+    """A paired set (one block V per slice, amplitudes folded into the FP64 phases) against the
+    FP64 oracle summing the same waves, Q_dn = V diag(beta_dn), Q_up = diag(1, 1, -1) V diag(beta_up)."""
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import SeparableSet
+    ps = synthetic.make_paired(M0=6, M1=4, Z=3, size=(12.0, 10.0, 3.0), seed=5)
+    sep = SeparableSet.from_paired(ctx, ps)
+    assert sep.form() == 1
+    got = _eval_device(ctx, sep, PAIRED_GRID, method)
+    ref = _volume_oracle(ps.to_factored(), PAIRED_GRID)
+    assert max(rel_l2(got, ref, floor=0.0)) < TOL[method]
+
+
+def test_paired_set_matches_two_half_set(ctx):
+    """The same coefficients as a paired set and as a two-half set give the same volume."""
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import TF32X3, SeparableSet
+    ps = synthetic.make_paired(M0=8, M1=6, Z=4, size=(16.0, 12.0, 4.0), seed=8)
+    a = _eval_device(ctx, SeparableSet.from_paired(ctx, ps), PAIRED_GRID, TF32X3)
+    b = _eval_device(ctx, SeparableSet.from_factored(ctx, ps.to_factored()), PAIRED_GRID, TF32X3)
+    assert max(rel_l2(a, b, floor=0.0)) < 1e-6
+
+
+@pytest.mark.parametrize("odd", [False, True])
+def test_paired_set_from_host_amplitudes(ctx, odd):
+    """scw_sep_eval_volume_host on a paired set: one block [3][MF][J] per slice from host memory."""
+    import dataclasses
+    import torch
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import TF32X3, SeparableSet
+    ps = synthetic.make_paired(M0=6, M1=4, Z=5, size=(12.0, 10.0, 5.0), seed=12)
+    if odd:
+        J = 2 * 24 - 3
+        base = dataclasses.replace(ps.base, gamma_dn=ps.base.gamma_dn[:, :J], gamma_up=ps.base.gamma_up[:, :J])
+        ps = dataclasses.replace(ps, base=base, V=ps.V[..., :J], beta_dn=ps.beta_dn[:, :J], beta_up=ps.beta_up[:, :J])
+    grid = (np.float32(-7), np.float32(-6), np.float32(-3.5), np.float32(0.3), np.float32(0.5), np.float32(0.1),
+            45, 23, 70)
+    ref = _eval_device(ctx, SeparableSet.from_paired(ctx, ps), grid, TF32X3)
+    zero = dataclasses.replace(ps, V=np.zeros_like(ps.V))
+    s = SeparableSet.from_paired(ctx, zero)
+    assert s.host_block_shape() == ps.V.shape
+    Vh = torch.from_numpy(np.ascontiguousarray(ps.V)).pin_memory()
+    s.set_streaming(chunk_bytes=1, slab_bytes=3 * 45 * 23 * 24)
+    got = s.eval_volume_host(Vh, *grid, method=TF32X3)
+    assert max(rel_l2(got, ref, floor=0.0)) < 1e-6
+
+
+def test_paired_factored_file_round_trip(ctx, tmp_path):
+    """A paired set is written as SCWSEP02 (half the amplitude bytes), reads back to the same
+    field bit for bit, and the host reader rebuilds its two-half blocks."""
+    from scwatter_gb300 import factored, synthetic
+    from scwatter_gb300.separable import TF32X3, SeparableSet
+    ps = synthetic.make_paired(M0=5, M1=4, Z=3, size=(10.0, 8.0, 3.0), seed=2)
+    s1 = SeparableSet.from_paired(ctx, ps)
+    f = tmp_path / "p.cwf"
+    s1.save(f)
+    assert f.read_bytes()[:8] == b"SCWSEP02"
+    s2 = SeparableSet.load(ctx, f)
+    assert s2.form() == 1
+    a = _eval_device(ctx, s1, PAIRED_GRID, TF32X3)
+    b = _eval_device(ctx, s2, PAIRED_GRID, TF32X3)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    host = factored.read_cwf(f)
+    fs = ps.to_factored()
+    np.testing.assert_allclose(host.Q[:, 0], fs.Q_dn, rtol=0, atol=1e-7 * np.abs(fs.Q_dn).max())
+    np.testing.assert_allclose(host.Q[:, 1], fs.Q_up, rtol=0, atol=1e-7 * np.abs(fs.Q_up).max())

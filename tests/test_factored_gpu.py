@@ -68,7 +68,7 @@ def test_factored_file_from_cw_and_errors(ctx, tmp_path):
     assert all(np.array_equal(a, b) for a, b in zip(e1, e2))
     data = f.read_bytes()
     bad = tmp_path / "bad.cwf"
-    for blob in (data[:-8], b"SCWSEP02" + data[8:], data[:20]):
+    for blob in (data[:-8], b"SCWSEP99" + data[8:], b"SCWSEP02" + data[8:], data[:20]):
         bad.write_bytes(blob)
         with pytest.raises(_lib.ScwError):
             sp.SeparableSet.load(ctx, bad)

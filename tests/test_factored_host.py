@@ -93,3 +93,38 @@ def test_streaming_conversion_matches_in_memory(tmp_path, name):
     (tmp_path / "t.cw").write_bytes(open(os.path.join(GOLDEN, name), "rb").read()[:-50])
     with pytest.raises(ValueError):
         factored.convert_cw_file(tmp_path / "t.cw", tmp_path / "t.cwf")
+
+
+def test_paired_file_read_on_the_host(tmp_path):
+    """SCWSEP02 (paired set: beta and one block V per slice) read without a GPU: the two-half
+    blocks are Q_dn = V diag(beta_dn), Q_up = diag(1, 1, -1) V diag(beta_up)."""
+    import numpy as np
+    from scwatter_gb300 import factored
+    rng = np.random.default_rng(3)
+    M0, M1, Z, J = 3, 2, 2, 12
+    MF = M0 * M1
+    kx, ky, zb = rng.standard_normal(M0), rng.standard_normal(M1), np.arange(Z + 1.0)
+    ext = rng.standard_normal(12 * MF) + 1j * rng.standard_normal(12 * MF)
+    kz = rng.standard_normal((Z, 2, J)) + 1j * rng.standard_normal((Z, 2, J))
+    beta = rng.standard_normal((Z, 2, J)) + 1j * rng.standard_normal((Z, 2, J))
+    V = (rng.standard_normal((Z, 3, MF, J)) + 1j * rng.standard_normal((Z, 3, MF, J))).astype(np.complex64)
+    path = tmp_path / "p.cwf"
+    with open(path, "wb") as f:
+        f.write(b"SCWSEP02")
+        f.write(np.array([M0, M1, Z, J, 0, 0], "<i4").tobytes())
+        for a in (kx, ky, zb):
+            f.write(a.astype("<f8").tobytes())
+        for a in (ext, kz, beta):
+            f.write(a.astype("<c16").tobytes())
+        f.write(V.astype("<c8").tobytes())
+    assert path.stat().st_size == factored.file_size(M0, M1, Z, J, paired=True)
+    fs = factored.read_cwf(path)
+    s = np.array([1.0, 1.0, -1.0])[:, None, None]
+    for l in range(Z):
+        v = V[l].astype(np.complex128)
+        np.testing.assert_allclose(fs.Q[l, 0], (v * beta[l, 0]).astype(np.complex64))
+        np.testing.assert_allclose(fs.Q[l, 1], (s * v * beta[l, 1]).astype(np.complex64))
+    path.write_bytes(path.read_bytes()[:-8])
+    import pytest
+    with pytest.raises(ValueError):
+        factored.read_cwf(path)

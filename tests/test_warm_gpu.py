@@ -135,10 +135,19 @@ def test_trained_network_beats_homogeneous_guess(ctx):
     PQ = torch.cat([lp.PQ for lp in probs[80:]])
     W_m, V_m, acc_m, st_m = warm_eig(ctx, PQ, torch.from_numpy(pred).cuda(), modes[ntr:])
     _, _, acc_b, st_b = warm_eig(ctx, PQ, torch.from_numpy(bases[ntr:]).cuda(), modes[ntr:])
+    # why per-eigenpair inverse iteration is not accepted: it reaches the intended eigenpair only
+    # when the shift lies within half the gap to the nearest other eigenvalue
+    truth = eigs[ntr:]
+    gaps = np.array([[np.min(np.abs(row[i] - np.delete(row, i))) for i in range(len(row))] for row in truth])
+    reach_m = float(np.mean(np.abs(pred - truth) < 0.5 * gaps))
+    reach_b = float(np.mean(np.abs(bases[ntr:] - truth) < 0.5 * gaps))
     print(f"held-out layers {len(acc_m)}: accepted with network {acc_m.sum()} (mean RQI iterations "
           f"{st_m['mean_iterations']:.2f}, repaired tasks {st_m['repaired']}), with the homogeneous guess "
           f"{acc_b.sum()} ({st_b['mean_iterations']:.2f}, {st_b['repaired']}); "
-          f"mean |shift - eigenvalue| {err_mlp:.3e} vs {err_base:.3e}")
-    assert acc_m.sum() >= acc_b.sum()
-    assert st_m["repaired"] <= st_b["repaired"]
+          f"mean |shift - eigenvalue| {err_mlp:.3e} vs {err_base:.3e}; shifts within half the nearest gap "
+          f"{reach_m:.3f} vs {reach_b:.3f}")
+    # strict gains of the network over the homogeneous-medium guess: closer shifts, more of them
+    # inside their eigenvalue's half gap, less repair work
+    assert reach_m > reach_b
+    assert st_m["repaired"] < st_b["repaired"]
     assert _max_residual(PQ, W_m, V_m) < 1e-11         # accepted or fallen back, always correct

@@ -276,15 +276,19 @@ __global__ void sep_rows_kernel(const float2* __restrict__ C, const float2* __re
 
 // Stage 2a for a volume: T[k*Ny + j][c][a] = sum_b Ey[b][j] C[k][c][a*M1 + b].
 // One CTA per (z-plane k, block of kRowsBlk rows j): C[k] is staged transposed ([c][b][a],
-// so lanes with consecutive a read consecutive words) with the block's Ey phases.
+// so lanes with consecutive a read consecutive words) with the block's Ey phases.  Each thread
+// computes a kRowsT x 2 block of outputs (rows j, two adjacent columns (c, a)): per harmonic b
+// it loads kRowsT row phases (the same for the warp: broadcast) and one column pair (16 bytes,
+// consecutive across the warp) for 2 kRowsT complex multiply-adds.
 constexpr int kRowsBlk = 64;
+constexpr int kRowsT = 4;
 
 __global__ void __launch_bounds__(256)
 sep_rows_volume_kernel(const float2* __restrict__ C, const float2* __restrict__ tabY, int Ny, int M0, int M1,
                        float2* __restrict__ T) {
     extern __shared__ float2 sm2[];
-    float2* sC = sm2;                              // [3][M1][M0]
-    float2* sR = sm2 + 3 * M0 * M1;                // [kRowsBlk][M1]
+    float2* sC = sm2;                              // [3][M1][M0] (+1 pad entry for odd M0)
+    float2* sR = sm2 + 3 * M0 * M1 + 2;            // [kRowsBlk][M1]
     const int k = blockIdx.y;
     const int j0 = blockIdx.x * kRowsBlk;
     const int MF = M0 * M1;
@@ -293,25 +297,46 @@ sep_rows_volume_kernel(const float2* __restrict__ C, const float2* __restrict__ 
         const int c = e / MF, p = e % MF, a = p / M1, b = p % M1;
         sC[(c * M1 + b) * M0 + a] = Ck[e];
     }
+    if (threadIdx.x < 2) sC[3 * MF + threadIdx.x] = make_float2(0.f, 0.f);
     for (int e = threadIdx.x; e < kRowsBlk * M1; e += blockDim.x) {
         const int r = e / M1, b = e % M1;
         sR[e] = (j0 + r < Ny) ? tabY[(long long)b * Ny + j0 + r] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     const int ncol = 3 * M0;
-    for (int e = threadIdx.x; e < kRowsBlk * ncol; e += blockDim.x) {
-        const int r = e / ncol, col = e % ncol;
-        if (j0 + r >= Ny) continue;
-        const int c = col / M0, a = col % M0;
-        const float2* cp = sC + c * M1 * M0 + a;
-        const float2* rp = sR + r * M1;
-        float sr = 0.f, si = 0.f;
+    const int npair = (ncol + 1) / 2;
+    const int nitems = (kRowsBlk / kRowsT) * npair;
+    for (int it = threadIdx.x; it < nitems; it += blockDim.x) {
+        const int rb = it / npair, q = it % npair;
+        const int r0 = rb * kRowsT;
+        if (j0 + r0 >= Ny) continue;
+        const int col0 = 2 * q, col1 = min(2 * q + 1, ncol - 1);
+        const int c0 = col0 / M0, a0 = col0 % M0, c1 = col1 / M0, a1 = col1 % M0;
+        const float2* cp0 = sC + c0 * M1 * M0 + a0;
+        const float2* cp1 = sC + c1 * M1 * M0 + a1;
+        const float2* rp = sR + r0 * M1;
+        float acc[kRowsT][2][2];
+#pragma unroll
+        for (int i = 0; i < kRowsT; i++) acc[i][0][0] = acc[i][0][1] = acc[i][1][0] = acc[i][1][1] = 0.f;
         for (int b = 0; b < M1; b++) {
-            const float2 rv = rp[b], cv = cp[b * M0];
-            sr = fmaf(rv.x, cv.x, fmaf(-rv.y, cv.y, sr));
-            si = fmaf(rv.x, cv.y, fmaf(rv.y, cv.x, si));
+            const float2 v0 = cp0[b * M0], v1 = cp1[b * M0];
+#pragma unroll
+            for (int i = 0; i < kRowsT; i++) {
+                const float2 rv = rp[i * M1 + b];
+                acc[i][0][0] = fmaf(rv.x, v0.x, fmaf(-rv.y, v0.y, acc[i][0][0]));
+                acc[i][0][1] = fmaf(rv.x, v0.y, fmaf(rv.y, v0.x, acc[i][0][1]));
+                acc[i][1][0] = fmaf(rv.x, v1.x, fmaf(-rv.y, v1.y, acc[i][1][0]));
+                acc[i][1][1] = fmaf(rv.x, v1.y, fmaf(rv.y, v1.x, acc[i][1][1]));
+            }
         }
-        T[(((long long)k * Ny + j0 + r) * 3 + c) * M0 + a] = make_float2(sr, si);
+#pragma unroll
+        for (int i = 0; i < kRowsT; i++) {
+            const int j = j0 + r0 + i;
+            if (j >= Ny) break;
+            float2* trow = T + ((long long)k * Ny + j) * 3 * M0;
+            trow[c0 * M0 + a0] = make_float2(acc[i][0][0], acc[i][0][1]);
+            if (col1 != col0) trow[c1 * M0 + a1] = make_float2(acc[i][1][0], acc[i][1][1]);
+        }
     }
 }
 
@@ -549,7 +574,7 @@ static scw_status sep_plan_finish(const scw_sep_s* s, SepEvalPlan& p) {
     else if (p.kind == 1) { p.nrows = p.Nb; p.ncols = p.Na; p.Mk = M0; }
     else { p.nrows = p.Nb; p.ncols = p.Na; p.Mk = M1; }
     if (p.kind == 0) {
-        const size_t smem = (size_t)(3 * M0 * M1 + kRowsBlk * M1) * sizeof(float2);
+        const size_t smem = (size_t)(3 * M0 * M1 + 2 + kRowsBlk * M1) * sizeof(float2);
         if (smem > 200 * 1024) return fail(SCW_ERR_UNSUPPORTED, "harmonic grid too large for the row stage");
     }
     // phases for the PGroups: at most nz groups
@@ -625,7 +650,7 @@ scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, 
         if ((st = launch_table(ctx, s->dkx, M0, p.a0, p.da, Na, tabA)) != SCW_OK) return st;
         if ((st = launch_table(ctx, s->dky, M1, p.b0, p.db, Nb, tabB)) != SCW_OK) return st;
         {
-            const size_t smem = (size_t)(3 * M0 * M1 + kRowsBlk * M1) * sizeof(float2);
+            const size_t smem = (size_t)(3 * M0 * M1 + 2 + kRowsBlk * M1) * sizeof(float2);
             SCW_CUDA_TRY(cudaFuncSetAttribute(sep_rows_volume_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem));
             dim3 grid((Nb + kRowsBlk - 1) / kRowsBlk, Nz);

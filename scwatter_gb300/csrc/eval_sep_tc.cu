@@ -23,9 +23,13 @@
 //   warps 8-14  producers: build B (hi, lo) of the next tile into one of two shared buffers,
 //               writing whole 16-byte core rows in address order (no bank conflicts)
 //   warp 15     one thread issues the MMAs into one of two TMEM accumulators and commits them
-// A (hi, lo) is built once by all warps before the roles split.  Operands use the SWIZZLE_NONE
-// K-major canonical layout: 8-row x 16-byte core matrices stored contiguously, LBO = 128 B
-// between core matrices along K, SBO = (K bytes / 16) * 128 B between 8-row groups.
+// A (hi, lo), the x-phase table of the CTA's x tile, is written once into tensor memory by warps
+// 0-3 (lane x = row x, one 32-bit column per tf32 element or per pair of bf16 elements, at
+// columns 256 and 256 + K columns) and read from there by every MMA, so the tensor core's operand
+// reads from shared memory are B's alone.  TMEM columns: accumulators at 0 and 128 (96 each),
+// A hi / lo above 256.  B uses the SWIZZLE_NONE K-major canonical layout in shared memory:
+// 8-row x 16-byte core matrices stored contiguously, LBO = 128 B between core matrices along K,
+// SBO = (K bytes / 16) * 128 B between 8-row groups.
 // Every mbarrier wait is bounded; on timeout the kernel records an error, waits (bounded)
 // for its own MMAs, frees its TMEM and returns, and the host reports SCW_ERR_TIMEOUT.
 #include <cuda_bf16.h>
@@ -41,7 +45,8 @@ namespace tc {
 constexpr int kM = 128;          // x-values per tile (TMEM lanes)
 constexpr int kRows = 16;        // output rows per tile
 constexpr int kN = kRows * 6;    // 96 accumulator columns per tile
-constexpr uint32_t kTmemCols = 512;     // two 96-column accumulators at columns 0 and 128; whole TMEM (1 CTA / SM)
+constexpr uint32_t kTmemCols = 512;     // accumulators at columns 0 and 128, A above kAcol; whole TMEM (1 CTA / SM)
+constexpr uint32_t kAcol = 256;         // first TMEM column of A (hi), then A (lo)
 constexpr long long kSpinLimit = 1ll << 22;   // polls per mbarrier wait before giving up
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -100,6 +105,32 @@ __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t b
             : "memory");
     }
 }
+
+// the same with A read from tensor memory at a_tmem (lanes 0..M-1, K along the columns)
+template <int kKind>
+__device__ __forceinline__ void umma_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    if (kKind == 0) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+            "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(acc)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+            "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(acc)
+            : "memory");
+    }
+}
+
+// this warp's 32 lanes x 8 consecutive columns of 32-bit values
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+                 "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -185,6 +216,18 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// one 32-bit TMEM column: a tf32 element, or two bf16 elements (the first in the low half)
+template <int kKind>
+__device__ __forceinline__ uint32_t pack1(const typename Split<kKind>::T* v);
+
+template <>
+__device__ __forceinline__ uint32_t pack1<0>(const float* v) { return __float_as_uint(v[0]); }
+
+template <>
+__device__ __forceinline__ uint32_t pack1<1>(const __nv_bfloat16* v) {
+    return (uint32_t)__bfloat16_as_ushort(v[0]) | ((uint32_t)__bfloat16_as_ushort(v[1]) << 16);
+}
+
 template <int kKind>
 __device__ __forceinline__ uint4 pack4(const typename Split<kKind>::T* v);
 
@@ -232,11 +275,9 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     const uint32_t kbytes = (uint32_t)Kp * EB;
     const int KC = (int)(kbytes / 16);                        // 16-byte core columns along K
     const uint32_t sbo = (uint32_t)KC * 128;
-    const uint32_t a_bytes = (kM / 8) * sbo;
     const uint32_t b_bytes = (kN / 8) * sbo;
-    unsigned char* sA_hi = smem;
-    unsigned char* sA_lo = sA_hi + a_bytes;
-    unsigned char* sB0 = sA_lo + a_bytes;                     // slot s, part h: sB0 + (2 s + h) b_bytes
+    const uint32_t acols = kbytes / 4;                        // TMEM columns of A (hi or lo): K * EB / 4
+    unsigned char* sB0 = smem;                                // slot s, part h: sB0 + (2 s + h) b_bytes
     float2* sT = reinterpret_cast<float2*>(sB0 + 4 * b_bytes);   // staged T tile [kRows * 3][tstr]
     const int t_tile = kRows * 3 * Mk;                           // float2 of T per tile
     // fast producer path: Mk a multiple of the elements per core row; T rows padded in shared
@@ -256,7 +297,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     const int ntiles = (nrows + kRows - 1) / kRows;
     const int n_my = blockIdx.y < ntiles ? (ntiles - 1 - (int)blockIdx.y) / (int)gridDim.y + 1 : 0;
 
-    for (uint32_t o = tid * 16; o < 2 * a_bytes + 4 * b_bytes; o += kWsThreads * 16)
+    for (uint32_t o = tid * 16; o < 4 * b_bytes; o += kWsThreads * 16)
         *reinterpret_cast<uint4*>(smem + o) = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int i = 0; i < 2; i++) {
@@ -273,30 +314,40 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         tmem_relinquish();
     }
     __syncthreads();
-    // A: the phase table of this x tile, written as whole core rows
-    for (int g = tid; g < kM * KC; g += kWsThreads) {
-        const int x = g & 7 | ((g / (8 * KC)) << 3);         // g = ((x / 8) * KC + kc) * 8 + x % 8
-        const int kc = (g >> 3) % KC;
-        const int xg = x0 + x;
-        E hi[EPC], lo[EPC];
+    const uint32_t tmem = *tmem_slot;
+    // A: the phase table of this x tile into TMEM, lane x = x0 + 32 w + lane (warps 0-3), 8 columns
+    // per store: tf32 one element per column, bf16 elements 2c (low half) and 2c + 1 per column c
+    if (warp < 4) {
+        const int xg = x0 + warp * 32 + lane;
+        constexpr int EPW = 4 / EB;                           // elements per 32-bit column
+        for (uint32_t c0 = 0; c0 < acols; c0 += 8) {
+            uint32_t vh[8], vl[8];
 #pragma unroll
-        for (int e = 0; e < EPC; e++) {
-            const int k = kc * EPC + e;
-            float v = 0.f;
-            if (xg < ncols && k < 2 * Mk) {
-                const float2 f = F[(long long)(k < Mk ? k : k - Mk) * ncols + xg];
-                v = k < Mk ? f.x : f.y;
+            for (int i = 0; i < 8; i++) {
+                E hi[EPW], lo[EPW];
+#pragma unroll
+                for (int e = 0; e < EPW; e++) {
+                    const int k = ((int)c0 + i) * EPW + e;
+                    float v = 0.f;
+                    if (xg < ncols && k < 2 * Mk) {
+                        const float2 f = F[(long long)(k < Mk ? k : k - Mk) * ncols + xg];
+                        v = k < Mk ? f.x : f.y;
+                    }
+                    Split<kKind>::split(v, hi[e], lo[e]);
+                }
+                vh[i] = pack1<kKind>(hi);
+                vl[i] = pack1<kKind>(lo);
             }
-            Split<kKind>::split(v, hi[e], lo[e]);
+            const uint32_t lanes = (uint32_t)(warp * 32) << 16;
+            tmem_st8(tmem + lanes + kAcol + c0, vh);
+            tmem_st8(tmem + lanes + kAcol + acols + c0, vl);
         }
-        *reinterpret_cast<uint4*>(sA_hi + (uint32_t)g * 16) = pack4<kKind>(hi);
-        *reinterpret_cast<uint4*>(sA_lo + (uint32_t)g * 16) = pack4<kKind>(lo);
+        tmem_st_wait();
     }
     fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
 
     if (warp >= kEpiWarps && warp < kEpiWarps + kProdWarps) {
         // ---------------- producers ----------------
@@ -451,13 +502,14 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                 }
                 tc_fence_after();
                 const uint32_t d = tmem + (uint32_t)(s * 128);
-                const uint32_t a_hi = smem_u32(sA_hi), a_lo = smem_u32(sA_lo);
+                const uint32_t a_hi = tmem + kAcol, a_lo = tmem + kAcol + acols;
                 const uint32_t b_hi = smem_u32(sB0 + (2 * s) * b_bytes), b_lo = smem_u32(sB0 + (2 * s + 1) * b_bytes);
                 for (int ks = 0; ks < nksteps; ks++) {
-                    const uint32_t ko = (uint32_t)ks * 256u;    // 32 bytes of K = two 16-byte core columns
-                    umma<kKind>(d, make_desc(a_hi + ko, 128, sbo), make_desc(b_hi + ko, 128, sbo), idesc, ks > 0);
-                    umma<kKind>(d, make_desc(a_hi + ko, 128, sbo), make_desc(b_lo + ko, 128, sbo), idesc, 1);
-                    umma<kKind>(d, make_desc(a_lo + ko, 128, sbo), make_desc(b_hi + ko, 128, sbo), idesc, 1);
+                    const uint32_t ko = (uint32_t)ks * 256u;    // 32 bytes of K = two 16-byte core columns of B
+                    const uint32_t ka = (uint32_t)ks * 8u;      // the same 32 bytes of K = 8 TMEM columns of A
+                    umma_ta<kKind>(d, a_hi + ka, make_desc(b_hi + ko, 128, sbo), idesc, ks > 0);
+                    umma_ta<kKind>(d, a_hi + ka, make_desc(b_lo + ko, 128, sbo), idesc, 1);
+                    umma_ta<kKind>(d, a_lo + ka, make_desc(b_hi + ko, 128, sbo), idesc, 1);
                 }
                 umma_commit(&empty_b[s]);
                 umma_commit(&acc_full[s]);
@@ -531,8 +583,9 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
     const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * (Mk + 4) * 8 + 127) / 128 * 128;   // padded rows
-    const size_t smem = (tc::kM / 8) * sbo * 2 + (tc::kN / 8) * sbo * 4 + t_tile_bytes + tc::kEpiWarps * 192 * 4 + 128;
+    const size_t smem = (tc::kN / 8) * sbo * 4 + t_tile_bytes + tc::kEpiWarps * 192 * 4 + 128;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
+    if (tc::kAcol + 2 * (size_t)Kp * EB / 4 > tc::kTmemCols) return SCW_ERR_UNSUPPORTED;   // A (hi, lo) in TMEM
     if (!ctx->tc_err) {
         if (cudaMalloc(&ctx->tc_err, sizeof(int)) != cudaSuccess) return fail(SCW_ERR_NOMEM, "cudaMalloc error flag");
     }

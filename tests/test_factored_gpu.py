@@ -40,10 +40,14 @@ def test_factored_file_round_trip(ctx, tmp_path):
     s1.save(f)
     s2 = sp.SeparableSet.load(ctx, f)
     assert s1.info() == s2.info()
+    # a solve gives a paired set (SCWSEP02): kz and beta [Z][2][Jp] complex128, one block V
+    # [Z][3][MF][Jp] complex64 -- half the amplitude bytes of the two-block file
+    assert s1.form() == 1 and s2.form() == 1
+    assert f.read_bytes()[:8] == b"SCWSEP02"
     MF, Z = 20, 3
     J = 2 * MF
     Jp = J + (J & 1)
-    want = 8 + 24 + 8 * (4 + 5 + Z + 1) + 16 * 12 * MF + 16 * Z * 2 * Jp + 8 * Z * 2 * 3 * MF * Jp
+    want = 8 + 24 + 8 * (4 + 5 + Z + 1) + 16 * 12 * MF + 2 * 16 * Z * 2 * Jp + 8 * Z * 3 * MF * Jp
     assert os.path.getsize(f) == want
     for method in (sp.FP32, sp.TF32X3):
         e1 = s1.evaluate_planes_host(-8.0, -8.0, -3.0, 0.5, -0.25, 0.75, 0.5, 32, method=method)

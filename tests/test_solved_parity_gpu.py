@@ -6,6 +6,13 @@ slices (24 x 24 points each), the separable evaluator (FP32 SIMT, tcgen05 3xTF32
 output GEMMs) and the plain summation kernel are compared with the FP64 oracle sum over the same
 region's waves.  Errors are relative L2 per field component, NOT floored: a near-zero
 component is measured against its own norm.
+
+Ey, the cross-polarised component, is about 5e-4 of the field here, and the mode terms that
+make it up cancel: the sum of their magnitudes is ~1e4 times |Ey| (Ex: ~16).  Any FP32
+representation of the terms (coefficients and phases rounded to complex64 alone give ~7e-5 on
+one slice, measured on the CPU) then shows up magnified in Ey's own relative error.  The
+thresholds below are the measured errors with a margin: 1e-5 for Ex and Ez, and for Ey a bound
+that the plain FP32 summation (the reference's arithmetic) misses by a factor of about 5.
 """
 import numpy as np
 import pytest
@@ -15,7 +22,9 @@ from oracle import sep_oracle as sepo
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp32": 1e-5, "tf32x3": 1e-5, "bf16x3": 1e-4, "plain": 2e-5}
+# [Ex, Ey, Ez] per form
+TOL = {"fp32": (1e-5, 4e-5, 1e-5), "tf32x3": (1e-5, 4e-5, 1e-5), "bf16x3": (2e-5, 4e-5, 2e-5),
+       "plain": (2e-5, 2e-4, 2e-5)}
 SLICES = (3, 8, 12, 17)
 N = 24
 
@@ -78,6 +87,11 @@ def test_solved_sample_fp64_parity(solved):
         got = np.concatenate([p[0] for p in pairs])
         ref = np.concatenate([p[1] for p in pairs])
         report[name] = _rel(got, ref)
+    norms = np.linalg.norm(ref, axis=0) / np.linalg.norm(ref)
+    print("component norms / field norm [Ex, Ey, Ez]:", norms)
     print("rel L2 vs FP64 [Ex, Ey, Ez]:", report)
     for name, e in report.items():
-        assert max(e) < TOL[name], (name, e)
+        assert all(ec < tc for ec, tc in zip(e, TOL[name])), (name, e)
+    # the separable forms are more accurate than the plain FP32 sum on every component
+    for name in ("fp32", "tf32x3"):
+        assert all(a <= b for a, b in zip(report[name], report["plain"])), (name, report)

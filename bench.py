@@ -776,7 +776,8 @@ def warm_leg(args):
 def probe(kind):
     """Small single-shot cases for ncu captures (one pass of the kernels named, nothing timed):
     ``eig-mixed``: the mixed eigen-solver on the first 2 slices of the sphere sample (n = 800);
-    ``zgemm``: 4 batched 800 x 800 x 800 complex128 products."""
+    ``zgemm``: 4 batched 800 x 800 x 800 complex128 products;
+    ``plain``: the plain summation kernel on a 32 x 32 patch of the config-2 set (two launches)."""
     import ctypes
     import torch
     from scwatter_gb300 import _lib, samples
@@ -796,6 +797,25 @@ def probe(kind):
         _lib.call("scw_zgeev_mixed", ctx.handle, n, ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(W.data_ptr()),
                   ctypes.c_void_p(V.data_ptr()), Z, ctypes.c_void_p(acc.ctypes.data), None, None)
         print(json.dumps({"probe": kind, "n": n, "matrices": Z, "accepted": acc.tolist()}))
+    elif kind == "plain":
+        # the plain summation kernel alone: a 32 x 32 xy patch inside one slice of the config-2
+        # synthetic set (2 MF x 2 MF = 10.24e6 waves per point; 1.05e10 points*modes)
+        from scwatter_gb300 import synthetic
+        cfg = CFG2
+        fs = synthetic.make_factored(cfg["M0"], cfg["M1"], 1, (cfg["size"][0], cfg["size"][1],
+                                                              cfg["size"][2] / cfg["Z"]), seed=1,
+                                     dtype=np.complex64)
+        W32 = region_waves(fs, fs.Q_dn[0], fs.Q_up[0], 0)
+        zl = np.array([fs.z[0], fs.z[1]], np.float32)
+        dx, _, _, _ = grid_params(cfg)
+        P = 32
+        wset = ev.WaveSet.from_unpacked(ctx, 2, zl, [0, 0, len(W32)], [0, len(W32), len(W32)], W32)
+        out = torch.empty((P, P, 3), dtype=torch.complex64, device="cuda")
+        for _ in range(2):
+            wset.eval_plane_device(0, cfg["x0"], cfg["y0"], np.float32(0.5 * (zl[0] + zl[1])), dx, P, out.data_ptr())
+        ctx.synchronize()
+        print(json.dumps({"probe": kind, "points": P * P, "waves_per_point": len(W32),
+                          "points_modes_per_launch": P * P * len(W32)}))
     elif kind == "zgemm":
         n, B = 800, 4
         g = torch.Generator(device="cuda").manual_seed(0)
@@ -833,7 +853,7 @@ def main():
     ap.add_argument("--warm-train", type=int, default=16)
     ap.add_argument("--warm-coef", type=int, default=24)
     ap.add_argument("--warm-epochs", type=int, default=200)
-    ap.add_argument("--probe", choices=["eig-mixed", "zgemm"], default=None,
+    ap.add_argument("--probe", choices=["eig-mixed", "zgemm", "plain"], default=None,
                     help="run one small case for an ncu capture and exit")
     args = ap.parse_args()
     if args.probe:

@@ -12,6 +12,7 @@
 // SMs where the algorithm allows it (GEMM, the trailing updates of LU); the inherently
 // sequential ones (Hessenberg reduction, QR sweeps) run one CTA per matrix and are batched over
 // the slices of a sample.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -388,6 +389,157 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
             column_axpy(Q + j, n, 0, n, y, CT<C>::mk(-v[j].x, v[j].y));
         __syncthreads();
     }
+}
+
+// ------------------------------------------------------------------------------------
+// The same reduction spread over the whole GPU: per column k three short launches for the
+// batch -- the Householder vector (one CTA per matrix), the products y = tau A[:, k+1:] v and
+// z = tau Q[:, k+1:] v (a warp per row, rows of every matrix over all SMs), and the updates of
+// the columns k+1.. of A (right then left, one thread per column) and of Q.  Every element sees
+// the operations of hessenberg_kernel in the same order; the kernel boundaries replace its
+// block barriers, so the O(n^2) work of a column runs on every SM instead of one per matrix.
+// Per matrix the 3n work entries hold v (slot 0: tau), y and z; the FP32 drop threshold
+// ulp^2 ||A||_F^2 (||A||_F is invariant under the reduction) is kept in Q[n-1][0], which the
+// reflectors never touch, and cleared at the end.
+// ------------------------------------------------------------------------------------
+constexpr int kHwRows = 8;        // rows (warps) per CTA of the product kernel
+constexpr int kHwCols = 128;      // columns (threads) per CTA of the update kernel
+
+template <typename C>
+__global__ void __launch_bounds__(256) hw_init_kernel(C* __restrict__ Q, int n, long long sA, const int* __restrict__ skip) {
+    if (skipped(skip, blockIdx.y)) return;
+    Q += sA * blockIdx.y;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)n * n;
+         i += (long long)gridDim.x * blockDim.x)
+        Q[i] = CT<C>::mk((i / n) == (i % n) ? 1 : 0, 0);
+}
+
+// ||A||_F^2 into Q[n-1][0].x (after hw_init_kernel)
+template <typename C>
+__global__ void __launch_bounds__(256) hw_fro_kernel(const C* __restrict__ A, C* __restrict__ Q, int n, long long sA,
+                                                     const int* __restrict__ skip) {
+    using R = typename CT<C>::R;
+    if (skipped(skip, blockIdx.y)) return;
+    A += sA * blockIdx.y;
+    __shared__ R sh[32];
+    R a2 = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (long long)n * n;
+         i += (long long)gridDim.x * blockDim.x)
+        a2 += cabs2(A[i]);
+    a2 = block_sum(a2, sh);
+    if (threadIdx.x == 0) atomicAdd(&Q[sA * blockIdx.y + (long long)(n - 1) * n].x, a2);
+}
+
+template <typename C>
+__global__ void __launch_bounds__(256) hw_vec_kernel(C* __restrict__ A, const C* __restrict__ Q, int n, long long sA,
+                                                     C* __restrict__ work, int k, const int* __restrict__ skip) {
+    using R = typename CT<C>::R;
+    if (skipped(skip, blockIdx.x)) return;
+    A += sA * blockIdx.x;
+    C* v = work + (long long)blockIdx.x * 3 * n;
+    __shared__ R sh[32];
+    __shared__ C s_beta;
+    __shared__ int s_skip;
+    constexpr bool kDropNegligible = sizeof(R) == sizeof(float);
+    R xn2 = 0;
+    for (int i = k + 2 + threadIdx.x; i < n; i += blockDim.x) xn2 += cabs2(A[(long long)i * n + k]);
+    xn2 = block_sum(xn2, sh);
+    const C alpha = A[(long long)(k + 1) * n + k];
+    if (threadIdx.x == 0) {
+        s_skip = 0;
+        const R neg2 = kDropNegligible ? Q[sA * blockIdx.x + (long long)(n - 1) * n].x * CT<C>::ulp * CT<C>::ulp : R(0);
+        if (kDropNegligible && xn2 + cabs2(alpha) <= neg2) {
+            s_skip = 2;                       // drop: zero the column below the diagonal
+        } else if (xn2 == 0 && alpha.y == 0) {
+            s_skip = 1;                       // already reduced
+        } else {
+            const R beta = -r_copysign(r_sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+            v[0] = CT<C>::mk((beta - alpha.x) / beta, -alpha.y / beta);      // tau
+            s_beta = CT<C>::mk(beta, 0);
+        }
+        if (s_skip) v[0] = CT<C>::mk(0, 0);
+    }
+    __syncthreads();
+    if (s_skip == 1) return;
+    if (s_skip == 2) {
+        for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[(long long)i * n + k] = CT<C>::mk(0, 0);
+        return;
+    }
+    const C scal = cdiv(CT<C>::mk(1, 0), csub(alpha, s_beta));
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
+        v[i] = (i == k + 1) ? CT<C>::mk(1, 0) : cmul(A[(long long)i * n + k], scal);
+        A[(long long)i * n + k] = (i == k + 1) ? s_beta : CT<C>::mk(0, 0);
+    }
+}
+
+// rows 0..n-1: y[i] = tau sum_{j > k} A[i][j] v[j]; rows n..2n-1: z[i] = tau sum_{j > k} Q[i][j] v[j]
+template <typename C>
+__global__ void __launch_bounds__(kHwRows * 32) hw_prod_kernel(const C* __restrict__ A, const C* __restrict__ Q, int n,
+                                                               long long sA, C* __restrict__ work, int k,
+                                                               const int* __restrict__ skip) {
+    if (skipped(skip, blockIdx.y)) return;
+    C* v = work + (long long)blockIdx.y * 3 * n;
+    const C tau = v[0];
+    if (tau.x == 0 && tau.y == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * kHwRows + (threadIdx.x >> 5);
+    if (r >= 2 * n) return;
+    const C* row = (r < n ? A + (long long)r * n : Q + (long long)(r - n) * n) + sA * blockIdx.y;
+    C acc = CT<C>::mk(0, 0);
+#pragma unroll 4
+    for (int j = k + 1 + lane; j < n; j += 32) acc = cfma(row[j], v[j], acc);
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) v[n + r] = cmul(tau, acc);          // y = v + n, z = v + 2n
+}
+
+// columns j > k of A: right update (all rows) while summing v^H of the updated column, then the
+// left update; columns j > k of Q (blocks past the A blocks): Q[:, j] -= z conj(v_j)
+template <typename C>
+__global__ void __launch_bounds__(kHwCols) hw_update_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA,
+                                                            const C* __restrict__ work, int k, int nblk_a,
+                                                            const int* __restrict__ skip) {
+    if (skipped(skip, blockIdx.y)) return;
+    const C* v = work + (long long)blockIdx.y * 3 * n;
+    const C tau = v[0];
+    if (tau.x == 0 && tau.y == 0) return;
+    constexpr int kStripe = sizeof(typename CT<C>::R) == sizeof(float) ? 8 : 4;
+    const bool isA = (int)blockIdx.x < nblk_a;
+    const int j = k + 1 + (isA ? (int)blockIdx.x : (int)blockIdx.x - nblk_a) * kHwCols + threadIdx.x;
+    if (j >= n) return;
+    if (isA) {
+        const C* y = v + n;
+        const C vc = CT<C>::mk(v[j].x, -v[j].y);
+        C* col = A + sA * blockIdx.y + j;
+        C s = CT<C>::mk(0, 0);
+        for (int i0 = 0; i0 < n; i0 += kStripe) {
+            C a[kStripe];
+#pragma unroll
+            for (int q = 0; q < kStripe; q++)
+                if (i0 + q < n) a[q] = col[(long long)(i0 + q) * n];
+#pragma unroll
+            for (int q = 0; q < kStripe; q++) {
+                const int i = i0 + q;
+                if (i < n) {
+                    a[q] = csub(a[q], cmul(y[i], vc));
+                    col[(long long)i * n] = a[q];
+                    if (i > k) s = cfma(CT<C>::mk(v[i].x, -v[i].y), a[q], s);
+                }
+            }
+        }
+        const C wj = cmul(CT<C>::mk(tau.x, -tau.y), s);
+        column_axpy(col, n, k + 1, n, v, CT<C>::mk(-wj.x, -wj.y));
+    } else {
+        column_axpy(Q + sA * blockIdx.y + j, n, 0, n, v + 2 * n, CT<C>::mk(-v[j].x, v[j].y));
+    }
+}
+
+template <typename C>
+__global__ void hw_finish_kernel(C* __restrict__ Q, int n, long long sA, int batch, const int* __restrict__ skip) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < batch && !skipped(skip, b)) Q[sA * b + (long long)(n - 1) * n] = CT<C>::mk(0, 0);
 }
 
 // ------------------------------------------------------------------------------------
@@ -779,8 +931,29 @@ scw_status zgehrd(cudaStream_t st, double2* A, double2* Q, int n, int batch, dou
     return SCW_OK;
 }
 
+// Hessenberg reduction with Schur-vector accumulation, spread over the GPU (3 launches per column)
 template <typename C>
-scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, int* status, const int* skip) {
+static scw_status gehrd_wide(cudaStream_t st, C* A, C* Q, int n, int batch, C* hw, const int* skip) {
+    const long long nn = (long long)n * n;
+    const unsigned gi = (unsigned)std::min<long long>((nn + 255) / 256, 1024);
+    z::hw_init_kernel<C><<<dim3(gi, batch), 256, 0, st>>>(Q, n, nn, skip);
+    z::hw_fro_kernel<C><<<dim3(gi, batch), 256, 0, st>>>(A, Q, n, nn, skip);
+    SCW_CUDA_TRY(cudaGetLastError());
+    for (int k = 0; k + 2 < n; k++) {
+        z::hw_vec_kernel<C><<<batch, 256, 0, st>>>(A, Q, n, nn, hw, k, skip);
+        z::hw_prod_kernel<C><<<dim3((2 * n + z::kHwRows - 1) / z::kHwRows, batch), z::kHwRows * 32, 0, st>>>(
+            A, Q, n, nn, hw, k, skip);
+        const int nblk = (n - k - 1 + z::kHwCols - 1) / z::kHwCols;
+        z::hw_update_kernel<C><<<dim3(2 * nblk, batch), z::kHwCols, 0, st>>>(A, Q, n, nn, hw, k, nblk, skip);
+    }
+    z::hw_finish_kernel<C><<<(batch + 255) / 256, 256, 0, st>>>(Q, n, nn, batch, skip);
+    SCW_CUDA_TRY(cudaGetLastError());
+    return SCW_OK;
+}
+
+template <typename C>
+scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, int* status, const int* skip,
+                bool wide) {
     // A (overwritten): n x n per batch entry; W: n eigenvalues; V: n x n right eigenvectors (columns)
     // work: >= batch * (n*n + 3 n) elements
     if (n <= 0 || batch <= 0) return SCW_OK;
@@ -788,8 +961,13 @@ scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, in
     C* Q = work;                             // batch * n * n: Schur vectors
     C* hw = work + nn * batch;               // batch * 3n
     SCW_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * batch, st));
-    z::hessenberg_kernel<C><<<batch, 1024, 0, st>>>(A, Q, n, nn, hw, skip);
-    SCW_CUDA_TRY(cudaGetLastError());
+    if (wide && n >= kWideMinN) {
+        scw_status s = gehrd_wide<C>(st, A, Q, n, batch, hw, skip);
+        if (s != SCW_OK) return s;
+    } else {
+        z::hessenberg_kernel<C><<<batch, 1024, 0, st>>>(A, Q, n, nn, hw, skip);
+        SCW_CUDA_TRY(cudaGetLastError());
+    }
     SCW_CUDA_TRY(cudaFuncSetAttribute(z::hqr_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)z::hqr_smem_bytes<C>()));
     z::hqr_kernel<C><<<batch, 1024, z::hqr_smem_bytes<C>(), st>>>(A, Q, n, nn, W, status, skip);
@@ -812,7 +990,7 @@ scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, in
     template scw_status getrf<C>(cudaStream_t, C*, int, long long, int*, long long, int*, int);                    \
     template scw_status getrs<C>(cudaStream_t, const C*, int, long long, const int*, long long, C*, int, long long, \
                                  int);                                                                             \
-    template scw_status geev<C>(cudaStream_t, C*, C*, C*, int, int, C*, int*, const int*);
+    template scw_status geev<C>(cudaStream_t, C*, C*, C*, int, int, C*, int*, const int*, bool);
 SCW_DENSE_INSTANTIATE(double2)
 SCW_DENSE_INSTANTIATE(float2)
 #undef SCW_DENSE_INSTANTIATE
@@ -880,7 +1058,7 @@ scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, i
         cudaFree(work);
         return fail(SCW_ERR_NOMEM, "scw_zgeev: workspace");
     }
-    scw_status st = scw::zgeev(ctx->stream, (double2*)A, (double2*)W, (double2*)V, n, batch, work, dst);
+    scw_status st = scw::zgeev(ctx->stream, (double2*)A, (double2*)W, (double2*)V, n, batch, work, dst, true);
     ctx->launches += 4;
     std::vector<int> status(batch, 0);
     if (st == SCW_OK) {
@@ -910,7 +1088,8 @@ scw_status scw_cgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, i
         cudaFree(work);
         return fail(SCW_ERR_NOMEM, "scw_cgeev: workspace");
     }
-    scw_status st = scw::geev<float2>(ctx->stream, (float2*)A, (float2*)W, (float2*)V, n, batch, work, dst);
+    scw_status st = scw::geev<float2>(ctx->stream, (float2*)A, (float2*)W, (float2*)V, n, batch, work, dst, nullptr,
+                                      true);
     ctx->launches += 5;
     std::vector<int> status(batch, 0);
     if (st == SCW_OK) {

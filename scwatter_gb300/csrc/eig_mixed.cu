@@ -630,7 +630,7 @@ scw_status geev_mixed(cudaStream_t st, double2* A, double2* lam, double2* V, int
     to_f32_kernel<<<nblk(nn * Z), 256, 0, st>>>(A, w.S0, nn * Z);
     MX_LAUNCHED(2);
     // FP32 Householder + QR + triangular eigenvectors: eigenvectors into S2, eigenvalues lam32
-    MX_TRY(geev<float2>(st, w.S0, w.lam32, w.S2, n, Z, w.S1, w.qr, nullptr));
+    MX_TRY(geev<float2>(st, w.S0, w.lam32, w.S2, n, Z, w.S1, w.qr, nullptr, prm.wide));
     if (launches) *launches += 5;
     init_kernel<<<dim3(gZ, Z), 256, 0, st>>>(w.lam32, w.S2, lam, V, n, w.qr, w.state, w.steps, w.res);
     cluster_kernel<<<Z, 1024, cl_smem, st>>>(lam, n, w.anorm, prm.tau_rel, w.label, w.member, w.cstart, w.ncl, w.state);
@@ -664,7 +664,7 @@ scw_status geev_mixed(cudaStream_t st, double2* A, double2* lam, double2* V, int
     // slices without convergence: the FP64 Householder + QR solver (qr[] reused as the skip mask)
     final_kernel<<<nblk(Z), 256, 0, st>>>(w.state, w.qr, Z);
     MX_LAUNCHED(1);
-    MX_TRY(geev<double2>(st, A, lam, V, n, Z, fb_work, status, w.qr));
+    MX_TRY(geev<double2>(st, A, lam, V, n, Z, fb_work, status, w.qr, prm.wide));
     if (launches) *launches += 5;
     return SCW_OK;
 }
@@ -706,8 +706,10 @@ extern "C" scw_status scw_zgeev_mixed(scw_ctx ctx, int n, void* A, void* W, void
     w.S2 = Wf;
     w.S3 = Wf + nn * batch;
     long long L = 0;
+    mx::EigMixParams prm;
+    prm.wide = true;
     scw_status st = mx::geev_mixed(ctx->stream, (double2*)A, (double2*)W, (double2*)V, n, batch, w,
-                                   reinterpret_cast<double2*>(blk), dst, mx::EigMixParams{}, &L);
+                                   reinterpret_cast<double2*>(blk), dst, prm, &L);
     ctx->launches += L;
     std::vector<int> status(batch, 0), state(batch, 0), steps(batch, 0);
     std::vector<double> res(batch, 0.0);

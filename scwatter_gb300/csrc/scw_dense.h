@@ -41,9 +41,14 @@ template <typename C>
 scw_status getrs(cudaStream_t st, const C* LU, int n, long long sA, const int* piv, long long sP, C* B, int nrhs,
                  long long sB, int batch);
 // eigenvalues W and right eigenvectors V (columns) of A (overwritten); work >= batch (n^2 + 3 n);
-// status[b] = 1 when the QR iteration did not converge
+// status[b] = 1 when the QR iteration did not converge.  wide: the Hessenberg reduction of
+// matrices with n >= kWideMinN is spread over the whole GPU (3 launches per column) instead of one
+// CTA per matrix -- for batches too small to fill the SMs; a batch graph with many concurrent
+// items keeps the one-CTA form (fewer nodes).
+constexpr int kWideMinN = 128;
 template <typename C>
-scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, int* status, const int* skip = nullptr);
+scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, int* status, const int* skip = nullptr,
+                bool wide = false);
 
 inline scw_status zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2* A, int lda, long long sA,
                         const double2* B, int ldb, long long sB, double2 beta, double2* C, int ldc, long long sC,
@@ -59,8 +64,8 @@ inline scw_status zgetrs(cudaStream_t st, const double2* LU, int n, long long sA
     return getrs<double2>(st, LU, n, sA, piv, sP, B, nrhs, sB, batch);
 }
 inline scw_status zgeev(cudaStream_t st, double2* A, double2* W, double2* V, int n, int batch, double2* work,
-                        int* status) {
-    return geev<double2>(st, A, W, V, n, batch, work, status);
+                        int* status, bool wide = false) {
+    return geev<double2>(st, A, W, V, n, batch, work, status, nullptr, wide);
 }
 // Hessenberg form of A (in place, n x n per batch entry) and the unitary Q (A = Q H Q^H);
 // work >= batch * 3 n

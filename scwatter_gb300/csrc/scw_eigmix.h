@@ -49,6 +49,7 @@ struct EigMixParams {
     double deg_rel = 1e-12;         // within a cluster: eigenvalues this close count as equal
     double tol = 1e-14;             // a slice stops refining once its max relative column residual is this small
     double tol_accept = 1e-12;      // after the last step: accepted at or below this, else the FP64 solver
+    bool wide = false;              // Hessenberg reductions spread over the GPU (see geev)
 };
 
 // Eigenpairs of Z matrices A (n x n, row-major, preserved unless a matrix falls back) into

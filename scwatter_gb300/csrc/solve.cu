@@ -648,14 +648,16 @@ scw_status record_solve(const SolvePlan& p, const SolveIn& in, const SolveWs& ws
     SCW_CUDA_TRY(cudaGetLastError());
     SCW_TRY(zgemm(st, n, n, n, kOne, ws.P, n, nn, ws.Q, n, nn, kZero, ws.PQ, n, nn, Zs));
     if (p.eig_mixed) {
-        SCW_TRY(mx::geev_mixed(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.mix, ws.P, out.status, mx::EigMixParams{}, &L));
+        mx::EigMixParams prm;
+        prm.wide = p.wide_hess;
+        SCW_TRY(mx::geev_mixed(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.mix, ws.P, out.status, prm, &L));
         if (out.eig) {
             SCW_CUDA_TRY(cudaMemcpyAsync(out.eig, ws.mix.state, sizeof(int) * Zs, cudaMemcpyDeviceToDevice, st));
             SCW_CUDA_TRY(cudaMemcpyAsync(out.eig + Zs, ws.mix.steps, sizeof(int) * Zs, cudaMemcpyDeviceToDevice, st));
             SCW_CUDA_TRY(cudaMemcpyAsync(out.eig_res, ws.mix.res, sizeof(double) * Zs, cudaMemcpyDeviceToDevice, st));
         }
     } else {
-        SCW_TRY(zgeev(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.P, out.status));
+        SCW_TRY(zgeev(st, ws.PQ, ws.lam, ws.U, n, Zs, ws.P, out.status, p.wide_hess));
         L += 5;
     }
     roots_kernel<<<nblk((long long)n * Zs), 256, 0, st>>>(ws.lam, n, Zs, in.dz, k, out.gam, ws.E);
@@ -817,6 +819,7 @@ scw_status scw_solve(scw_ctx ctx, const double* sample, int Zs, int Y, int X, co
     SolvePlan p;
     scw_status st = plan_solve(prm, Zs, Y, X, p);
     if (st != SCW_OK) return st;
+    p.wide_hess = true;          // one sample: spread the Hessenberg reductions over the GPU
     SCW_ON_DEVICE(ctx->device);
     std::unique_ptr<scw_solution_s> sol(new (std::nothrow) scw_solution_s());
     if (!sol) return fail(SCW_ERR_NOMEM, "host allocation");

@@ -28,6 +28,7 @@ struct SolvePlan {
     double k = 0, n0 = 1, n1 = 1;
     bool external = false, pz = true;
     bool eig_mixed = true;                  // FP32 QR + FP64 refinement (else FP64 QR throughout)
+    bool wide_hess = false;                 // Hessenberg reductions over the whole GPU (single solves)
     std::vector<double> zb, dz;             // Z + 1 boundaries, Z thicknesses
     std::vector<int> ps, qs;                // integer harmonic series
     std::vector<double> up, wq;             // k grids (reference PI)

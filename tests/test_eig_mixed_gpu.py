@@ -102,3 +102,41 @@ def test_solve_matches_fp64_eigen_solver(ctx):
     assert g.eig["mixed"] and g.eig["accepted"] == 8 and g.eig["max_residual"] <= 1e-12
     assert not f.eig["mixed"]
     assert np.linalg.norm(g.x - f.x) < 1e-11 * np.linalg.norm(f.x)
+
+
+def test_wide_hessenberg_path(ctx):
+    """Matrices of order >= 128 take the Hessenberg reduction spread over the GPU (3 launches per
+    column): random and layer-like (nearly diagonal, clustered) matrices in one batch, refined to
+    FP64 residuals, eigenvalues equal to LAPACK's."""
+    rng = np.random.default_rng(11)
+    n = 200
+    A = rng.standard_normal((3, n, n)) + 1j * rng.standard_normal((3, n, n))
+    d = np.repeat(np.linspace(0.5, 1.5, n // 8), 8)             # multiplicity-8 diagonal with couplings
+    A[2] = np.diag(d + 0.01j) + 1e-3 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    W, V, acc, steps, res = _mixed(ctx, A)
+    _check(A, W, V)
+    assert (acc == 1).all()
+
+
+def test_wide_fp32_stage_matches_lapack(ctx):
+    """scw_cgeev at n = 256 (wide Hessenberg + FP32 QR): FP32 eigenvalues against LAPACK's."""
+    import torch
+    from scwatter_gb300 import _lib
+    rng = np.random.default_rng(5)
+    n, B = 256, 2
+    A = (rng.standard_normal((B, n, n)) + 1j * rng.standard_normal((B, n, n))).astype(np.complex64)
+    dA = torch.from_numpy(A.copy()).cuda()
+    dW = torch.zeros((B, n), dtype=torch.complex64, device="cuda")
+    dV = torch.zeros((B, n, n), dtype=torch.complex64, device="cuda")
+    st = np.zeros(B, np.int32)
+    torch.cuda.synchronize()
+    _lib.call("scw_cgeev", ctx.handle, n, _p(dA), _p(dW), _p(dV), B, ctypes.c_void_p(st.ctypes.data))
+    W, V = dW.cpu().numpy(), dV.cpu().numpy()
+    assert (st == 0).all()
+    for b in range(B):
+        A64 = A[b].astype(np.complex128)
+        ref = np.linalg.eigvals(A64)
+        nA = np.linalg.norm(A64, 1)
+        assert np.abs(W[b][:, None] - ref[None, :]).min(axis=1).max() < 1e-4 * nA
+        r = np.linalg.norm(A64 @ V[b] - V[b] * W[b][None, :], axis=0) / (nA * np.linalg.norm(V[b], axis=0))
+        assert r.max() < 1e-5

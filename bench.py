@@ -347,6 +347,49 @@ def run_ours(args):
                        "rel_l2_vs_tf32x3": rel_l2(out[nz_local // 2].cpu().numpy(),
                                                   sep_field_all[nz_local // 2].cpu().numpy())}
 
+    # e2e through the host-buffer API before the host-side legs (the CPU baseline's threads would
+    # compete with the host thread that queues the uploads)
+    e2e_line = None
+    # (scw_sep_eval_slab_host: the amplitude blocks uploaded from pinned host memory slice by slice
+    # while earlier slices are evaluated, planes read back as they finish)
+    if not args.no_e2e:
+        host_out = torch.empty((max(nz_local, 1), Ny, Nx, 3), dtype=torch.complex64, pin_memory=True)
+        e2e_t = []
+        # Q bytes this rank uploads per step: the slices its planes lie in
+        regions = shard.region_of_z(shard.plane_z(z0, dz, Nz)[k0:k1], fs.z)
+        h2d_local = int(len({int(r) for r in regions if 1 <= r <= Z}) * q_bytes // Z)
+        for i in range(max(2, min(args.steps, 3)) + 1):
+            ctx.synchronize()
+            if ws > 1:
+                torch.distributed.barrier()
+            t0 = time.perf_counter()
+            if nz_local > 0:
+                sep.eval_slab_host(hQ, cfg["x0"], cfg["y0"], z0, dx, dy, dz, Nx, Ny, k0, k1, out=host_out,
+                                   method=sp.TF32X3)
+            if i > 0:
+                e2e_t.append(time.perf_counter() - t0)
+        t_e2e = float(np.mean(e2e_t))
+        h2d_total, d2h_total = h2d_local, nz_local * Ny * Nx * 24
+        if ws > 1:
+            tt = torch.tensor([t_e2e], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(tt.item())
+            bb = torch.tensor([h2d_total, d2h_total], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(bb)
+            h2d_total, d2h_total = int(bb[0].item()), int(bb[1].item())
+        link = link_peaks(torch)
+        if rank == 0:
+            t_bound = max(h2d_local / (link["h2d_gbs"] * 1e9), nz_local * Ny * Nx * 24 / (link["d2h_gbs"] * 1e9))
+            e2e_line = {"value": units / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d_total,
+                        "d2h_bytes_per_step": d2h_total, "ms_per_step": t_e2e * 1e3,
+                        "api": "scw_sep_eval_slab_host (the whole volume at N = 1; pinned host amplitude blocks "
+                               "in, pinned host planes out)",
+                        "roofline": {"bound": "host link",
+                                     "achieved": (h2d_local + nz_local * Ny * Nx * 24) / t_e2e / 1e9,
+                                     "unit": "GB/s", "link_peaks_GBs": link,
+                                     "t_link_bound_ms": t_bound * 1e3, "frac": t_bound / t_e2e,
+                                     "note": "frac = time the measured link needs for the step's H2D and D2H "
+                                             "bytes (the two directions overlap) / e2e time"}}
     # dominant kernel: the stage-1 coefficient contraction streams every Q block once
     contract_ms = kt.get("sep_contract_kernel", (0.0, 0))[0]
     synth_ms = sum(v[0] for k, v in kt.items() if "synth" in k)
@@ -431,48 +474,10 @@ def run_ours(args):
                                  "sample": f"{rows} rows x {cw_} points of the same patch ({len(W32)} waves/point), "
                                            f"FP32 reference CPU evaluator"},
                 "gpu_launches": int(launches), "clocks": clocks}
+        if e2e_line is not None:
+            line["e2e"] = e2e_line
     del sep_field_all
 
-    # e2e through the host-buffer API (scw_sep_eval_volume_host): Q uploaded from pinned host
-    # memory slice by slice while earlier slices are evaluated, planes read back as they finish
-    if not args.no_e2e:
-        del out
-        torch.cuda.empty_cache()
-        host_out = torch.empty((max(nz_local, 1), Ny, Nx, 3), dtype=torch.complex64, pin_memory=True)
-        e2e_t = []
-        # Q bytes this rank uploads per step: the slices its planes lie in
-        regions = shard.region_of_z(shard.plane_z(z0, dz, Nz)[k0:k1], fs.z)
-        h2d_local = int(len({int(r) for r in regions if 1 <= r <= Z}) * q_bytes // Z)
-        for i in range(max(2, min(args.steps, 3)) + 1):
-            ctx.synchronize()
-            if ws > 1:
-                torch.distributed.barrier()
-            t0 = time.perf_counter()
-            if nz_local > 0:
-                sep.eval_slab_host(hQ, cfg["x0"], cfg["y0"], z0, dx, dy, dz, Nx, Ny, k0, k1, out=host_out,
-                                   method=sp.TF32X3)
-            if i > 0:
-                e2e_t.append(time.perf_counter() - t0)
-        t_e2e = float(np.mean(e2e_t))
-        h2d_total, d2h_total = h2d_local, nz_local * Ny * Nx * 24
-        if ws > 1:
-            tt = torch.tensor([t_e2e], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            t_e2e = float(tt.item())
-            bb = torch.tensor([h2d_total, d2h_total], dtype=torch.float64, device="cuda")
-            torch.distributed.all_reduce(bb)
-            h2d_total, d2h_total = int(bb[0].item()), int(bb[1].item())
-        link = link_peaks(torch)
-        if line is not None:
-            t_bound = max(h2d_local / (link["h2d_gbs"] * 1e9), nz_local * Ny * Nx * 24 / (link["d2h_gbs"] * 1e9))
-            line["e2e"] = {"value": units / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d_total,
-                           "d2h_bytes_per_step": d2h_total, "ms_per_step": t_e2e * 1e3,
-                           "api": "scw_sep_eval_slab_host (the whole volume at N = 1; pinned host Q in, pinned host planes out)",
-                           "roofline": {"bound": "host link", "achieved": (h2d_local + nz_local * Ny * Nx * 24) / t_e2e / 1e9,
-                                        "unit": "GB/s", "link_peaks_GBs": link,
-                                        "t_link_bound_ms": t_bound * 1e3, "frac": t_bound / t_e2e,
-                                        "note": "frac = time the measured link needs for the step's H2D and D2H "
-                                                "bytes (the two directions overlap) / e2e time"}}
     if line is not None and not args.no_solve:
         line["solve"] = solve_leg(ctx)
     if line is not None:

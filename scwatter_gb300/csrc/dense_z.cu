@@ -304,17 +304,18 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
     __shared__ R sh[32];
     __shared__ C s_tau, s_beta;
     // FP32 (first stage of the mixed solver): a column whose part below the diagonal is under
-    // ulp ||A||_F is set to zero instead of reflected.  That is a backward error of rounding size,
-    // and it keeps a (nearly) diagonal matrix, e.g. the reduced matrix of a homogeneous layer
-    // whose off-diagonal entries are DFT rounding, from being scrambled by reflectors built
-    // from noise.  FP64 keeps zgehd2's behaviour.
+    // ulp ||A||_F / sqrt(n) (ulp times the root-mean-square row norm) is set to zero instead of
+    // reflected.  That is a backward error of rounding size, and it keeps a (nearly) diagonal
+    // matrix, e.g. the reduced matrix of a homogeneous layer whose off-diagonal entries are DFT
+    // rounding, from being scrambled by reflectors built from noise.  (ulp ||A||_F itself grows as
+    // sqrt(n) and at n = 3200 dropped real couplings.)  FP64 keeps zgehd2's behaviour.
     constexpr bool kDropNegligible = sizeof(R) == sizeof(float);
     constexpr int kStripe = sizeof(R) == sizeof(float) ? 8 : 4;
     R neg2 = 0;
     if (kDropNegligible) {
         R a2 = 0;
         for (long long i = threadIdx.x; i < (long long)n * n; i += blockDim.x) a2 += cabs2(A[i]);
-        neg2 = block_sum(a2, sh) * CT<C>::ulp * CT<C>::ulp;
+        neg2 = block_sum(a2, sh) * CT<C>::ulp * CT<C>::ulp / (R)n;
     }
     for (int i = threadIdx.x; i < n * n; i += blockDim.x) Q[i] = CT<C>::mk((i / n) == (i % n) ? 1 : 0, 0);
     __syncthreads();
@@ -398,9 +399,9 @@ hessenberg_kernel(C* __restrict__ A, C* __restrict__ Q, int n, long long sA, C* 
 // the columns k+1.. of A (right then left, one thread per column) and of Q.  Every element sees
 // the operations of hessenberg_kernel in the same order; the kernel boundaries replace its
 // block barriers, so the O(n^2) work of a column runs on every SM instead of one per matrix.
-// Per matrix the 3n work entries hold v (slot 0: tau), y and z; the FP32 drop threshold
-// ulp^2 ||A||_F^2 (||A||_F is invariant under the reduction) is kept in Q[n-1][0], which the
-// reflectors never touch, and cleared at the end.
+// Per matrix the 3n work entries hold v (slot 0: tau), y and z; ||A||_F^2 for the FP32 drop
+// threshold ulp^2 ||A||_F^2 / n (||A||_F is invariant under the reduction) is kept in Q[n-1][0],
+// which the reflectors never touch, and cleared at the end.
 // ------------------------------------------------------------------------------------
 constexpr int kHwRows = 8;        // rows (warps) per CTA of the product kernel
 constexpr int kHwCols = 128;      // columns (threads) per CTA of the update kernel
@@ -447,7 +448,8 @@ __global__ void __launch_bounds__(256) hw_vec_kernel(C* __restrict__ A, const C*
     const C alpha = A[(long long)(k + 1) * n + k];
     if (threadIdx.x == 0) {
         s_skip = 0;
-        const R neg2 = kDropNegligible ? Q[sA * blockIdx.x + (long long)(n - 1) * n].x * CT<C>::ulp * CT<C>::ulp : R(0);
+        const R neg2 =
+            kDropNegligible ? Q[sA * blockIdx.x + (long long)(n - 1) * n].x * CT<C>::ulp * CT<C>::ulp / (R)n : R(0);
         if (kDropNegligible && xn2 + cabs2(alpha) <= neg2) {
             s_skip = 2;                       // drop: zero the column below the diagonal
         } else if (xn2 == 0 && alpha.y == 0) {
@@ -790,10 +792,13 @@ hqr_kernel(C* __restrict__ H, C* __restrict__ Z, int n, long long sA, C* __restr
 // X[:, k] solves (T - T_kk I) x = 0 with x_k = 1, x_i = 0 for i > k.  One warp per vector.
 // X is written row-major (column k = eigenvector k).
 // FP64: a denominator T_ii - T_kk below smin is replaced by smin, as ztrevc does.  FP32 (the
-// first stage of the mixed solver): diagonal entries within 16 ulp of max |T_jj| of each other
-// count as one degenerate eigenvalue and x_i = 0, so each keeps its own Schur vector.  (Dividing
-// rounding noise by rounding noise gives numerically parallel vectors for the exactly degenerate
-// eigenvalues of homogeneous layers; the refinement resolves such clusters in FP64.)
+// first stage of the mixed solver): where both the denominator and the coupling sum
+// sum_j T_ij x_j are within 16 ulp of max |T_jj|, the pair counts as one degenerate eigenvalue and
+// x_i = 0, so each keeps its own Schur vector.  (Dividing rounding noise by rounding noise gives
+// numerically parallel vectors for the exactly degenerate eigenvalues of homogeneous layers; the
+// refinement resolves such clusters in FP64.)  A close pair with a real coupling is divided as in
+// FP64: zeroing it would leave the coupling as residual, which the refinement of dense spectra
+// (n = 3200 layers) could not remove.
 // ------------------------------------------------------------------------------------
 template <typename C>
 __global__ void __launch_bounds__(256)
@@ -829,7 +834,7 @@ trevc_kernel(const C* __restrict__ T, C* __restrict__ X, int n, long long sA, co
         }
         if (lane == 0) {
             C d = csub(T[(long long)i * n + i], lam);
-            if (kDegenerateSkip && cabs1(d) <= deg) {
+            if (kDegenerateSkip && cabs1(d) <= deg && cabs1(s) <= deg) {
                 X[(long long)i * n + k] = CT<C>::mk(0, 0);
             } else {
                 if (cabs1(d) < smin) d = CT<C>::mk(smin, 0);

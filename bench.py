@@ -44,9 +44,10 @@ UNIT = "points*modes/s"
 
 CFG2 = dict(name="spheres[64,128,128] coef40x40 64 slices, grid 512x512x256", M0=40, M1=40, Z=64,
             size=(128.0, 128.0, 64.0), Nx=512, Ny=512, Nz=256, x0=-64.0, x1=64.0, y0=-64.0, y1=64.0)
-# DRAM bytes / algorithmic bytes of sep_contract_kernel from one ncu capture of the 8-slice case
-# (dram__bytes_read.sum + dram__bytes_write.sum = 1.968409 GB + 4.705 MB for 1.967309 GB of Q and C)
-CONTRACT_TRAFFIC_RATIO = (1.968409e9 + 4.704768e6) / 1.9673088e9
+# DRAM bytes / algorithmic bytes of sep_contract_kernel from one ncu capture of the 8-slice case of
+# the paired set (dram__bytes_read.sum + dram__bytes_write.sum = 985.03 MB + 4.47 MB for 984.27 MB of
+# V and C: 8 x 3 x 1600 x 3200 x 8 B + 32 x 3 x 1600 x 8 B)
+CONTRACT_TRAFFIC_RATIO = (985.032448e6 + 4.474368e6) / (8 * 3 * 1600 * 3200 * 8 + 32 * 3 * 1600 * 8)
 PLAIN_PATCH = 128          # plain-form sample: PLAIN_PATCH x PLAIN_PATCH points of one interior xy plane
 CPU_SLICE = 3              # the slice the plain and CPU samples lie in
 
@@ -453,7 +454,7 @@ def run_ours(args):
                              "achieved": contract_gbs, "peak": hbm_peak, "unit": "GB/s",
                              "frac": contract_gbs / hbm_peak if contract_gbs else None,
                              "traffic": (q_bytes + c_bytes) * CONTRACT_TRAFFIC_RATIO,
-                             "traffic_source": "ncu DRAM bytes of the 8-slice case (1.973 GB for 1.967 GB "
+                             "traffic_source": "ncu DRAM bytes of the 8-slice case (989.5 MB for 984.3 MB "
                                                "algorithmic), scaled by the units of a full launch",
                              "algorithmic_bytes": q_bytes + c_bytes, "peak_source": peak_src},
                 "kernels_ms": {k: v[0] for k, v in kt.items()},

@@ -545,9 +545,9 @@ static scw_status launch_rows(scw_ctx ctx, const float2* C, const float2* Rtab, 
 scw_status sep_synth(scw_ctx ctx, const float2* T, const float2* F, int nrows, int ncols, int Mk, float* out,
                      int method) {
     if (method == SCW_SEP_TF32X3 || method == SCW_SEP_BF16X3) {
-        // shapes whose operands do not fit the tensor-core kernel's shared memory (more than
-        // 40 harmonics along the synthesis axis for 3xTF32, 72 for split-BF16) run the FP32 SIMT
-        // GEMM below, which is at least as accurate
+        // shapes whose operands do not fit the tensor-core kernel's shared and tensor memory (more
+        // than 48 harmonics along the synthesis axis for 3xTF32, 80 for split-BF16) run the FP32
+        // SIMT GEMM below, which is at least as accurate
         scw_status st = sep_synth_tc(ctx, T, F, nrows, ncols, Mk, out, method);
         if (st != SCW_ERR_UNSUPPORTED) return st;
     }

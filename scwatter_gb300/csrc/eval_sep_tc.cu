@@ -248,6 +248,14 @@ __device__ __forceinline__ uint4 pack4<1>(const __nv_bfloat16* v) { // 8 bf16 va
 
 constexpr int kEpiWarps = 8, kProdWarps = 7;      // 16 warps with the MMA warp: 128 registers each
 constexpr int kEpiRows = kRows * 4 / kEpiWarps;     // output rows per epilogue warp and tile (8)
+constexpr int kTStages = 3;                          // staged T tiles in flight (cp.async ring)
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // OR of v over the producer warps (named barrier 1): keeps their loop decisions uniform so
 // every producer thread reaches the same named barriers
@@ -278,13 +286,15 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     const uint32_t b_bytes = (kN / 8) * sbo;
     const uint32_t acols = kbytes / 4;                        // TMEM columns of A (hi or lo): K * EB / 4
     unsigned char* sB0 = smem;                                // slot s, part h: sB0 + (2 s + h) b_bytes
-    float2* sT = reinterpret_cast<float2*>(sB0 + 4 * b_bytes);   // staged T tile [kRows * 3][tstr]
+    // ring of kTStages staged T tiles [kRows * 3][tstr], filled by cp.async kTStages - 1 tiles ahead
+    const int t_slot = (((kRows * 3 * (Mk + 4) * 8 + 127) / 128) * 128) / 8;     // float2 per slot
+    float2* sT = reinterpret_cast<float2*>(sB0 + 4 * b_bytes);
     const int t_tile = kRows * 3 * Mk;                           // float2 of T per tile
     // fast producer path: Mk a multiple of the elements per core row; T rows padded in shared
     // memory to an odd number of 16-byte chunks so a warp's 16-byte reads spread over the banks
     const bool fast = (Mk % EPC) == 0 && (Mk % 2) == 0;
     const int tstr = fast ? ((Mk / 2) % 2 == 0 ? Mk + 2 : Mk + 4) : Mk;
-    float* sOut = reinterpret_cast<float*>(sB0 + 4 * b_bytes + ((kRows * 3 * (Mk + 4) * 8 + 127) / 128) * 128);   // [4 warps][192]
+    float* sOut = reinterpret_cast<float*>(sT + kTStages * t_slot);   // [epilogue warps][192]
     uint64_t* bar = reinterpret_cast<uint64_t*>(sOut + kEpiWarps * 192);
     uint64_t* full_b = bar;          // [2] producers -> MMA
     uint64_t* empty_b = bar + 2;     // [2] MMA completion -> producers
@@ -352,17 +362,25 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     if (warp >= kEpiWarps && warp < kEpiWarps + kProdWarps) {
         // ---------------- producers ----------------
         const int pt = tid - kEpiWarps * 32;                  // 0 .. kProdWarps * 32 - 1
-        constexpr int kPer = (kRows * 3 * 64 / 2 + kProdWarps * 32 - 1) / (kProdWarps * 32);
         const int n4 = t_tile / 2;
-        float4 tbuf[kPer];
-        auto load_t = [&](int rr0, float4 (&buf)[kPer]) {
-            const float4* src = reinterpret_cast<const float4*>(T + (long long)rr0 * 3 * Mk);
-#pragma unroll
-            for (int u = 0; u < kPer; u++) {
-                const int e = pt + u * kProdWarps * 32;
-                if (e < n4) buf[u] = __ldg(src + e);
+        // fast path: tile ti's rows of T into ring slot ti % kTStages with 16-byte cp.async
+        // (row (r, c) at slot + (3 r + c) * tstr; the buffer has slack past the last row, whose
+        // values are masked below), one commit group per tile, empty groups past the last tile
+        auto issue_t = [&](int ti) {
+            if (ti < n_my) {
+                const int rr0 = ((int)blockIdx.y + ti * (int)gridDim.y) * kRows;
+                const float4* src = reinterpret_cast<const float4*>(T + (long long)rr0 * 3 * Mk);
+                float2* dst = sT + (ti % kTStages) * t_slot;
+                const int h = Mk / 2;                              // float4 per T row
+                for (int e = pt; e < n4; e += kProdWarps * 32) {
+                    const int row = e / h;
+                    cp_async16(reinterpret_cast<float4*>(dst + row * tstr) + (e - row * h), src + e);
+                }
             }
+            cp_async_commit();
         };
+        if (fast)
+            for (int ti = 0; ti < kTStages - 1; ti++) issue_t(ti);
         for (int i = 0; i < n_my; i++) {
             const int s = i & 1;
             int stop = *abort_flag;
@@ -374,25 +392,16 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
             unsigned char* bh = sB0 + (2 * s + 0) * b_bytes;
             unsigned char* bl = sB0 + (2 * s + 1) * b_bytes;
-            // stage the tile's rows of T: the coalesced 16-byte loads of tile i were issued while
-            // tile i-1 was being built (or just now for the first tile); the buffer has slack past
-            // the last row, whose values are masked below; row (r, c) lands at sT + (3 r + c) * tstr
-            if (i == 0) load_t(r0, tbuf);
+            // tile i's T: this thread's copies are in once all but the kTStages - 1 newest groups
+            // have completed; the barrier makes every producer's copies visible
+            float2* sTi = sT + (i % kTStages) * t_slot;
             if (fast) {
-                const int h = Mk / 2;                          // float4 per T row
-#pragma unroll
-                for (int u = 0; u < kPer; u++) {
-                    const int e = pt + u * kProdWarps * 32;
-                    if (e < n4) {
-                        const int row = e / h;
-                        reinterpret_cast<float4*>(sT + row * tstr)[e - row * h] = tbuf[u];
-                    }
-                }
+                issue_t(i + kTStages - 1);
+                cp_async_wait<kTStages - 1>();
             } else {
-                for (int e = pt; e < t_tile; e += kProdWarps * 32) sT[e] = T[(long long)r0 * 3 * Mk + e];
+                for (int e = pt; e < t_tile; e += kProdWarps * 32) sTi[e] = T[(long long)r0 * 3 * Mk + e];
             }
             asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");
-            if (i + 1 < n_my) load_t(r0 + (int)gridDim.y * kRows, tbuf);    // prefetch the next tile
             if (fast) {
                 // task = (8-row block nb, row pair nq, core column kc); lanes: nq fastest, then kc.
                 // One task reads 16 bytes x EPC/2 of T row (4 nb + nq) once and writes the Re (n even)
@@ -409,7 +418,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                     const int nb = q / KC, kc = q - nb * KC;
                     const int trow = 4 * nb + nq, k0 = kc * EPC;
                     const bool ok = tsk < ntask && ((r0 + trow / 3) < nrows) && k0 < 2 * Mk;
-                    const float4* tp = reinterpret_cast<const float4*>(sT + (ok ? trow * tstr + (k0 < Mk ? k0 : k0 - Mk) : 0));
+                    const float4* tp = reinterpret_cast<const float4*>(sTi + (ok ? trow * tstr + (k0 < Mk ? k0 : k0 - Mk) : 0));
 #pragma unroll
                     for (int e2 = 0; e2 < EPC / 2; e2++) tv[u][e2] = ok ? tp[e2] : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
@@ -458,7 +467,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                     const int n = (nb << 3) | nlo;
                     const int r = n / 6, c = (n - 6 * r) >> 1, sri = n & 1;
                     const bool live = (r0 + r) < nrows;
-                    const float2* trow = sT + (r * 3 + c) * tstr;
+                    const float2* trow = sTi + (r * 3 + c) * tstr;
                     E hi[EPC], lo[EPC];
 #pragma unroll
                     for (int e = 0; e < EPC; e++) {
@@ -482,8 +491,9 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             }
             fence_proxy_async();
             mbar_arrive(&full_b[s]);
-            asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");   // sT reusable
+            asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");   // sT slot reusable
         }
+        cp_async_wait<0>();        // no copy into shared memory outlives the loop (also after an abort)
     } else if (warp == kEpiWarps + kProdWarps) {
         // ---------------- MMA issuer ----------------
         const uint32_t ab_fmt = kKind == 0 ? 2u : 1u;
@@ -583,7 +593,7 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
     const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * (Mk + 4) * 8 + 127) / 128 * 128;   // padded rows
-    const size_t smem = (tc::kN / 8) * sbo * 4 + t_tile_bytes + tc::kEpiWarps * 192 * 4 + 128;
+    const size_t smem = (tc::kN / 8) * sbo * 4 + tc::kTStages * t_tile_bytes + tc::kEpiWarps * 192 * 4 + 128;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     if (tc::kAcol + 2 * (size_t)Kp * EB / 4 > tc::kTmemCols) return SCW_ERR_UNSUPPORTED;   // A (hi, lo) in TMEM
     if (!ctx->tc_err) {

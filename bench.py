@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import glob
 import json
 import os
 import subprocess
@@ -48,6 +49,10 @@ CFG2 = dict(name="spheres[64,128,128] coef40x40 64 slices, grid 512x512x256", M0
 # the paired set (dram__bytes_read.sum + dram__bytes_write.sum = 985.03 MB + 4.47 MB for 984.27 MB of
 # V and C: 8 x 3 x 1600 x 3200 x 8 B + 32 x 3 x 1600 x 8 B)
 CONTRACT_TRAFFIC_RATIO = (985.032448e6 + 4.474368e6) / (8 * 3 * 1600 * 3200 * 8 + 32 * 3 * 1600 * 8)
+# XU (MUFU) thread instructions per point*mode of plain_eval_kernel on an xy plane, from ncu
+# (smsp__inst_executed_pipe_xu.sum x 32 / points*modes = 656e6 x 32 / 1.0486e10 on a 32 x 32 patch
+# of the config-2 set)
+PLAIN_XU_PER_PM = 2.0
 PLAIN_PATCH = 128          # plain-form sample: PLAIN_PATCH x PLAIN_PATCH points of one interior xy plane
 CPU_SLICE = 3              # the slice the plain and CPU samples lie in
 
@@ -185,6 +190,67 @@ def run_reference(args):
                       "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def bare_copies(torch, hQ, host_out, out, nz):
+    """The e2e step's copies alone, on the step's own pinned buffers: every slice of ``hQ`` up
+    (one cudaMemcpyAsync each, into one device slice buffer) and ``nz`` planes of ``out`` down
+    into ``host_out`` (8 planes per copy); best of 2 each."""
+    d = torch.empty(hQ[0].shape, dtype=hQ.dtype, device="cuda")
+    s = torch.cuda.Stream()
+
+    def best(fn):
+        ts = []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with torch.cuda.stream(s):
+                fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    def up():
+        for l in range(hQ.shape[0]):
+            d.copy_(hQ[l], non_blocking=True)
+
+    def down():
+        for k in range(0, nz, 8):
+            host_out[k:k + 8].copy_(out[k:k + 8], non_blocking=True)
+    t_up, t_down = best(up), (best(down) if nz > 0 else 0.0)
+    del d
+    return {"h2d_ms": t_up * 1e3, "d2h_ms": t_down * 1e3,
+            "h2d_gbs": hQ.numel() * 8 / t_up / 1e9,
+            "d2h_gbs": (nz * out[0].numel() * 8 / t_down / 1e9) if t_down > 0 else None}
+
+
+def host_numa(torch):
+    """NUMA node of the GPU's PCI function and free memory per host node (from sysfs)."""
+    info = {}
+    try:
+        p = torch.cuda.get_device_properties(0)
+        bus = "%04x:%02x:%02x.0" % (getattr(p, "pci_domain_id", 0), getattr(p, "pci_bus_id", 0),
+                                    getattr(p, "pci_device_id", 0))
+        info["gpu_pci"] = bus
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            info["gpu_numa_node"] = int(f.read().strip())
+    except (OSError, ValueError, RuntimeError):
+        pass
+    free = {}
+    for node in sorted(glob.glob("/sys/devices/system/node/node[0-9]*")):
+        try:
+            with open(node + "/meminfo") as f:
+                for ln in f:
+                    if "MemFree" in ln:
+                        free[os.path.basename(node)] = int(ln.split()[-2]) >> 20   # GiB
+        except OSError:
+            pass
+    info["memfree_gib_per_node"] = free
+    try:
+        info["cpus_allowed"] = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        pass
+    return info
+
+
 def link_peaks(torch, nbytes=2 << 30):
     """Pinned host <-> device copy bandwidth of this machine (best of 3 single cudaMemcpyAsync of
     nbytes each way, and both directions at once on two streams)."""
@@ -221,13 +287,14 @@ _PEAKS = {}
 
 
 def measured_peaks(ctx):
-    """MUFU ops/s (sin, cos, ex2 mix), FP32 and FP64 FMA FLOP/s measured on this GPU
+    """MUFU ops/s for sin / cos and for ex2, FP32 and FP64 FMA FLOP/s measured on this GPU
     (scw_measure_peaks; once per process)."""
     if not _PEAKS:
         from scwatter_gb300 import _lib
-        m, f32, f64 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-        _lib.call("scw_measure_peaks", ctx.handle, ctypes.byref(m), ctypes.byref(f32), ctypes.byref(f64))
-        _PEAKS.update(mufu_ops_per_s=m.value, fp32_flops=f32.value, fp64_flops=f64.value)
+        sc, e2, f32, f64 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _lib.call("scw_measure_peaks", ctx.handle, ctypes.byref(sc), ctypes.byref(e2), ctypes.byref(f32),
+                  ctypes.byref(f64))
+        _PEAKS.update(sincos_ops_per_s=sc.value, ex2_ops_per_s=e2.value, fp32_flops=f32.value, fp64_flops=f64.value)
     return dict(_PEAKS)
 
 
@@ -370,6 +437,7 @@ def run_ours(args):
             if i > 0:
                 e2e_t.append(time.perf_counter() - t0)
         t_e2e = float(np.mean(e2e_t))
+        bare = bare_copies(torch, hQ, host_out, out, nz_local)
         h2d_total, d2h_total = h2d_local, nz_local * Ny * Nx * 24
         if ws > 1:
             tt = torch.tensor([t_e2e], device="cuda")
@@ -389,8 +457,13 @@ def run_ours(args):
                                      "achieved": (h2d_local + nz_local * Ny * Nx * 24) / t_e2e / 1e9,
                                      "unit": "GB/s", "link_peaks_GBs": link,
                                      "t_link_bound_ms": t_bound * 1e3, "frac": t_bound / t_e2e,
+                                     "bare_copies_of_these_buffers_ms": bare,
+                                     "frac_vs_bare_copies": max(bare["h2d_ms"], bare["d2h_ms"]) / (t_e2e * 1e3),
+                                     "host_numa": host_numa(torch),
                                      "note": "frac = time the measured link needs for the step's H2D and D2H "
-                                             "bytes (the two directions overlap) / e2e time"}}
+                                             "bytes (the two directions overlap) / e2e time; bare copies: the "
+                                             "same pinned buffers copied alone, one cudaMemcpyAsync per slice "
+                                             "up and per 8 planes down"}}
     # dominant kernel: the stage-1 coefficient contraction streams every Q block once
     contract_ms = kt.get("sep_contract_kernel", (0.0, 0))[0]
     synth_ms = sum(v[0] for k, v in kt.items() if "synth" in k)
@@ -465,11 +538,14 @@ def run_ours(args):
                 "plain": {"value": plain_v, "unit": UNIT, "ms": plain_ms,
                           "sample": f"{P}x{P} xy patch in slice {CPU_SLICE}, {len(W32)} waves/point",
                           "sm_count": sm_count,
-                          "roofline": {"bound": "mufu", "achieved": 3 * plain_v,
-                                       "peak": pk["mufu_ops_per_s"], "unit": "MUFU ops/s",
-                                       "frac": 3 * plain_v / pk["mufu_ops_per_s"],
-                                       "count": "3 MUFU ops (sin, cos, ex2) per point*mode, the kernel's "
-                                                "inner loop; peak measured by scw_measure_peaks (same mix)"}},
+                          "roofline": {"bound": "mufu (sin, cos)", "achieved": PLAIN_XU_PER_PM * plain_v,
+                                       "peak": pk["sincos_ops_per_s"], "unit": "MUFU ops/s",
+                                       "frac": PLAIN_XU_PER_PM * plain_v / pk["sincos_ops_per_s"],
+                                       "count": f"{PLAIN_XU_PER_PM} XU instructions per point*mode (ncu "
+                                                "smsp__inst_executed_pipe_xu on an xy patch: one sin and one "
+                                                "cos; ex2 is skipped where the in-plane k is real); peak: "
+                                                "sin / cos rate measured by scw_measure_peaks",
+                                       "ex2_ops_per_s": pk["ex2_ops_per_s"]}},
                 "parity": parity,
                 "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                                  "sample": f"{rows} rows x {cw_} points of the same patch ({len(W32)} waves/point), "

@@ -434,10 +434,12 @@ SCW_API scw_status scw_layer_solve(scw_ctx ctx, int L, const double* ri, const d
 /* ---------------------------------------------------------------------------------- */
 /* Diagnostics (no reference counterpart)                                              */
 /* ---------------------------------------------------------------------------------- */
-/* Measured issue peaks of this GPU (any output may be NULL): MUFU operations per second for the
- * plain evaluator's mix (one sin.approx, cos.approx and ex2.approx each), FP32 and FP64 FMA
- * FLOP/s; independent dependency chains on every SM, event-timed; synchronises. */
-SCW_API scw_status scw_measure_peaks(scw_ctx ctx, double* mufu_ops_per_s, double* fp32_flops, double* fp64_flops);
+/* Measured issue peaks of this GPU (any output may be NULL): MUFU operations per second for
+ * sin.approx / cos.approx (the plain evaluator issues one of each per point and wave) and for
+ * ex2.approx (issued only where a wave's k has an imaginary part in the evaluated plane), FP32 and
+ * FP64 FMA FLOP/s; independent dependency chains on every SM, event-timed; synchronises. */
+SCW_API scw_status scw_measure_peaks(scw_ctx ctx, double* sincos_ops_per_s, double* ex2_ops_per_s, double* fp32_flops,
+                                     double* fp64_flops);
 
 #ifdef __cplusplus
 }

@@ -112,7 +112,7 @@ _SIGS = {
     "scw_sep_create_paired": [P, I32, I32, I32, I32, P, P, P, PP],
     "scw_sep_set_slice_paired": [P, I32, P, P, P, P, P],
     "scw_sep_form": [P, ctypes.POINTER(I32)],
-    "scw_measure_peaks": [P, P, P, P],
+    "scw_measure_peaks": [P, P, P, P, P],
     "scw_sep_get_grid": [P, P, P, P],
     "scw_sep_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
     "scw_sep_eval_volume_host": [P, P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],

@@ -212,6 +212,19 @@ struct Split<1> {           // bf16
     }
 };
 
+// bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from shared to global
+// memory, tracked by this thread's bulk groups
+__device__ __forceinline__ void bulk_store(void* gdst, const void* ssrc, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_u32(ssrc)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// this thread's committed bulk copies have finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// ... and have finished writing global memory
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -250,6 +263,15 @@ constexpr int kEpiWarps = 8, kProdWarps = 7;      // 16 warps with the MMA warp:
 constexpr int kEpiRows = kRows * 4 / kEpiWarps;     // output rows per epilogue warp and tile (8)
 constexpr int kTStages = 3;                          // staged T tiles in flight (cp.async ring)
 
+// Staged T rows (float2) in shared memory.  Fast path (Mk a multiple of the elements per core
+// row): a row holds a multiple of 8 16-byte chunks and chunk c of row r sits at c ^ t_swz(r), so
+// the producers' 16-byte reads (8 lanes per phase: 4 consecutive rows x 2 consecutive tasks
+// along K) land on 8 distinct bank groups.  Generic path: rows of Mk, unswizzled.
+__host__ __device__ constexpr bool t_fast(int Mk, int kind) { return Mk % (kind == 0 ? 4 : 8) == 0 && Mk % 2 == 0; }
+__host__ __device__ constexpr int t_row_stride(int Mk, int kind) { return t_fast(Mk, kind) ? ((Mk / 2 + 7) / 8) * 16 : Mk; }
+template <int kKind>
+__device__ __forceinline__ int t_swz(int row) { return kKind == 0 ? ((row & 1) | ((row & 2) << 1)) : (row & 3); }
+
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
 }
@@ -274,7 +296,7 @@ constexpr int kWsThreads = (kEpiWarps + kProdWarps + 1) * 32;
 template <int kKind>
 __global__ void __launch_bounds__(kWsThreads, 1)
 synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int nrows, int ncols, int Mk, int Kp,
-                float* __restrict__ out, int* __restrict__ err) {
+                int srows, float* __restrict__ out, int* __restrict__ err) {
     using E = typename Split<kKind>::T;
     constexpr int EB = Split<kKind>::kBytes;
     constexpr int EPC = 16 / EB;                              // elements per 16-byte core row
@@ -287,15 +309,15 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     const uint32_t acols = kbytes / 4;                        // TMEM columns of A (hi or lo): K * EB / 4
     unsigned char* sB0 = smem;                                // slot s, part h: sB0 + (2 s + h) b_bytes
     // ring of kTStages staged T tiles [kRows * 3][tstr], filled by cp.async kTStages - 1 tiles ahead
-    const int t_slot = (((kRows * 3 * (Mk + 4) * 8 + 127) / 128) * 128) / 8;     // float2 per slot
+    const int t_slot = (((kRows * 3 * t_row_stride(Mk, kKind) * 8 + 127) / 128) * 128) / 8;   // float2 per slot
     float2* sT = reinterpret_cast<float2*>(sB0 + 4 * b_bytes);
     const int t_tile = kRows * 3 * Mk;                           // float2 of T per tile
-    // fast producer path: Mk a multiple of the elements per core row; T rows padded in shared
-    // memory to an odd number of 16-byte chunks so a warp's 16-byte reads spread over the banks
-    const bool fast = (Mk % EPC) == 0 && (Mk % 2) == 0;
-    const int tstr = fast ? ((Mk / 2) % 2 == 0 ? Mk + 2 : Mk + 4) : Mk;
-    float* sOut = reinterpret_cast<float*>(sT + kTStages * t_slot);   // [epilogue warps][192]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sOut + kEpiWarps * 192);
+    // fast producer path: Mk a multiple of the elements per core row, swizzled T rows
+    const bool fast = t_fast(Mk, kKind);
+    const int tstr = t_row_stride(Mk, kKind);
+    // output staging: srows rows of 32 x-values x 6 floats (768 bytes) per epilogue warp
+    float* sOut = reinterpret_cast<float*>(sT + kTStages * t_slot);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sOut + kEpiWarps * srows * 192);
     uint64_t* full_b = bar;          // [2] producers -> MMA
     uint64_t* empty_b = bar + 2;     // [2] MMA completion -> producers
     uint64_t* acc_full = bar + 4;    // [2] MMA completion -> epilogue
@@ -364,8 +386,9 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         const int pt = tid - kEpiWarps * 32;                  // 0 .. kProdWarps * 32 - 1
         const int n4 = t_tile / 2;
         // fast path: tile ti's rows of T into ring slot ti % kTStages with 16-byte cp.async
-        // (row (r, c) at slot + (3 r + c) * tstr; the buffer has slack past the last row, whose
-        // values are masked below), one commit group per tile, empty groups past the last tile
+        // (row (r, c) at slot + (3 r + c) * tstr, chunks swizzled; the buffer has slack past the
+        // last row, whose values are masked below), one commit group per tile, empty groups past
+        // the last tile
         auto issue_t = [&](int ti) {
             if (ti < n_my) {
                 const int rr0 = ((int)blockIdx.y + ti * (int)gridDim.y) * kRows;
@@ -374,11 +397,36 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                 const int h = Mk / 2;                              // float4 per T row
                 for (int e = pt; e < n4; e += kProdWarps * 32) {
                     const int row = e / h;
-                    cp_async16(reinterpret_cast<float4*>(dst + row * tstr) + (e - row * h), src + e);
+                    cp_async16(reinterpret_cast<float4*>(dst + row * tstr) + ((e - row * h) ^ t_swz<kKind>(row)),
+                               src + e);
                 }
             }
             cp_async_commit();
         };
+        // fast path: task = (8-row block nb, row pair nq, core column kc); lanes: nq fastest, then
+        // kc. One task reads 16 bytes x EPC/2 of T row (4 nb + nq) once and writes the Re (n even)
+        // and Im (n odd) rows of B, hi and lo. A task's offsets are the same for every tile, so
+        // they are computed once: t_off[u] = T offset in float2 of the slot (-1: no task), the
+        // first of the task's EPC/2 chunks once swizzled; b_off[u] = B byte offset | T row / 3 << 20
+        // | (order of the task's chunks, XOR) << 24 | (kc odd) << 28 | (first K half) << 29.
+        constexpr int kTasks = (kN / 8 * 22 * 4 + kProdWarps * 32 - 1) / (kProdWarps * 32);
+        int t_off[kTasks];
+        uint32_t b_off[kTasks];
+#pragma unroll
+        for (int u = 0; u < kTasks; u++) {
+            const int tsk = pt + u * kProdWarps * 32;
+            const int q = tsk >> 2, nq = tsk & 3;
+            const int nb = q / KC, kc = q - nb * KC;
+            const int trow = 4 * nb + nq, k0 = kc * EPC;
+            const bool live = tsk < (kN / 8) * KC * 4 && k0 < 2 * Mk;
+            constexpr int m = EPC / 2 - 1;                        // chunks of one task - 1
+            const int g = t_swz<kKind>(trow);
+            const int c0 = (k0 < Mk ? k0 : k0 - Mk) / 2;          // first chunk of the task in its row
+            t_off[u] = live ? trow * tstr + 2 * (c0 ^ (g & ~m)) : -1;
+            b_off[u] = ((uint32_t)nb * sbo + (uint32_t)kc * 128u + (uint32_t)(2 * nq) * 16u) |
+                       ((uint32_t)(trow / 3) << 20) | ((uint32_t)(g & m) << 24) | ((uint32_t)(kc & 1) << 28) |
+                       ((uint32_t)(k0 < Mk) << 29);
+        }
         if (fast)
             for (int ti = 0; ti < kTStages - 1; ti++) issue_t(ti);
         for (int i = 0; i < n_my; i++) {
@@ -403,32 +451,22 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             }
             asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");
             if (fast) {
-                // task = (8-row block nb, row pair nq, core column kc); lanes: nq fastest, then kc.
-                // One task reads 16 bytes x EPC/2 of T row (4 nb + nq) once and writes the Re (n even)
-                // and Im (n odd) rows of B, hi and lo; the two stores per part are issued in an
-                // order that alternates with kc so each warp store covers all 8 bank groups.
-                const int ntask = (kN / 8) * KC * 4;
-                // up to kTasks tasks per thread, loads of all of them issued before any use
-                constexpr int kTasks = (kN / 8 * 22 * 4 + kProdWarps * 32 - 1) / (kProdWarps * 32);
+                // loads of all of this thread's tasks issued before any use; rows past nrows
+                // (the last tile) read as zeros
+                const int rows_left = nrows - r0;
                 float4 tv[kTasks][EPC / 2];
 #pragma unroll
                 for (int u = 0; u < kTasks; u++) {
-                    const int tsk = pt + u * kProdWarps * 32;
-                    const int q = tsk >> 2, nq = tsk & 3;
-                    const int nb = q / KC, kc = q - nb * KC;
-                    const int trow = 4 * nb + nq, k0 = kc * EPC;
-                    const bool ok = tsk < ntask && ((r0 + trow / 3) < nrows) && k0 < 2 * Mk;
-                    const float4* tp = reinterpret_cast<const float4*>(sTi + (ok ? trow * tstr + (k0 < Mk ? k0 : k0 - Mk) : 0));
+                    const bool ok = t_off[u] >= 0 && (int)((b_off[u] >> 20) & 15u) < rows_left;
+                    const float4* tp = reinterpret_cast<const float4*>(sTi + (ok ? t_off[u] : 0));
+                    const int gx = (int)((b_off[u] >> 24) & 3u);
 #pragma unroll
-                    for (int e2 = 0; e2 < EPC / 2; e2++) tv[u][e2] = ok ? tp[e2] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int e2 = 0; e2 < EPC / 2; e2++) tv[u][e2] = ok ? tp[e2 ^ gx] : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
 #pragma unroll
                 for (int u = 0; u < kTasks; u++) {
-                    const int tsk = pt + u * kProdWarps * 32;
-                    if (tsk >= ntask) break;
-                    const int q = tsk >> 2, nq = tsk & 3;
-                    const int nb = q / KC, kc = q - nb * KC;
-                    const bool first = kc * EPC < Mk;
+                    if (t_off[u] < 0) continue;
+                    const bool first = (b_off[u] >> 29) & 1u;
                     E h0[EPC], l0[EPC], h1[EPC], l1[EPC];
 #pragma unroll
                     for (int e2 = 0; e2 < EPC / 2; e2++) {
@@ -441,11 +479,11 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                         Split<kKind>::split(b0, h1[2 * e2], l1[2 * e2]);
                         Split<kKind>::split(b1, h1[2 * e2 + 1], l1[2 * e2 + 1]);
                     }
-                    const uint32_t base = (uint32_t)nb * sbo + (uint32_t)kc * 128u + (uint32_t)(2 * nq) * 16u;
+                    const uint32_t base = b_off[u] & 0xFFFFFu;
                     const uint4 vh0 = pack4<kKind>(h0), vh1 = pack4<kKind>(h1);
                     const uint4 vl0 = pack4<kKind>(l0), vl1 = pack4<kKind>(l1);
                     // the store order alternates with kc so each warp store covers all 8 bank groups
-                    if ((kc & 1) == 0) {
+                    if (((b_off[u] >> 28) & 1u) == 0) {
                         *reinterpret_cast<uint4*>(bh + base) = vh0;
                         *reinterpret_cast<uint4*>(bh + base + 16) = vh1;
                         *reinterpret_cast<uint4*>(bl + base) = vl0;
@@ -531,6 +569,15 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         __syncwarp();
     } else {
         // -------- epilogue (warp w: TMEM lanes 32 (w % 4) .. + 31, rows kEpiRows (w / 4) ..) --------
+        // TMEM -> registers (8 rows x 6 floats per lane); the accumulator is released as soon as the
+        // values are in registers.  Rows then go out through the warp's srows staging rows (lane l
+        // at float offset 6 l: 768 contiguous bytes per row), each full row as one bulk copy
+        // (cp.async.bulk shared -> global, issued by lane 0); a ragged or unaligned row is stored
+        // by the warp's lanes instead.
+        float* stage = sOut + warp * srows * 192;
+        const int quarter = warp & 3, part = warp >> 2;
+        const int xw = x0 + quarter * 32;                  // first x of this warp
+        const int nx = min(32, ncols - xw);               // valid x of this warp
         for (int i = 0; i < n_my; i++) {
             if (*abort_flag) break;
             const int a = i & 1;
@@ -541,39 +588,47 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                 break;
             }
             tc_fence_after();
-            const int quarter = warp & 3, part = warp >> 2;
             const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows + part * kEpiRows;
             const uint32_t tbase =
                 tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 128) + (uint32_t)(part * kEpiRows * 6);
-            // TMEM -> registers (8 rows x 6 floats per lane) -> per-row staging in shared memory
-            // (lane l at float offset 6 l) -> 768 contiguous bytes per row with 16-byte stores
             uint32_t v[kEpiRows * 6];
 #pragma unroll
             for (int c16 = 0; c16 < kEpiRows * 6 / 16; c16++) tmem_ld16(tbase + (uint32_t)(16 * c16), &v[16 * c16]);
             tmem_ld_wait();
-            float* stage = sOut + warp * 192;
-            const int xw = x0 + quarter * 32;                  // first x of this warp
-            const int nx = min(32, ncols - xw);               // valid x of this warp
-#pragma unroll
-            for (int r = 0; r < kEpiRows; r++) {
-                const int row = r0 + r;
-                if (row >= nrows || nx <= 0) break;           // warp-uniform
-                reinterpret_cast<float2*>(stage)[3 * lane + 0] = make_float2(__uint_as_float(v[6 * r + 0]), __uint_as_float(v[6 * r + 1]));
-                reinterpret_cast<float2*>(stage)[3 * lane + 1] = make_float2(__uint_as_float(v[6 * r + 2]), __uint_as_float(v[6 * r + 3]));
-                reinterpret_cast<float2*>(stage)[3 * lane + 2] = make_float2(__uint_as_float(v[6 * r + 4]), __uint_as_float(v[6 * r + 5]));
-                __syncwarp();
-                float* dst = out + ((long long)row * ncols + xw) * 6;
-                if (nx == 32 && ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0)) {
-                    reinterpret_cast<float4*>(dst)[lane] = reinterpret_cast<const float4*>(stage)[lane];
-                    if (lane < 16) reinterpret_cast<float4*>(dst)[32 + lane] = reinterpret_cast<const float4*>(stage)[32 + lane];
-                } else {
-                    for (int f = lane; f < nx * 6; f += 32) dst[f] = stage[f];
-                }
-                __syncwarp();
-            }
             tc_fence_before();
             mbar_arrive(&acc_empty[a]);
+            for (int g0 = 0; g0 < kEpiRows; g0 += srows) {
+                // the staging rows are reusable once the bulk copies issued from them have read them
+                if (lane == 0) bulk_wait_read0();
+                __syncwarp();
+#pragma unroll
+                for (int r = 0; r < kEpiRows; r++) {
+                    if (r < g0 || r >= g0 + srows) continue;
+                    float2* st = reinterpret_cast<float2*>(stage + (r - g0) * 192);
+                    st[3 * lane + 0] = make_float2(__uint_as_float(v[6 * r + 0]), __uint_as_float(v[6 * r + 1]));
+                    st[3 * lane + 1] = make_float2(__uint_as_float(v[6 * r + 2]), __uint_as_float(v[6 * r + 3]));
+                    st[3 * lane + 2] = make_float2(__uint_as_float(v[6 * r + 4]), __uint_as_float(v[6 * r + 5]));
+                }
+                fence_proxy_async();              // the staged rows visible to the bulk copies
+                __syncwarp();
+                for (int r = g0; r < g0 + srows; r++) {
+                    const int row = r0 + r;
+                    if (row >= nrows || nx <= 0) break;           // warp-uniform
+                    float* dst = out + ((long long)row * ncols + xw) * 6;
+                    const float* src = stage + (r - g0) * 192;
+                    if (nx == 32 && ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0)) {
+                        if (lane == 0) bulk_store(dst, src, 768u);
+                    } else {
+                        for (int f = lane; f < nx * 6; f += 32) dst[f] = src[f];
+                    }
+                }
+                if (lane == 0) bulk_commit();
+                __syncwarp();
+            }
         }
+        // every bulk copy of this warp has written global memory before the kernel ends
+        if (lane == 0) bulk_wait_all();
+        __syncwarp();
     }
     __syncthreads();
     if (tid == 0 && *abort_flag) atomicExch(err, 1);
@@ -592,8 +647,12 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int kalign = kind == 0 ? 8 : 16;                  // K per MMA instruction
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
-    const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * (Mk + 4) * 8 + 127) / 128 * 128;   // padded rows
-    const size_t smem = (tc::kN / 8) * sbo * 4 + tc::kTStages * t_tile_bytes + tc::kEpiWarps * 192 * 4 + 128;
+    const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * tc::t_row_stride(Mk, kind) * 8 + 127) / 128 * 128;
+    // output staging rows per epilogue warp: 8 (one bulk group per tile) when shared memory allows
+    const size_t fixed = (tc::kN / 8) * sbo * 4 + tc::kTStages * t_tile_bytes + 128;
+    int srows = tc::kEpiRows;
+    while (srows > 1 && fixed + (size_t)tc::kEpiWarps * srows * 768 > 227 * 1024) srows /= 2;
+    const size_t smem = fixed + (size_t)tc::kEpiWarps * srows * 768;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     if (tc::kAcol + 2 * (size_t)Kp * EB / 4 > tc::kTmemCols) return SCW_ERR_UNSUPPORTED;   // A (hi, lo) in TMEM
     if (!ctx->tc_err) {
@@ -609,10 +668,12 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     LaunchTimer lt(ctx, kind == 0 ? "synth_tc_kernel<tf32x3>" : "synth_tc_kernel<bf16x3>");
     if (kind == 0) {
         SCW_CUDA_TRY(cudaFuncSetAttribute(tc::synth_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        tc::synth_tc_kernel<0><<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, out, ctx->tc_err);
+        tc::synth_tc_kernel<0><<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, srows, out,
+                                                                             ctx->tc_err);
     } else {
         SCW_CUDA_TRY(cudaFuncSetAttribute(tc::synth_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        tc::synth_tc_kernel<1><<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, out, ctx->tc_err);
+        tc::synth_tc_kernel<1><<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, srows, out,
+                                                                             ctx->tc_err);
     }
     SCW_CUDA_TRY(cudaGetLastError());
     ctx->launches++;

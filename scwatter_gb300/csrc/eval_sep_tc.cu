@@ -429,27 +429,27 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         }
         if (fast)
             for (int ti = 0; ti < kTStages - 1; ti++) issue_t(ti);
+        // one producer barrier per tile: it publishes tile i's T (this thread's copies are in once
+        // all but the newest group have completed), frees the slot of tile i - 1 for the copies of
+        // tile i + kTStages - 1 issued after it, and makes the abort decision uniform
         for (int i = 0; i < n_my; i++) {
             const int s = i & 1;
             int stop = *abort_flag;
             if (!stop && i >= 2 && !mbar_wait(&empty_b[s], (uint32_t)(((i >> 1) - 1) & 1))) stop = 1;
+            const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
+            unsigned char* bh = sB0 + (2 * s + 0) * b_bytes;
+            unsigned char* bl = sB0 + (2 * s + 1) * b_bytes;
+            float2* sTi = sT + (i % kTStages) * t_slot;
+            if (fast) {
+                cp_async_wait<kTStages - 2>();
+            } else if (!stop) {
+                for (int e = pt; e < t_tile; e += kProdWarps * 32) sTi[e] = T[(long long)r0 * 3 * Mk + e];
+            }
             if (producers_any(stop)) {
                 *abort_flag = 1;
                 break;
             }
-            const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows;
-            unsigned char* bh = sB0 + (2 * s + 0) * b_bytes;
-            unsigned char* bl = sB0 + (2 * s + 1) * b_bytes;
-            // tile i's T: this thread's copies are in once all but the kTStages - 1 newest groups
-            // have completed; the barrier makes every producer's copies visible
-            float2* sTi = sT + (i % kTStages) * t_slot;
-            if (fast) {
-                issue_t(i + kTStages - 1);
-                cp_async_wait<kTStages - 1>();
-            } else {
-                for (int e = pt; e < t_tile; e += kProdWarps * 32) sTi[e] = T[(long long)r0 * 3 * Mk + e];
-            }
-            asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");
+            if (fast) issue_t(i + kTStages - 1);
             if (fast) {
                 // loads of all of this thread's tasks issued before any use; rows past nrows
                 // (the last tile) read as zeros
@@ -529,7 +529,6 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             }
             fence_proxy_async();
             mbar_arrive(&full_b[s]);
-            asm volatile("bar.sync 1, %0;" ::"n"(kProdWarps * 32) : "memory");   // sT slot reusable
         }
         cp_async_wait<0>();        // no copy into shared memory outlives the loop (also after an abort)
     } else if (warp == kEpiWarps + kProdWarps) {

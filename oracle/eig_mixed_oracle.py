@@ -72,9 +72,11 @@ def refine(A, lam32, X32, steps=10, tau_rel=1e-5, deg_rel=1e-12, tol=1e-14, tol_
         if s == steps:
             return False, lam, X, hist
         X32s = X.astype(np.complex64)
+        # E = X^-1 R by LAPACK's single-precision LU (cgesv).  numpy.linalg.solve would compute
+        # in double precision for complex64 input and round, which is not what the GPU does.
         try:                                   # a singular eigenvector matrix: lu_check_kernel's refusal
-            E = np.linalg.solve(X32s, R.astype(np.complex64)).astype(np.complex128)
-        except np.linalg.LinAlgError:
+            E = scipy.linalg.solve(X32s, R.astype(np.complex64), check_finite=False).astype(np.complex128)
+        except (np.linalg.LinAlgError, scipy.linalg.LinAlgError):
             return False, lam, X, hist
         lam = lam + np.where(single, np.diag(E), 0)
         Ys = []

@@ -3,6 +3,7 @@ on reduced layer matrices of the workloads: FP32 eigenpairs refined to FP64 resi
 eigenvalues matching FP64 LAPACK, and a defective matrix refused."""
 import numpy as np
 import pytest
+import scipy.linalg
 
 from oracle import eig_mixed_oracle as emo
 from oracle import solve_oracle as so
@@ -29,8 +30,16 @@ def _pq(vol, coef, lam=1.0, size=None, direction=(0.0, 0.0, 1.0)):
     return out
 
 
+def _eig32(A):
+    """Eigenpairs from LAPACK's single-precision cgeev.  (numpy.linalg.eig on complex64 input
+    computes in double precision and rounds the result, which is not an FP32 start.)"""
+    lam32, X32 = scipy.linalg.eig(A.astype(np.complex64), check_finite=False)
+    assert lam32.dtype == np.complex64 and X32.dtype == np.complex64
+    return lam32, X32
+
+
 def _check(A, tol_eig=1e-11):
-    lam32, X32 = np.linalg.eig(A.astype(np.complex64))
+    lam32, X32 = _eig32(A)
     ok, lam, X, hist = emo.refine(A, lam32, X32)
     assert ok, hist
     assert hist[0] > 1e-9 and hist[-1] <= 1e-12          # from FP32 quality to FP64 quality
@@ -63,6 +72,6 @@ def test_grf_layer():
 def test_jordan_block_is_refused():
     n = 24
     J = np.diag(np.full(n, 0.5 + 0.1j)) + np.diag(np.ones(n - 1), 1)
-    lam32, X32 = np.linalg.eig(J.astype(np.complex64))
+    lam32, X32 = _eig32(J)
     ok, lam, X, hist = emo.refine(J, lam32, X32)
     assert not ok

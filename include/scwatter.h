@@ -231,6 +231,10 @@ SCW_API scw_status scw_sep_eval_slab_host(scw_sep s, const void* Q_host, float x
  * 192 MiB) and output bytes per read-back slab (whole planes, at least one; default 64 MiB; three
  * slabs are kept on the device).  0 restores a default. */
 SCW_API scw_status scw_sep_set_streaming(scw_sep s, int64_t chunk_bytes, int64_t slab_bytes);
+/* Tile shape of the coefficient contraction: 0 (default) = 8, 8, 4, 2 mode rows per warp for
+ * launches of 1, 2, 4, 8 planes per group; 1 = half as many.  Results are bit-identical; the
+ * batch autotuner picks it for its items. */
+SCW_API scw_status scw_sep_set_tiles(scw_sep s, int ctr_shape);
 SCW_API scw_status scw_sep_eval_plane_device(scw_sep s, int axis, float a_start, float b_start, float c,
                                              float d, int N, float* dE, int method);
 SCW_API scw_status scw_sep_gpu_cw_evaluate(scw_sep s, float* E_xy, float* E_xz, float* E_yz,
@@ -352,8 +356,9 @@ typedef struct scw_batch_item {
     float dx, dy, dz;
     int Nx, Ny, Nz;
 } scw_batch_item;
-/* lanes: concurrent streams (0 = autotune); method: SCW_SEP_* output GEMM (0 = autotune).
- * Plans, uploads, autotunes on a stratified subset, and captures the graph. */
+/* lanes: concurrent streams (0 = autotune); method: SCW_SEP_* output GEMM (0 = autotune); the
+ * contraction tile shape is always autotuned.  Plans, uploads, autotunes on stratified subsets,
+ * and captures the graph. */
 SCW_API scw_status scw_batch_create(scw_ctx ctx, const scw_batch_item* items, int count, int lanes, int method,
                                     scw_batch* out);
 /* One cudaGraphLaunch on the context stream (asynchronous). */
@@ -364,13 +369,14 @@ SCW_API scw_status scw_batch_wait(scw_batch b, int* item_status);
 SCW_API scw_status scw_batch_get(scw_batch b, int i, double* x, double* gamma, float* field_host, float** field_device);
 /* harmonics, slices and points x modes of the item's volume */
 SCW_API scw_status scw_batch_item_info(scw_batch b, int i, int* M0, int* M1, int* n_slices, int64_t* points_modes);
-/* chosen lanes / method, graph nodes, kernels per launch, tuning time and its log
- * (triples lanes, method, ms; n_tune entries). */
 /* The mixed eigen-solver's record of item i after a run, as scw_solution_eig_info. */
 SCW_API scw_status scw_batch_item_eig(scw_batch b, int i, int* mixed, int* accepted, int* max_steps,
                                       double* max_residual, int* residual_checks);
-SCW_API scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int64_t* graph_nodes, int64_t* kernels,
-                                  double* tune_ms, double* tune_log, int* n_tune);
+/* chosen lanes / method / contraction tile shape (0: default rows per warp, 1: half), graph
+ * nodes, kernels per launch, tuning time and its log (quadruples lanes, method, tile shape, ms;
+ * n_tune entries, at most 16). */
+SCW_API scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int* ctr_shape, int64_t* graph_nodes,
+                                  int64_t* kernels, double* tune_ms, double* tune_log, int* n_tune);
 SCW_API scw_status scw_batch_destroy(scw_batch b);
 
 /* ---------------------------------------------------------------------------------- */

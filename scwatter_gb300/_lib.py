@@ -85,7 +85,7 @@ _SIGS = {
     "scw_batch_get": [P, I32, P, P, P, PP],
     "scw_batch_item_info": [P, I32, P, P, P, P],
     "scw_batch_item_eig": [P, I32, P, P, P, P, P],
-    "scw_batch_info": [P, P, P, P, P, P, P, P],
+    "scw_batch_info": [P, P, P, P, P, P, P, P, P],
     "scw_batch_destroy": [P],
     "scw_layer_problem": [P, P, I32, I32, I32, P, P, P, P, P],
     "scw_mlp_create": [P, I32, I32, I32, ctypes.c_uint64, PP],
@@ -117,6 +117,7 @@ _SIGS = {
     "scw_sep_eval_volume_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
     "scw_sep_eval_volume_host": [P, P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
     "scw_sep_set_streaming": [P, I64, I64],
+    "scw_sep_set_tiles": [P, I32],
     "scw_sep_eval_slab_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, I32, P, I32],
     "scw_sep_eval_slab_host": [P, P, F32, F32, F32, F32, F32, F32, I32, I32, I32, I32, P, I32],
     "scw_sep_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P, I32],

@@ -110,15 +110,16 @@ class Batch:
         return x, g, f
 
     def info(self) -> dict:
-        lanes, method, n_tune = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        lanes, method, shape, n_tune = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         nodes, kernels = ctypes.c_int64(), ctypes.c_int64()
         tune_ms = ctypes.c_double()
-        log = np.zeros(3 * 16, np.float64)
-        _lib.call("scw_batch_info", self.handle, ctypes.byref(lanes), ctypes.byref(method), ctypes.byref(nodes),
-                  ctypes.byref(kernels), ctypes.byref(tune_ms), ctypes.c_void_p(log.ctypes.data), ctypes.byref(n_tune))
-        return {"lanes": lanes.value, "method": method.value, "graph_nodes": nodes.value, "kernels": kernels.value,
-                "tune_ms": tune_ms.value,
-                "tune_log": [tuple(log[3 * k:3 * k + 3]) for k in range(n_tune.value)]}
+        log = np.zeros(4 * 16, np.float64)
+        _lib.call("scw_batch_info", self.handle, ctypes.byref(lanes), ctypes.byref(method), ctypes.byref(shape),
+                  ctypes.byref(nodes), ctypes.byref(kernels), ctypes.byref(tune_ms), ctypes.c_void_p(log.ctypes.data),
+                  ctypes.byref(n_tune))
+        return {"lanes": lanes.value, "method": method.value, "ctr_shape": shape.value, "graph_nodes": nodes.value,
+                "kernels": kernels.value, "tune_ms": tune_ms.value,
+                "tune_log": [tuple(log[4 * k:4 * k + 4]) for k in range(n_tune.value)]}
 
     def close(self):
         if self.handle:

@@ -14,7 +14,8 @@
 //  * results (x, gamma, status words, field volumes) live in arenas indexed per item.
 // The autotuner picks the lane count (bounded by free memory) and the output-GEMM form
 // (3xTF32 or split-BF16 tcgen05, or FP32 SIMT) by timing graphs of a stratified subset of the
-// cheaper half of the items.
+// cheaper half of the items, and the contraction tile shape (rows per warp) by timing the
+// evaluations alone of a stratified subset of all items.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -75,7 +76,8 @@ struct scw_batch_s {
     long long kernels = 0;
     double tune_ms = 0;
     int tuned = 0;
-    std::vector<double> tune_log;  // lanes, method, ms per candidate
+    std::vector<double> tune_log;  // lanes, method, contraction tile shape, ms per candidate
+    int ctr_shape = 0;             // chosen contraction tile shape (scw_sep_s::ctr_shape)
     ~scw_batch_s() {
         ::scw::DeviceScope dev_scope_(ctx ? ctx->device : -1);
         g.reset();
@@ -159,8 +161,11 @@ scw_status ensure_lanes(scw_batch b, int lanes) {
     return SCW_OK;
 }
 
-// Captures the items `idx` on `lanes` lanes with output-GEMM `method` into graph `g`.
-scw_status build_graph(scw_batch b, const std::vector<int>& idx, int lanes, int method, Graph& g) {
+// Captures the items `idx` on `lanes` lanes with output-GEMM `method` and contraction tile shape
+// `ctr_shape` into graph `g`; `eval_only`: the evaluations alone (the tile-shape tuning: their
+// time does not depend on the amplitude values, which are whatever the lane arenas hold)
+scw_status build_graph(scw_batch b, const std::vector<int>& idx, int lanes, int method, int ctr_shape, Graph& g,
+                       bool eval_only = false) {
     g.reset();
     scw_status st = ensure_lanes(b, lanes);
     if (st != SCW_OK) return st;
@@ -205,7 +210,7 @@ scw_status build_graph(scw_batch b, const std::vector<int>& idx, int lanes, int 
             o.Qsep = sb.Q;
             o.sepKz = sb.kz;
             o.sepExt = sb.ext;
-            rec = scw::sv::record_solve(it.sp, it.in, ws, o, b->lane_stream[l], &kernels);
+            if (!eval_only) rec = scw::sv::record_solve(it.sp, it.in, ws, o, b->lane_stream[l], &kernels);
             if (rec != SCW_OK) break;
             it.sep.ctx = b->lane_ctx[l];
             it.sep.dkx = it.dkx;
@@ -215,6 +220,7 @@ scw_status build_graph(scw_batch b, const std::vector<int>& idx, int lanes, int 
             it.sep.dKz = sb.kz;
             it.sep.dQ = sb.Q;
             it.ep.method = method;
+            it.sep.ctr_shape = ctr_shape;
             const long long before = b->lane_ctx[l]->launches;
             rec = scw::sep_eval_record(&it.sep, it.ep, it.desc, scratch, it.field);
             kernels += b->lane_ctx[l]->launches - before;
@@ -384,12 +390,12 @@ scw_status scw_batch_create(scw_ctx ctx, const scw_batch_item* items, int count,
             for (int L : {1, 2, 4, 8, 16}) {
                 if (L > max_lanes || L > (int)sub.size() * 2) break;
                 Graph g;
-                scw_status st = build_graph(b.get(), sub, L, best_m, g);
+                scw_status st = build_graph(b.get(), sub, L, best_m, 0, g);
                 double ms = 0;
                 if (st == SCW_OK) st = time_graph(b.get(), g, &ms);
                 g.reset();
                 if (st != SCW_OK) return st;
-                b->tune_log.insert(b->tune_log.end(), {(double)L, (double)best_m, ms});
+                b->tune_log.insert(b->tune_log.end(), {(double)L, (double)best_m, 0.0, ms});
                 b->tuned++;
                 if (ms < best) {
                     best = ms;
@@ -401,12 +407,12 @@ scw_status scw_batch_create(scw_ctx ctx, const scw_batch_item* items, int count,
             best = 1e300;
             for (int m : {SCW_SEP_TF32X3, SCW_SEP_BF16X3, SCW_SEP_FP32}) {
                 Graph g;
-                scw_status st = build_graph(b.get(), sub, best_l, m, g);
+                scw_status st = build_graph(b.get(), sub, best_l, m, 0, g);
                 double ms = 0;
                 if (st == SCW_OK) st = time_graph(b.get(), g, &ms);
                 g.reset();
                 if (st != SCW_OK) return st;
-                b->tune_log.insert(b->tune_log.end(), {(double)best_l, (double)m, ms});
+                b->tune_log.insert(b->tune_log.end(), {(double)best_l, (double)m, 0.0, ms});
                 b->tuned++;
                 if (ms < best) {
                     best = ms;
@@ -417,10 +423,38 @@ scw_status scw_batch_create(scw_ctx ctx, const scw_batch_item* items, int count,
         lanes = best_l;
         method = best_m;
     }
-    b->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     b->lanes = std::min(lanes, max_lanes);
     b->method = method;
-    scw_status st = build_graph(b.get(), all, b->lanes, b->method, b->g);
+    // contraction tile shape: the evaluations of the calibration subset alone, each shape timed
+    {
+        std::vector<int> by_cost(all);
+        std::sort(by_cost.begin(), by_cost.end(), [&](int x, int y) { return b->items[x].cost < b->items[y].cost; });
+        std::vector<int> sub;
+        const int want = std::min(count, 8);
+        for (int j = 0; j < want; j++) sub.push_back(by_cost[(size_t)j * count / want]);
+        double best = 1e300;
+        for (int shape : {0, 1}) {
+            Graph g;
+            const int tl = std::min(b->lanes, (int)sub.size());
+            scw_status st = build_graph(b.get(), sub, tl, b->method, shape, g, true);
+            // defined amplitudes and wave numbers (zeros) for the timed evaluations
+            for (int l = 0; l < tl && st == SCW_OK; l++)
+                if (b->lane_arena[l] && cudaMemsetAsync(b->lane_arena[l], 0, b->lane_bytes[l], b->origin) != cudaSuccess)
+                    st = fail(SCW_ERR_CUDA, "scw_batch: clearing a lane arena");
+            double ms = 0;
+            if (st == SCW_OK) st = time_graph(b.get(), g, &ms);
+            g.reset();
+            if (st != SCW_OK) return st;
+            b->tune_log.insert(b->tune_log.end(), {(double)b->lanes, (double)b->method, (double)shape, ms});
+            b->tuned++;
+            if (ms < best) {
+                best = ms;
+                b->ctr_shape = shape;
+            }
+        }
+    }
+    b->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    scw_status st = build_graph(b.get(), all, b->lanes, b->method, b->ctr_shape, b->g);
     if (st != SCW_OK) return st;
     // lane error flags start clear
     for (auto c : b->lane_ctx) SCW_CUDA_TRY(cudaMemset(c->tc_err, 0, sizeof(int)));
@@ -526,11 +560,12 @@ scw_status scw_batch_item_eig(scw_batch b, int i, int* mixed, int* accepted, int
     return SCW_OK;
 }
 
-scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int64_t* graph_nodes, int64_t* kernels,
+scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int* ctr_shape, int64_t* graph_nodes, int64_t* kernels,
                           double* tune_ms, double* tune_log, int* n_tune) {
     if (!b) return fail(SCW_ERR_ARG, "null batch");
     if (lanes) *lanes = b->lanes;
     if (method) *method = b->method;
+    if (ctr_shape) *ctr_shape = b->ctr_shape;
     if (graph_nodes) *graph_nodes = (int64_t)b->g.nodes;
     if (kernels) *kernels = b->kernels;
     if (tune_ms) *tune_ms = b->tune_ms;

@@ -495,10 +495,17 @@ static scw_status stage1_record(scw_sep s, const SepEvalPlan& p, const char* d_d
                 return SCW_OK;
             };
             scw_status ls;
-            if (nks == 1) ls = launch(sep_contract_kernel<1, 8>, 8, CtrCfg<8, 1>::kSmem);
-            else if (nks == 2) ls = launch(sep_contract_kernel<2, 8>, 8, CtrCfg<8, 2>::kSmem);
-            else if (nks == 4) ls = launch(sep_contract_kernel<4, 4>, 4, CtrCfg<4, 4>::kSmem);
-            else ls = launch(sep_contract_kernel<8, 2>, 2, CtrCfg<2, 8>::kSmem);
+            if (s->ctr_shape == 0) {
+                if (nks == 1) ls = launch(sep_contract_kernel<1, 8>, 8, CtrCfg<8, 1>::kSmem);
+                else if (nks == 2) ls = launch(sep_contract_kernel<2, 8>, 8, CtrCfg<8, 2>::kSmem);
+                else if (nks == 4) ls = launch(sep_contract_kernel<4, 4>, 4, CtrCfg<4, 4>::kSmem);
+                else ls = launch(sep_contract_kernel<8, 2>, 2, CtrCfg<2, 8>::kSmem);
+            } else {
+                if (nks == 1) ls = launch(sep_contract_kernel<1, 4>, 4, CtrCfg<4, 1>::kSmem);
+                else if (nks == 2) ls = launch(sep_contract_kernel<2, 4>, 4, CtrCfg<4, 2>::kSmem);
+                else if (nks == 4) ls = launch(sep_contract_kernel<4, 2>, 2, CtrCfg<2, 4>::kSmem);
+                else ls = launch(sep_contract_kernel<8, 1>, 1, CtrCfg<1, 8>::kSmem);
+            }
             if (ls != SCW_OK) return ls;
             SCW_CUDA_TRY(cudaGetLastError());
             ctx->launches++;
@@ -1091,6 +1098,12 @@ scw_status scw_sep_set_streaming(scw_sep s, int64_t chunk_bytes, int64_t slab_by
     if (!s || chunk_bytes < 0 || slab_bytes < 0) return fail(SCW_ERR_ARG, "scw_sep_set_streaming: bad arguments");
     s->chunk_bytes = (size_t)chunk_bytes;
     s->slab_target = (size_t)slab_bytes;
+    return SCW_OK;
+}
+
+scw_status scw_sep_set_tiles(scw_sep s, int ctr_shape) {
+    if (!s || ctr_shape < 0 || ctr_shape > 1) return fail(SCW_ERR_ARG, "scw_sep_set_tiles: bad arguments");
+    s->ctr_shape = ctr_shape;
     return SCW_OK;
 }
 

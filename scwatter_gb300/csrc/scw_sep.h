@@ -65,6 +65,10 @@ struct scw_sep_s {
     //     over (Ex, Ey, Ez) -- the structure of the solver's modes, whose E rows are the same
     //     eigenvector for the two roots +-gamma and whose H rows (hence Ez) change sign.
     int halves = 2;
+    // contraction tile shape: 0 = the default rows per warp for the launch's planes per group
+    // (8, 8, 4, 2 for 1, 2, 4, 8 planes), 1 = half as many rows per warp (twice the CTAs);
+    // chosen by the batch autotuner
+    int ctr_shape = 0;
     float2* dQ = nullptr;
     double2* dBeta = nullptr;
     bool own_Q = false;

@@ -209,6 +209,10 @@ class SeparableSet:
                   ctypes.c_void_p(_host_ptr(out, "out")), int(method))
         return out
 
+    def set_tiles(self, ctr_shape: int = 0):
+        """Contraction tile shape (``scw_sep_set_tiles``): 0 = default rows per warp, 1 = half."""
+        _lib.call("scw_sep_set_tiles", self.handle, int(ctr_shape))
+
     def set_streaming(self, chunk_bytes: int = 0, slab_bytes: int = 0):
         """Upload chunk (Q bytes, whole slices) and read-back slab (output bytes, whole planes)
         of :meth:`eval_volume_host`; 0 keeps the defaults (192 MiB, 64 MiB)."""

@@ -83,7 +83,10 @@ def test_batch_autotune(ctx):
     items = _items()
     b = Batch(ctx, items)
     info = b.info()
-    assert info["lanes"] >= 1 and info["method"] in (1, 2, 3) and len(info["tune_log"]) >= 3
+    assert info["lanes"] >= 1 and info["method"] in (1, 2, 3) and len(info["tune_log"]) >= 5
+    assert info["ctr_shape"] in (0, 1)
+    # the tile-shape candidates were timed on evaluation-only graphs, both shapes
+    assert {int(e[2]) for e in info["tune_log"]} == {0, 1}
     b.run()
     assert (b.wait() == 0).all()
     for i, it in enumerate(items):

@@ -273,3 +273,21 @@ def test_paired_factored_file_round_trip(ctx, tmp_path):
     fs = ps.to_factored()
     np.testing.assert_allclose(host.Q[:, 0], fs.Q_dn, rtol=0, atol=1e-7 * np.abs(fs.Q_dn).max())
     np.testing.assert_allclose(host.Q[:, 1], fs.Q_up, rtol=0, atol=1e-7 * np.abs(fs.Q_up).max())
+
+
+@pytest.mark.parametrize("dz,Nz", [(1.0, 4), (0.5, 8), (0.3, 11), (0.1, 31)])
+def test_contraction_tile_shapes_bit_identical(ctx, dz, Nz):
+    """Both contraction tile shapes (scw_sep_set_tiles: default rows per warp, or half) give the
+    same volume bit for bit, for plane densities that select 1 to 8 planes per contraction
+    group, on a paired and a two-half set."""
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import TF32X3, SeparableSet
+    ps = synthetic.make_paired(M0=8, M1=6, Z=3, size=(16.0, 12.0, 3.0), seed=11)
+    grid = (np.float32(-7), np.float32(-6), np.float32(-1.6), np.float32(0.4), np.float32(0.55), np.float32(dz),
+            37, 21, Nz)
+    for sep in (SeparableSet.from_paired(ctx, ps), SeparableSet.from_factored(ctx, ps.to_factored())):
+        a = _eval_device(ctx, sep, grid, TF32X3)
+        sep.set_tiles(1)
+        b = _eval_device(ctx, sep, grid, TF32X3)
+        sep.set_tiles(0)
+        assert np.array_equal(a, b)

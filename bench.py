@@ -773,7 +773,9 @@ def batch_leg(args):
     macs = sum(fp64_solve_macs(M0, M1, Z, it.sample.shape[1], it.sample.shape[2], e["residual_checks"])
                for (M0, M1, Z), it, e in zip(shapes, items, eigs))
     eig = {"slices": sum(sh[2] for sh in shapes), "accepted": sum(e["accepted"] for e in eigs),
-           "max_steps": max(e["max_steps"] for e in eigs), "max_residual": max(e["max_residual"] for e in eigs)}
+           "max_steps": max(e["max_steps"] for e in eigs), "max_residual": max(e["max_residual"] for e in eigs),
+           "items_with_fp64_qr_slices": [[i, 2 * sh[0] * sh[1], sh[2] - e["accepted"]]
+                                         for i, (sh, e) in enumerate(zip(shapes, eigs)) if e["accepted"] < sh[2]]}
     print(json.dumps({"metric": "samples/s", "value": len(items) / t, "unit": "samples/s", "n_gpus": 1,
                       "steps": len(times), "warmup": args.batch_warmup, "ms_per_step": t * 1e3,
                       "higher_is_better": True,

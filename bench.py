@@ -51,7 +51,7 @@ CFG2 = dict(name="spheres[64,128,128] coef40x40 64 slices, grid 512x512x256", M0
 CONTRACT_TRAFFIC_RATIO = (985.032448e6 + 4.474368e6) / (8 * 3 * 1600 * 3200 * 8 + 32 * 3 * 1600 * 8)
 # XU (MUFU) thread instructions per point*mode of plain_eval_kernel on an xy plane, from ncu
 # (smsp__inst_executed_pipe_xu.sum x 32 / points*modes = 656e6 x 32 / 1.0486e10 on a 32 x 32 patch
-# of the config-2 set)
+# of the [64,128,128] sphere set, 40 x 40 harmonics)
 PLAIN_XU_PER_PM = 2.0
 PLAIN_PATCH = 128          # plain-form sample: PLAIN_PATCH x PLAIN_PATCH points of one interior xy plane
 CPU_SLICE = 3              # the slice the plain and CPU samples lie in
@@ -565,7 +565,7 @@ def run_ours(args):
 
 CFG1 = dict(name="spheres[20,64,64] coef20x20, 20 slices (the CPU-runnable sphere workload)", shape=(20, 64, 64),
             coef=(20, 20), size=(64.0, 64.0, 20.0))
-CPU_SOLVE_SLICES = 2       # slices of the config-1 sample the CPU oracle solve is timed on
+CPU_SOLVE_SLICES = 2       # slices of the [20,64,64] sphere sample the CPU oracle solve is timed on
 
 
 def fp64_solve_macs(M0, M1, Z, Y, X, checks, pz=True):
@@ -662,7 +662,7 @@ def solve_leg(ctx):
     eig = g.eig
     macs = fp64_solve_macs(c["coef"][0], c["coef"][1], c["shape"][0], c["shape"][1], c["shape"][2],
                            eig["residual_checks"])
-    # every evaluator against FP64 on the solved coefficients (BASELINE config 3 at M = 20)
+    # every evaluator against FP64 on the solved coefficients (the solved sphere sample, coef 20 x 20)
     parity = solved_parity(ctx, g, slices=(3, 7, 10, 14, 17))
     del g
     cut = vol[:CPU_SOLVE_SLICES]
@@ -691,7 +691,7 @@ def solve_leg(ctx):
 
 
 def solved_leg(args):
-    """The config-2 sphere sample ([64, 128, 128], 40 x 40 harmonics, 64 slices) solved on the GPU
+    """The sphere sample [64, 128, 128] (40 x 40 harmonics, 64 slices) solved on the GPU
     (FP64), then its separable set evaluated on the 512 x 512 x 256 grid (time per step) and every
     evaluator checked against FP64 on 2 x 16 x 16 points in each of 8 slices (4096 points)."""
     import torch
@@ -861,7 +861,7 @@ def probe(kind):
     """Small single-shot cases for ncu captures (one pass of the kernels named, nothing timed):
     ``eig-mixed``: the mixed eigen-solver on the first 2 slices of the sphere sample (n = 800);
     ``zgemm``: 4 batched 800 x 800 x 800 complex128 products;
-    ``plain``: the plain summation kernel on a 32 x 32 patch of the config-2 set (two launches)."""
+    ``plain``: the plain summation kernel on a 32 x 32 patch of the [64,128,128] sphere set (two launches)."""
     import ctypes
     import torch
     from scwatter_gb300 import _lib, samples
@@ -882,7 +882,7 @@ def probe(kind):
                   ctypes.c_void_p(V.data_ptr()), Z, ctypes.c_void_p(acc.ctypes.data), None, None)
         print(json.dumps({"probe": kind, "n": n, "matrices": Z, "accepted": acc.tolist()}))
     elif kind == "plain":
-        # the plain summation kernel alone: a 32 x 32 xy patch inside one slice of the config-2
+        # the plain summation kernel alone: a 32 x 32 xy patch inside one slice of the [64,128,128]
         # synthetic set (2 MF x 2 MF = 10.24e6 waves per point; 1.05e10 points*modes)
         from scwatter_gb300 import synthetic
         cfg = CFG2
@@ -927,7 +927,7 @@ def main():
     ap.add_argument("--no-solve", action="store_true", help="skip the FP64 solve leg")
     ap.add_argument("--solve-only", action="store_true", help="only the FP64 solve leg (its own JSON line)")
     ap.add_argument("--solved", action="store_true",
-                    help="solve the config-2 sphere sample on the GPU, then time and FP64-check its evaluation")
+                    help="solve the [64,128,128] sphere sample (40 x 40 harmonics) on the GPU, then time and FP64-check its evaluation")
     ap.add_argument("--solved-slices", type=int, default=0, help="with --solved: only the first N slices")
     ap.add_argument("--batch", type=int, default=0, help="batched-graph measurement on the first N uneven samples")
     ap.add_argument("--batch-lanes", type=int, default=0)

@@ -1,7 +1,7 @@
 // Compact factored coefficient file (.cwf): the separable set itself -- per slice the mode
 // amplitudes Q_check / Q_hat (complex64) and the kz of the modes, plus the exterior blocks and
 // the k grids -- instead of the reference's flat list of plane waves (CoupledWaveStructure.h:72-134).
-// At config 2 (MF = 1600, 64 slices) that is 15.7 GB (7.9 GB as a paired set) against the .cw file's ~63 GB, and the
+// At MF = 1600 and 64 slices that is 15.7 GB (7.9 GB as a paired set) against the .cw file's ~63 GB, and the
 // evaluator reads it without re-factoring.  Written and read slice by slice through a pinned
 // staging buffer, so host memory stays at one slice.
 //

@@ -1194,7 +1194,7 @@ scw_status scw_solution_to_cw(scw_solution s, scw_cw* out) {
 
 // Streaming writer of the same .cw file (CoupledWaveStructure.h:72-100 layout): one layer's
 // two slice halves on the host at a time, records written in chunks, so host memory stays
-// O(slice) whatever the file size (about 63 GB at config 2).
+// O(slice) whatever the file size (about 63 GB at MF = 1600, 64 slices).
 scw_status scw_solution_write_cw(scw_solution s, const char* path) {
     if (!s || !path) return fail(SCW_ERR_ARG, "null argument");
     const int MF = s->MF, n = 2 * MF, Z = s->Z, ZL = Z + 1;

@@ -241,7 +241,7 @@ def _cw_layout(path):
 def convert_cw_file(src, dst, rule: int = 0) -> FactoredSet:
     """Factors a volume-solver .cw file into a .cwf file, streaming: the .cw is memory-mapped
     and read one slice's two mode blocks at a time, so host memory stays at one slice however
-    large the file (about 63 GB at config 2).  Returns the set with an empty Q."""
+    large the file (about 63 GB at MF = 1600, 64 slices).  Returns the set with an empty Q."""
     pi_off, npi, layers = _cw_layout(src)
     mm = np.memmap(src, dtype=np.uint8, mode="r")
 

@@ -10,7 +10,7 @@ tira (SolidAnglePolar / SolidAngleMC), which is not part of the reference source
 polar mode places N0 x N1 directions at the midpoints of a (polar angle, azimuth) grid over the
 cap between beta and alpha around the direction, and the montecarlo mode draws directions
 uniformly over that cap (seeded).  Each amplitude is weighted by the cap's solid angle over the
-sample count (the polar weights carry sin(theta)).  These sample sets are this build's own,
+sample count (the polar weights carry sin(theta)).  These sample sets are this package's own,
 not tira's.
 """
 from __future__ import annotations

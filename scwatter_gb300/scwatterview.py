@@ -55,7 +55,7 @@ def main(argv=None) -> int:
         print("the interactive viewer needs a graphics stack, which this machine lacks; use --nogui", file=sys.stderr)
         return 2
     if a.cuda < 0:
-        print("CPU-only evaluation (--cuda -1) is not part of this build", file=sys.stderr)
+        print("CPU-only evaluation (--cuda -1) is not supported: every evaluation runs on the GPU", file=sys.stderr)
         return 2
     import torch
     from . import _lib

@@ -1,4 +1,4 @@
-"""FP64 parity of every evaluator on SOLVED coefficients: the config-1 sphere sample.
+"""FP64 parity of every evaluator on SOLVED coefficients: the [20,64,64] sphere sample (20 x 20 harmonics).
 
 The sphere sample [20, 64, 64] (6 spheres of n = 1.4 + 0.01i, radius 4-12 px), x-polarised
 normal incidence at lambda = 1, 20 x 20 harmonics, solved on the GPU (FP64).  On 8 planes of 4

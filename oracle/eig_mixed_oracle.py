@@ -11,7 +11,8 @@ eigenpairs (LAPACK cgeev through numpy stands in for the FP32 Householder + QR s
   (cluster_eig_kernel); F_ij = E_ij / (lambda_j - lambda_i) between clusters (f_kernel);
   X += X F with an FP32 product (xupdate_kernel); cluster columns rotated by their block's
   eigenvectors (rotate_kernel);
-* stop at tol, accept at tol_accept after the last step, else the FP64 solver.
+* stop at tol; from step ``steps`` on accept at tol_accept; after the last step (``steps``, or
+  ``steps_large`` for matrices of order >= ``large_n``) the FP64 solver.
 
 The reference solves the same eigenproblems with LAPACKE_zgeev (third_Lapack.h:38-47); the
 tests compare the refined eigenvalues with numpy's FP64 LAPACK ones.
@@ -47,8 +48,10 @@ def cluster_eig(M, deg):
     return np.diag(T).copy(), U @ Y
 
 
-def refine(A, lam32, X32, steps=10, tau_rel=1e-5, deg_rel=1e-12, tol=1e-14, tol_accept=1e-12, max_cluster=64):
-    """Returns (accepted, lam, X, residual per check)."""
+def refine(A, lam32, X32, steps=10, tau_rel=1e-5, deg_rel=1e-12, tol=1e-14, tol_accept=1e-12, max_cluster=64,
+           steps_large=16, large_n=1600):
+    """Returns (accepted, lam, X, residual per check).  Matrices of order >= large_n refine for up
+    to steps_large steps; from step ``steps`` on a slice is accepted at tol_accept (eig_mixed.cu)."""
     A = np.asarray(A, np.complex128)
     nA = np.linalg.norm(A, 1)
     lam = np.asarray(lam32).astype(np.complex128)
@@ -63,13 +66,14 @@ def refine(A, lam32, X32, steps=10, tau_rel=1e-5, deg_rel=1e-12, tol=1e-14, tol_
     same = lab[:, None] == lab[None, :]
     single = sizes[lab] == 1
     hist = []
-    for s in range(steps + 1):
+    last = max(steps, steps_large) if A.shape[0] >= large_n else steps
+    for s in range(last + 1):
         R = A @ X - X * lam[None, :]
         res = (np.linalg.norm(R, axis=0) / np.linalg.norm(X, axis=0)).max() / nA
         hist.append(res)
-        if res <= (tol_accept if s == steps else tol):
+        if res <= (tol_accept if s >= steps else tol):
             return True, lam, X, hist
-        if s == steps:
+        if s == last:
             return False, lam, X, hist
         X32s = X.astype(np.complex64)
         # E = X^-1 R by LAPACK's single-precision LU (cgesv).  numpy.linalg.solve would compute

@@ -260,7 +260,7 @@ resid_kernel(const double2* __restrict__ AX, const double2* __restrict__ X, cons
 __global__ void __launch_bounds__(256)
 gate_kernel(int n, const double* __restrict__ rn, const double* __restrict__ xn, const double* __restrict__ anorm,
             double tol, int step, int* __restrict__ state, int* __restrict__ steps, double* __restrict__ res) {
-    // tol: the stopping tolerance at intermediate checks, the acceptance tolerance at the last
+    // tol: the stopping tolerance at early checks, the acceptance tolerance from step `steps` on
     const int b = blockIdx.x;
     if (state[b] != kRefining) return;
     __shared__ double red[256];
@@ -635,14 +635,15 @@ scw_status geev_mixed(cudaStream_t st, double2* A, double2* lam, double2* V, int
     init_kernel<<<dim3(gZ, Z), 256, 0, st>>>(w.lam32, w.S2, lam, V, n, w.qr, w.state, w.steps, w.res);
     cluster_kernel<<<Z, 1024, cl_smem, st>>>(lam, n, w.anorm, prm.tau_rel, w.label, w.member, w.cstart, w.ncl, w.state);
     MX_LAUNCHED(2);
-    for (int s = 0; s <= prm.steps; s++) {
+    const int last = n >= EigMixParams::kLargeN ? std::max(prm.steps, prm.steps_large) : prm.steps;
+    for (int s = 0; s <= last; s++) {
         // residual check (and right-hand side of the correction)
         MX_TRY(gemm<double2>(st, n, n, n, d1, A, n, nn, V, n, nn, d0, AX, n, nn, Z, w.state));
         resid_kernel<<<dim3((n + 31) / 32, Z), 256, 0, st>>>(AX, V, lam, n, w.S3, w.rn, w.xn, w.state);
-        gate_kernel<<<Z, 256, 0, st>>>(n, w.rn, w.xn, w.anorm, s == prm.steps ? prm.tol_accept : prm.tol, s, w.state,
+        gate_kernel<<<Z, 256, 0, st>>>(n, w.rn, w.xn, w.anorm, s >= prm.steps ? prm.tol_accept : prm.tol, s, w.state,
                                        w.steps, w.res);
         MX_LAUNCHED(3);
-        if (s == prm.steps) break;
+        if (s == last) break;
         // E = X^-1 R in FP32
         to32_kernel<<<dim3(gZ, Z), 256, 0, st>>>(V, w.S0, w.S2, n, w.state);
         MX_LAUNCHED(1);

@@ -45,10 +45,14 @@ struct EigMixParams {
     int steps = 10;                 // refinement steps (each begins with the residual check); converged
                                     // slices skip the rest, and a step costs about 1/50 of the FP64 QR
                                     // fallback that a slow slice would otherwise take
+    int steps_large = 16;           // the same for n >= kLargeN: dense spectra there converge linearly
+                                    // (about 3x per step from an FP32 start), so more steps pay
+    static constexpr int kLargeN = 1600;
     double tau_rel = 1e-5;          // cluster threshold relative to ||A||_1
     double deg_rel = 1e-12;         // within a cluster: eigenvalues this close count as equal
     double tol = 1e-14;             // a slice stops refining once its max relative column residual is this small
-    double tol_accept = 1e-12;      // after the last step: accepted at or below this, else the FP64 solver
+    double tol_accept = 1e-12;      // from step `steps` on: accepted at or below this; after the last
+                                    // step, else the FP64 solver
     bool wide = false;              // Hessenberg reductions spread over the GPU (see geev)
 };
 

@@ -643,6 +643,57 @@ def solved_parity(ctx, sol, slices, N=24, pin_every=9):
     return out
 
 
+def grid_leg(ctx, sol, c, Nx=128, Ny=128, Nz=64, reps=3):
+    """The solved [20,64,64] sphere sample evaluated on the full 128 x 128 x 64 grid (x, y over
+    the sample, z over the sample +-10 units) by the separable form (3xTF32 tcgen05) and by the
+    plain summation kernel; their times, points*modes/s and agreement over the whole grid."""
+    import torch
+    from scwatter_gb300 import evaluator as ev
+    from scwatter_gb300 import separable as sp
+    sep = sol.to_sep()
+    kx, ky, zb = sep.grid()
+    x0, y0 = np.float32(-c["size"][0] / 2), np.float32(-c["size"][1] / 2)
+    dx, dy = np.float32(c["size"][0] / (Nx - 1)), np.float32(c["size"][1] / (Ny - 1))
+    z0 = np.float32(zb[0] - 10.0)
+    dz = np.float32((zb[-1] - zb[0] + 20.0) / (Nz - 1))
+    MF = len(kx) * len(ky)
+    zs = (z0 + dz * np.arange(Nz, dtype=np.float32)).astype(np.float32)
+    # waves a point sees: region rule of the GPU evaluator (z >= z_l - 0.001, the last satisfied)
+    Z = len(zb) - 1
+    waves = np.empty(Nz, np.int64)
+    for k, z in enumerate(zs):
+        r = 0
+        for l in range(Z + 1):
+            if z >= zb[l] - 0.001:
+                r = l + 1
+        waves[k] = 2 * MF if r == 0 else (MF if r == Z + 1 else 4 * MF * MF)
+    units = int(Nx * Ny * waves.sum())
+
+    def timed(fn):
+        fn()
+        ctx.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ctx.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts))
+    a = torch.empty((Nz, Ny, Nx, 3), dtype=torch.complex64, device="cuda")
+    b = torch.empty_like(a)
+    t_sep = timed(lambda: sep.eval_volume_device(x0, y0, z0, dx, dy, dz, Nx, Ny, Nz, a.data_ptr(), method=sp.TF32X3))
+    wset = ev.WaveSet.from_cw(ctx, sol.to_cw())
+    t_plain = timed(lambda: wset.eval_volume_device(x0, y0, z0, dx, dy, dz, Nx, Ny, Nz, b.data_ptr()))
+    agree = rel_l2(a.cpu().numpy(), b.cpu().numpy())
+    del wset
+    return {"grid": [Nx, Ny, Nz], "z_range": [float(z0), float(z0 + dz * (Nz - 1))], "points_modes": units,
+            "separable_tf32x3": {"s": t_sep, "points_modes_per_s": units / t_sep},
+            "plain": {"s": t_plain, "points_modes_per_s": units / t_plain},
+            "separable_vs_plain_rel_l2": agree,
+            "note": "wall time around each call with a synchronise (median of 3); FP64 agreement of both "
+                    "evaluators on this solve is in evaluators_vs_fp64_on_this_solve"}
+
+
 def solve_leg(ctx):
     """GPU FP64 solve of the 20-slice sphere sample (samples/s) beside the CPU oracle solve of
     a 2-slice cut of it (the reference's algorithm: 4MF zgeev per slice, explicit inverses),
@@ -664,6 +715,7 @@ def solve_leg(ctx):
                            eig["residual_checks"])
     # every evaluator against FP64 on the solved coefficients (the solved sphere sample, coef 20 x 20)
     parity = solved_parity(ctx, g, slices=(3, 7, 10, 14, 17))
+    grid = grid_leg(ctx, g, c)
     del g
     cut = vol[:CPU_SOLVE_SLICES]
     size_cut = (c["size"][0], c["size"][1], c["size"][2] * CPU_SOLVE_SLICES / c["shape"][0])
@@ -682,6 +734,7 @@ def solve_leg(ctx):
                              "sample": f"first {CPU_SOLVE_SLICES} of the 20 slices, scipy LAPACK (OpenBLAS threads)"},
             "parity": {"x_rel_err_vs_oracle": err, "on": f"the {CPU_SOLVE_SLICES}-slice cut"},
             "evaluators_vs_fp64_on_this_solve": parity,
+            "evaluation_on_the_full_grid": grid,
             "eigen": eig,
             "roofline": {"bound": "fp64", "achieved": 8 * macs / t_gpu / 1e12, "peak": fp64_peak,
                          "unit": "TFLOP/s", "frac": 8 * macs / t_gpu / 1e12 / fp64_peak,

@@ -744,19 +744,25 @@ def solve_leg(ctx):
 
 
 def solved_leg(args):
-    """The sphere sample [64, 128, 128] (40 x 40 harmonics, 64 slices) solved on the GPU
-    (FP64), then its separable set evaluated on the 512 x 512 x 256 grid (time per step) and every
-    evaluator checked against FP64 on 2 x 16 x 16 points in each of 8 slices (4096 points)."""
+    """The sphere sample [64, 128, 128] (40 x 40 harmonics, 64 slices; or, with
+    ``--solved-sample 20x64x64``, the [20, 64, 64] sample at ``--solved-coef`` harmonics per axis)
+    solved on the GPU (FP64), then its separable set evaluated on the 512 x 512 x 256 grid
+    (128 x 128 x 64) (time per step) and every evaluator checked against FP64 on 2 x 16 x 16
+    points in each of 8 slices."""
     import torch
     from scwatter_gb300 import evaluator as ev
     from scwatter_gb300 import samples, solver
     from scwatter_gb300 import separable as sp
-    cfg = CFG2
+    if args.solved_sample == "20x64x64":
+        cfg = dict(M0=args.solved_coef, M1=args.solved_coef, Z=20, size=(64.0, 64.0, 20.0), Nx=128, Ny=128, Nz=64,
+                   x0=-32.0, x1=32.0, y0=-32.0, y1=32.0, shape=(20, 64, 64))
+    else:
+        cfg = dict(CFG2, shape=(CFG2["Z"], 128, 128))
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx = ev.Context(0, stream=stream.cuda_stream)
     Zs = args.solved_slices or cfg["Z"]
-    vol = samples.spheres((cfg["Z"], 128, 128), n_spheres=6, radius=(4.0, 12.0), n_sphere=1.4 + 0.01j, seed=0)[:Zs]
+    vol = samples.spheres(cfg["shape"], n_spheres=6, radius=(4.0, 12.0), n_sphere=1.4 + 0.01j, seed=0)[:Zs]
     size = (cfg["size"][0], cfg["size"][1], cfg["size"][2] * Zs / cfg["Z"])
     t0 = time.perf_counter()
     sol = solver.solve(vol, lam=1.0, direction=(0.0, 0.0, 1.0), ex=(1.0, 0.0), ey=(0.0, 0.0), size=size,
@@ -784,8 +790,9 @@ def solved_leg(args):
     units = Nx * Ny * Nz * 4 * (cfg["M0"] * cfg["M1"]) ** 2
     print(json.dumps({"metric": METRIC, "value": units / float(np.mean(ts)), "unit": UNIT, "n_gpus": 1,
                       "dtype": "c64", "data": "synthetic (seeded sphere sample, solved on the GPU)",
-                      "config": {"workload": f"spheres[{Zs},128,128] (the first {Zs} slices of the [64,128,128] "
-                                             f"sample) coef 40x40, grid {Nx}x{Ny}x{Nz}",
+                      "config": {"workload": f"spheres[{Zs},{cfg['shape'][1]},{cfg['shape'][2]}] (the first {Zs} "
+                                             f"slices of the {list(cfg['shape'])} sample) coef "
+                                             f"{cfg['M0']}x{cfg['M1']}, grid {Nx}x{Ny}x{Nz}",
                                  "form": "separable paired set of the solve, tcgen05 3xTF32"},
                       "ms_per_step": float(np.mean(ts)) * 1e3, "solve_s": t_solve, "eigen": sol.eig,
                       "eigen_slices": {"state": st.tolist(), "steps": steps.tolist(),
@@ -982,6 +989,9 @@ def main():
     ap.add_argument("--solved", action="store_true",
                     help="solve the [64,128,128] sphere sample (40 x 40 harmonics) on the GPU, then time and FP64-check its evaluation")
     ap.add_argument("--solved-slices", type=int, default=0, help="with --solved: only the first N slices")
+    ap.add_argument("--solved-sample", choices=["64x128x128", "20x64x64"], default="64x128x128",
+                    help="with --solved: the sphere sample to solve")
+    ap.add_argument("--solved-coef", type=int, default=40, help="with --solved-sample 20x64x64: harmonics per axis")
     ap.add_argument("--batch", type=int, default=0, help="batched-graph measurement on the first N uneven samples")
     ap.add_argument("--batch-lanes", type=int, default=0)
     ap.add_argument("--batch-method", type=int, default=0)

@@ -291,6 +291,21 @@ __device__ __forceinline__ int producers_any(int v) {
         : "memory");
     return r;
 }
+// named barrier 2 + part among the 4 epilogue warps of a half-tile; the vote form returns the OR
+// of v over them, so their loop decisions stay uniform
+__device__ __forceinline__ void epi_part_sync(int part) {
+    asm volatile("bar.sync %0, 128;" ::"r"(2 + part) : "memory");
+}
+__device__ __forceinline__ int epi_part_any(int v, int part) {
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 q, %1, 0;\n\t"
+        "bar.red.or.pred p, %2, 128, q;\n\tselp.s32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"(v), "r"(2 + part)
+        : "memory");
+    return r;
+}
 constexpr int kWsThreads = (kEpiWarps + kProdWarps + 1) * 32;
 
 template <int kKind>
@@ -569,20 +584,25 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     } else {
         // -------- epilogue (warp w: TMEM lanes 32 (w % 4) .. + 31, rows kEpiRows (w / 4) ..) --------
         // TMEM -> registers (8 rows x 6 floats per lane); the accumulator is released as soon as the
-        // values are in registers.  Rows then go out through the warp's srows staging rows (lane l
-        // at float offset 6 l: 768 contiguous bytes per row), each full row as one bulk copy
-        // (cp.async.bulk shared -> global, issued by lane 0); a ragged or unaligned row is stored
-        // by the warp's lanes instead.
-        float* stage = sOut + warp * srows * 192;
+        // values are in registers.  The four warps of a half-tile (part) then stage their 32 x-values
+        // of each row side by side (warp q at float offset 192 q, lane l at 6 l), so that a row of
+        // the tile is 3 KB contiguous in shared memory as in global memory, and one thread of the
+        // part hands each row to the bulk copy engine (cp.async.bulk shared -> global): 16 copies of
+        // 3 KB per tile.  Tiles whose rows are ragged or not 16-byte aligned are stored by the warps'
+        // lanes.  The part's warps synchronise on named barrier 2 + part (128 threads); the abort
+        // decision is taken by a vote on that barrier, so all four reach the same barriers.
         const int quarter = warp & 3, part = warp >> 2;
+        const bool issuer = quarter == 0 && lane == 0;
+        float* stage = sOut + part * srows * (kM * 6);
         const int xw = x0 + quarter * 32;                  // first x of this warp
         const int nx = min(32, ncols - xw);               // valid x of this warp
+        // every row of this CTA's tiles goes out as one 3 KB copy
+        const bool bulk = x0 + kM <= ncols && (ncols & 1) == 0 && (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
         for (int i = 0; i < n_my; i++) {
-            if (*abort_flag) break;
             const int a = i & 1;
-            bool got = mbar_wait(&acc_full[a], (uint32_t)((i >> 1) & 1));
-            got = __all_sync(0xffffffffu, got);
-            if (!got) {
+            int stop = *abort_flag;
+            if (!stop && !__all_sync(0xffffffffu, mbar_wait(&acc_full[a], (uint32_t)((i >> 1) & 1)))) stop = 1;
+            if (epi_part_any(stop, part)) {
                 *abort_flag = 1;
                 break;
             }
@@ -597,36 +617,39 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             tc_fence_before();
             mbar_arrive(&acc_empty[a]);
             for (int g0 = 0; g0 < kEpiRows; g0 += srows) {
-                // the staging rows are reusable once the bulk copies issued from them have read them
-                if (lane == 0) bulk_wait_read0();
-                __syncwarp();
+                // the staging rows are reusable once the part's earlier bulk copies have read them
+                if (issuer) bulk_wait_read0();
+                epi_part_sync(part);
 #pragma unroll
                 for (int r = 0; r < kEpiRows; r++) {
                     if (r < g0 || r >= g0 + srows) continue;
-                    float2* st = reinterpret_cast<float2*>(stage + (r - g0) * 192);
+                    float2* st = reinterpret_cast<float2*>(stage + (r - g0) * (kM * 6) + quarter * 192);
                     st[3 * lane + 0] = make_float2(__uint_as_float(v[6 * r + 0]), __uint_as_float(v[6 * r + 1]));
                     st[3 * lane + 1] = make_float2(__uint_as_float(v[6 * r + 2]), __uint_as_float(v[6 * r + 3]));
                     st[3 * lane + 2] = make_float2(__uint_as_float(v[6 * r + 4]), __uint_as_float(v[6 * r + 5]));
                 }
                 fence_proxy_async();              // the staged rows visible to the bulk copies
-                __syncwarp();
-                for (int r = g0; r < g0 + srows; r++) {
-                    const int row = r0 + r;
-                    if (row >= nrows || nx <= 0) break;           // warp-uniform
-                    float* dst = out + ((long long)row * ncols + xw) * 6;
-                    const float* src = stage + (r - g0) * 192;
-                    if (nx == 32 && ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0)) {
-                        if (lane == 0) bulk_store(dst, src, 768u);
-                    } else {
+                epi_part_sync(part);
+                if (bulk) {
+                    if (issuer) {
+                        for (int r = g0; r < g0 + srows && r0 + r < nrows; r++)
+                            bulk_store(out + ((long long)(r0 + r) * ncols + x0) * 6, stage + (r - g0) * (kM * 6),
+                                       (uint32_t)(kM * 6 * sizeof(float)));
+                        bulk_commit();
+                    }
+                } else {
+                    for (int r = g0; r < g0 + srows; r++) {
+                        const int row = r0 + r;
+                        if (row >= nrows || nx <= 0) break;       // warp-uniform
+                        float* dst = out + ((long long)row * ncols + xw) * 6;
+                        const float* src = stage + (r - g0) * (kM * 6) + quarter * 192;
                         for (int f = lane; f < nx * 6; f += 32) dst[f] = src[f];
                     }
                 }
-                if (lane == 0) bulk_commit();
-                __syncwarp();
             }
         }
-        // every bulk copy of this warp has written global memory before the kernel ends
-        if (lane == 0) bulk_wait_all();
+        // every bulk copy of this part has written global memory before the kernel ends
+        if (issuer) bulk_wait_all();
         __syncwarp();
     }
     __syncthreads();

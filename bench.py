@@ -836,6 +836,15 @@ def batch_leg(args):
            "max_steps": max(e["max_steps"] for e in eigs), "max_residual": max(e["max_residual"] for e in eigs),
            "items_with_fp64_qr_slices": [[i, 2 * sh[0] * sh[1], sh[2] - e["accepted"]]
                                          for i, (sh, e) in enumerate(zip(shapes, eigs)) if e["accepted"] < sh[2]]}
+    # reason codes of the slices that left the mixed path (2 FP32 QR, 3 cluster above 64,
+    # 4 singular X, 5 cluster Schur, 6 residual above 1e-12 after the last step)
+    reasons = {}
+    for i, (sh, e) in enumerate(zip(shapes, eigs)):
+        if e["mixed"] and e["accepted"] < sh[2]:
+            for code in b.item_eig_slices(i)[0]:
+                if int(code) != 1:
+                    reasons[str(int(code))] = reasons.get(str(int(code)), 0) + 1
+    eig["fp64_qr_reasons"] = reasons
     print(json.dumps({"metric": "samples/s", "value": len(items) / t, "unit": "samples/s", "n_gpus": 1,
                       "steps": len(times), "warmup": args.batch_warmup, "ms_per_step": t * 1e3,
                       "higher_is_better": True,

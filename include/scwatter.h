@@ -372,6 +372,9 @@ SCW_API scw_status scw_batch_item_info(scw_batch b, int i, int* M0, int* M1, int
 /* The mixed eigen-solver's record of item i after a run, as scw_solution_eig_info. */
 SCW_API scw_status scw_batch_item_eig(scw_batch b, int i, int* mixed, int* accepted, int* max_steps,
                                       double* max_residual, int* residual_checks);
+/* Per slice of item i after a run, as scw_solution_eig_slices (n_slices entries each, any may be
+ * NULL); SCW_ERR_STATE when the item's FP64 solver ran for every slice. */
+SCW_API scw_status scw_batch_item_eig_slices(scw_batch b, int i, int* state, int* steps, double* residual);
 /* chosen lanes / method / contraction tile shape (0: default rows per warp, 1: half), graph
  * nodes, kernels per launch, tuning time and its log (quadruples lanes, method, tile shape, ms;
  * n_tune entries, at most 16). */

@@ -71,6 +71,7 @@ _SIGS = {
     "scw_solution_destroy": [P],
     "scw_solution_info": [P, P, P, P, P],
     "scw_solution_eig_slices": [P, P, P, P],
+    "scw_batch_item_eig_slices": [P, I32, P, P, P],
     "scw_solution_eig_info": [P, P, P, P, P, P],
     "scw_solution_get": [P, P, P, P, P],
     "scw_solution_get_modes": [P, I32, P, P],

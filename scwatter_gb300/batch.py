@@ -97,6 +97,14 @@ class Batch:
                 "fell_back": Z - acc.value if mixed.value else Z, "max_steps": steps.value,
                 "max_residual": res.value, "residual_checks": checks.value}
 
+    def item_eig_slices(self, i: int):
+        """Per slice of item ``i`` after a run: (state, steps, residual) as ``Solution.eig_slices``
+        (state 1 = accepted by the mixed path, else the fallback's reason code)."""
+        Z = self.item_info(i)[2]
+        st, steps, res = np.zeros(Z, np.int32), np.zeros(Z, np.int32), np.zeros(Z, np.float64)
+        _lib.call("scw_batch_item_eig_slices", self.handle, int(i), *(ctypes.c_void_p(a.ctypes.data) for a in (st, steps, res)))
+        return st, steps, res
+
     def result(self, i: int):
         """(x [6MF], gamma [Z, 2MF], field [Nz, Ny, Nx, 3] complex64) of item ``i``."""
         M0, M1, Z, _ = self.item_info(i)

@@ -560,6 +560,18 @@ scw_status scw_batch_item_eig(scw_batch b, int i, int* mixed, int* accepted, int
     return SCW_OK;
 }
 
+scw_status scw_batch_item_eig_slices(scw_batch b, int i, int* state, int* steps, double* residual) {
+    if (!b || i < 0 || i >= (int)b->items.size()) return fail(SCW_ERR_ARG, "scw_batch_item_eig_slices: item out of range");
+    const Item& it = b->items[i];
+    if (!it.out.eig) return fail(SCW_ERR_STATE, "scw_batch_item_eig_slices: the FP64 solver ran for every slice");
+    const int Z = it.sp.Z;
+    SCW_ON_DEVICE(b->ctx->device);
+    if (state) SCW_CUDA_TRY(cudaMemcpy(state, it.out.eig, sizeof(int) * Z, cudaMemcpyDeviceToHost));
+    if (steps) SCW_CUDA_TRY(cudaMemcpy(steps, it.out.eig + Z, sizeof(int) * Z, cudaMemcpyDeviceToHost));
+    if (residual) SCW_CUDA_TRY(cudaMemcpy(residual, it.out.eig_res, sizeof(double) * Z, cudaMemcpyDeviceToHost));
+    return SCW_OK;
+}
+
 scw_status scw_batch_info(scw_batch b, int* lanes, int* method, int* ctr_shape, int64_t* graph_nodes, int64_t* kernels,
                           double* tune_ms, double* tune_log, int* n_tune) {
     if (!b) return fail(SCW_ERR_ARG, "null batch");

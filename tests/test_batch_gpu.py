@@ -71,6 +71,8 @@ def test_batch_matches_oracle(ctx, lanes, method):
             x, g, f = b.result(i)
             e = b.item_eig(i)                 # the mixed eigen-solver finished every slice itself
             assert e["mixed"] and e["fell_back"] == 0 and e["max_residual"] <= 1e-12
+            st_s, steps_s, res_s = b.item_eig_slices(i)
+            assert (st_s == 1).all() and res_s.max() == e["max_residual"] and steps_s.max() == e["max_steps"]
             r, cw = _oracle(it)
             assert np.linalg.norm(x - r.x) / np.linalg.norm(r.x) < TOL_X
             W, bb, e, zl = so.unpack(cw)

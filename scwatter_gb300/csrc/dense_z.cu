@@ -575,14 +575,10 @@ __device__ __forceinline__ void rot_cols(typename CT<C>::R c, C s, C& x, C& y) {
 constexpr int kHqrW = 64;
 
 // Givens generator of the chase: FP64 as zlartg; FP32 from two reciprocal square roots (c =
-// |f| / d, s = conj(g) f / (|f| d), r = f d / |f| with d = sqrt(|f|^2 + |g|^2)), each taken to
-// about 1 ulp by one Newton-Raphson step for 1/sqrt(x), y' = y (3 - x y^2) / 2, so that every
-// rotation is unitary to about 1 ulp: the Schur vectors are products of tens of thousands of
-// them at n = 3200, and a few ulp per rotation added up there
-__device__ __forceinline__ float rsqrt_nr(float x) {
-    const float y = rsqrtf(x);
-    return y * fmaf(-0.5f * x * y, y, 1.5f);
-}
+// |f| / d, s = conj(g) f / (|f| d), r = f d / |f| with d = sqrt(|f|^2 + |g|^2)), which keeps
+// the rotation unitary to a few ulp.  (One Newton-Raphson step on each reciprocal square root,
+// unitary to about 1 ulp, was measured on two n = 3200 layers: eigenpair residuals 1.6-2.5x
+// larger and fewer layers accepted by the refinement, so the plain form stays.)
 __device__ __forceinline__ void givens_chase(double2 f, double2 g, double& c, double2& s, double2& r) {
     zlartg(f, g, c, s, r);
 }
@@ -595,13 +591,13 @@ __device__ __forceinline__ void givens_chase(float2 f, float2 g, float& c, float
         return;
     }
     if (ff == 0.0f) {
-        const float ig = rsqrt_nr(gf);
+        const float ig = rsqrtf(gf);
         c = 0.0f;
         s = make_float2(g.x * ig, -g.y * ig);
         r = make_float2(gf * ig, 0.0f);
         return;
     }
-    const float iaf = rsqrt_nr(ff), id = rsqrt_nr(ff + gf);
+    const float iaf = rsqrtf(ff), id = rsqrtf(ff + gf);
     c = ff * iaf * id;
     const float2 fs = make_float2(f.x * iaf, f.y * iaf);
     const float2 t = cmulc(g, fs);

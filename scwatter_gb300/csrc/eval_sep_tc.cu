@@ -404,14 +404,17 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         // (row (r, c) at slot + (3 r + c) * tstr, chunks swizzled; the buffer has slack past the
         // last row, whose values are masked below), one commit group per tile, empty groups past
         // the last tile
+        // row = e / h as (e * hinv) >> 20 with hinv = ceil(2^20 / h): exact for e < 2^11 (n4 = 24 Mk
+        // <= 1920 chunks) and h < 2^9, and it keeps the division off the per-tile copy loop
+        const int h = Mk / 2;                                      // float4 per T row
+        const uint32_t hinv = fast ? ((1u << 20) + (uint32_t)h - 1u) / (uint32_t)h : 0u;
         auto issue_t = [&](int ti) {
             if (ti < n_my) {
                 const int rr0 = ((int)blockIdx.y + ti * (int)gridDim.y) * kRows;
                 const float4* src = reinterpret_cast<const float4*>(T + (long long)rr0 * 3 * Mk);
                 float2* dst = sT + (ti % kTStages) * t_slot;
-                const int h = Mk / 2;                              // float4 per T row
                 for (int e = pt; e < n4; e += kProdWarps * 32) {
-                    const int row = e / h;
+                    const int row = (int)(((uint32_t)e * hinv) >> 20);
                     cp_async16(reinterpret_cast<float4*>(dst + row * tstr) + ((e - row * h) ^ t_swz<kKind>(row)),
                                src + e);
                 }

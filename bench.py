@@ -270,6 +270,25 @@ def hbm_write_peak(torch, nbytes=4 << 30, reps=5):
     return nbytes / best / 1e9
 
 
+def hbm_read_peak(torch, nbytes=4 << 30, reps=5):
+    """Read-only HBM bandwidth of this GPU: torch's sum over an nbytes buffer (larger than L2),
+    best of ``reps`` launches timed with CUDA events on the current stream."""
+    buf = torch.ones(nbytes // 4, dtype=torch.float32, device="cuda")
+    buf.sum()
+    best = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        buf.sum()
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        best = t if best is None else min(best, t)
+    del buf
+    torch.cuda.empty_cache()
+    return nbytes / best / 1e9
+
+
 def link_peaks(torch, nbytes=2 << 30):
     """Pinned host <-> device copy bandwidth of this machine (best of 3 single cudaMemcpyAsync of
     nbytes each way, and both directions at once on two streams)."""
@@ -501,6 +520,7 @@ def run_ours(args):
     contract_gbs = (q_bytes + c_bytes) / (contract_ms / 1e3) / 1e9 if contract_ms > 0 else None
     synth_gbs = out_bytes / (synth_ms / 1e3) / 1e9 if synth_ms > 0 else None
     write_peak = hbm_write_peak(torch)
+    read_peak = hbm_read_peak(torch)
 
     # plain summation on a bounded sample of the same workload: a PLAIN_PATCH^2 xy patch of the
     # grid plane nearest the middle of slice CPU_SLICE, against that slice's 10.24e6 waves
@@ -552,7 +572,11 @@ def run_ours(args):
                              "traffic": (q_bytes + c_bytes) * CONTRACT_TRAFFIC_RATIO,
                              "traffic_source": "ncu DRAM bytes of the 8-slice case (989.5 MB for 984.3 MB "
                                                "algorithmic), scaled by the units of a full launch",
-                             "algorithmic_bytes": q_bytes + c_bytes, "peak_source": peak_src},
+                             "algorithmic_bytes": q_bytes + c_bytes, "peak_source": peak_src,
+                             "read_only_peak": read_peak,
+                             "frac_of_read_only_peak": contract_gbs / read_peak if contract_gbs else None,
+                             "read_only_peak_source": "torch sum over a 4 GiB buffer measured in this run (best "
+                                                      "of 5); the kernel's traffic is reads but for 12.6 MB of C"},
                 "kernels_ms": {k: v[0] for k, v in kt.items()},
                 "synth_roofline": {"bound": "hbm write", "achieved": synth_gbs, "peak": write_peak, "unit": "GB/s",
                                    "frac": synth_gbs / write_peak if synth_gbs else None,

@@ -464,7 +464,7 @@ def run_ours(args):
         # Q bytes this rank uploads per step: the slices its planes lie in
         regions = shard.region_of_z(shard.plane_z(z0, dz, Nz)[k0:k1], fs.z)
         h2d_local = int(len({int(r) for r in regions if 1 <= r <= Z}) * q_bytes // Z)
-        for i in range(max(5, min(args.steps, 7)) + 1):
+        for i in range(9 + 1):
             ctx.synchronize()
             if ws > 1:
                 torch.distributed.barrier()

@@ -241,6 +241,13 @@ __device__ __forceinline__ uint32_t pack1<1>(const __nv_bfloat16* v) {
     return (uint32_t)__bfloat16_as_ushort(v[0]) | ((uint32_t)__bfloat16_as_ushort(v[1]) << 16);
 }
 
+// the negated values of a packed core row: a sign flip per tf32 element or per bf16 half
+template <int kKind>
+__device__ __forceinline__ uint4 neg4(uint4 v) {
+    const uint32_t s = kKind == 0 ? 0x80000000u : 0x80008000u;
+    return make_uint4(v.x ^ s, v.y ^ s, v.z ^ s, v.w ^ s);
+}
+
 template <int kKind>
 __device__ __forceinline__ uint4 pack4(const typename Split<kKind>::T* v);
 
@@ -262,6 +269,7 @@ __device__ __forceinline__ uint4 pack4<1>(const __nv_bfloat16* v) { // 8 bf16 va
 constexpr int kEpiWarps = 8, kProdWarps = 7;      // 16 warps with the MMA warp: 128 registers each
 constexpr int kEpiRows = kRows * 4 / kEpiWarps;     // output rows per epilogue warp and tile (8)
 constexpr int kTStages = 3;                          // staged T tiles in flight (cp.async ring)
+constexpr int kMaxKH = 12;                           // fast producer path: 16-byte core columns per K half
 
 // Staged T rows (float2) in shared memory.  Fast path (Mk a multiple of the elements per core
 // row): a row holds a multiple of 8 16-byte chunks and chunk c of row r sits at c ^ t_swz(r), so
@@ -421,30 +429,35 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             }
             cp_async_commit();
         };
-        // fast path: task = (8-row block nb, row pair nq, core column kc); lanes: nq fastest, then
-        // kc. One task reads 16 bytes x EPC/2 of T row (4 nb + nq) once and writes the Re (n even)
-        // and Im (n odd) rows of B, hi and lo. A task's offsets are the same for every tile, so
-        // they are computed once: t_off[u] = T offset in float2 of the slot (-1: no task), the
-        // first of the task's EPC/2 chunks once swizzled; b_off[u] = B byte offset | T row / 3 << 20
-        // | (order of the task's chunks, XOR) << 24 | (kc odd) << 28 | (first K half) << 29.
-        constexpr int kTasks = (kN / 8 * 22 * 4 + kProdWarps * 32 - 1) / (kProdWarps * 32);
+        // fast path (K has no padding: KC = 2 KH core columns, the second half holding the same T
+        // values as the first): task = (8-row block nb, row pair nq, core column kh of the first
+        // half); lanes: nq fastest, then kh. One task reads 16 bytes x EPC/2 of T row (4 nb + nq)
+        // once, splits its Re and Im parts into hi and lo once, and writes the Re (n even) and Im
+        // (n odd) rows of B in both halves: core column kh gets [Re T, Im T], core column kh + KH
+        // gets [-Im T, Re T] (negation is a sign flip of the split parts, exact). A task's offsets
+        // are the same for every tile, so they are computed once: t_off[u] = T offset in float2 of
+        // the slot (-1: no task), the first of the task's EPC/2 chunks once swizzled; b_off[u] = B
+        // byte offset of core column kh | T row / 3 << 20 | (order of the task's chunks, XOR) << 24
+        // | (kh odd) << 28.  The host admits the fast path for KH <= kMaxKH only.
+        constexpr int kTasks = (kN / 8 * kMaxKH * 4 + kProdWarps * 32 - 1) / (kProdWarps * 32);
+        const int KH = KC / 2;
         int t_off[kTasks];
         uint32_t b_off[kTasks];
 #pragma unroll
         for (int u = 0; u < kTasks; u++) {
             const int tsk = pt + u * kProdWarps * 32;
             const int q = tsk >> 2, nq = tsk & 3;
-            const int nb = q / KC, kc = q - nb * KC;
-            const int trow = 4 * nb + nq, k0 = kc * EPC;
-            const bool live = tsk < (kN / 8) * KC * 4 && k0 < 2 * Mk;
+            const int nb = q / KH, kh = q - nb * KH;
+            const int trow = 4 * nb + nq, k0 = kh * EPC;
+            const bool live = tsk < (kN / 8) * KH * 4 && k0 < Mk;
             constexpr int m = EPC / 2 - 1;                        // chunks of one task - 1
             const int g = t_swz<kKind>(trow);
-            const int c0 = (k0 < Mk ? k0 : k0 - Mk) / 2;          // first chunk of the task in its row
+            const int c0 = k0 / 2;                                // first chunk of the task in its row
             t_off[u] = live ? trow * tstr + 2 * (c0 ^ (g & ~m)) : -1;
-            b_off[u] = ((uint32_t)nb * sbo + (uint32_t)kc * 128u + (uint32_t)(2 * nq) * 16u) |
-                       ((uint32_t)(trow / 3) << 20) | ((uint32_t)(g & m) << 24) | ((uint32_t)(kc & 1) << 28) |
-                       ((uint32_t)(k0 < Mk) << 29);
+            b_off[u] = ((uint32_t)nb * sbo + (uint32_t)kh * 128u + (uint32_t)(2 * nq) * 16u) |
+                       ((uint32_t)(trow / 3) << 20) | ((uint32_t)(g & m) << 24) | ((uint32_t)(kh & 1) << 28);
         }
+        const uint32_t half_off = (uint32_t)KH * 128u;             // core column kh -> kh + KH
         if (fast)
             for (int ti = 0; ti < kTStages - 1; ti++) issue_t(ti);
         // one producer barrier per tile: it publishes tile i's T (this thread's copies are in once
@@ -484,33 +497,39 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
 #pragma unroll
                 for (int u = 0; u < kTasks; u++) {
                     if (t_off[u] < 0) continue;
-                    const bool first = (b_off[u] >> 29) & 1u;
-                    E h0[EPC], l0[EPC], h1[EPC], l1[EPC];
+                    E rh[EPC], rl[EPC], ih[EPC], il[EPC];         // hi / lo of Re T and Im T
 #pragma unroll
                     for (int e2 = 0; e2 < EPC / 2; e2++) {
-                        const float4 t = tv[u][e2];
-                        // s = 0 (Re E): [Re T | -Im T];  s = 1 (Im E): [Im T | Re T]
-                        const float a0 = first ? t.x : -t.y, a1 = first ? t.z : -t.w;
-                        const float b0 = first ? t.y : t.x, b1 = first ? t.w : t.z;
-                        Split<kKind>::split(a0, h0[2 * e2], l0[2 * e2]);
-                        Split<kKind>::split(a1, h0[2 * e2 + 1], l0[2 * e2 + 1]);
-                        Split<kKind>::split(b0, h1[2 * e2], l1[2 * e2]);
-                        Split<kKind>::split(b1, h1[2 * e2 + 1], l1[2 * e2 + 1]);
+                        const float4 t = tv[u][e2];              // (Re, Im) of two T values
+                        Split<kKind>::split(t.x, rh[2 * e2], rl[2 * e2]);
+                        Split<kKind>::split(t.z, rh[2 * e2 + 1], rl[2 * e2 + 1]);
+                        Split<kKind>::split(t.y, ih[2 * e2], il[2 * e2]);
+                        Split<kKind>::split(t.w, ih[2 * e2 + 1], il[2 * e2 + 1]);
                     }
-                    const uint32_t base = b_off[u] & 0xFFFFFu;
-                    const uint4 vh0 = pack4<kKind>(h0), vh1 = pack4<kKind>(h1);
-                    const uint4 vl0 = pack4<kKind>(l0), vl1 = pack4<kKind>(l1);
-                    // the store order alternates with kc so each warp store covers all 8 bank groups
+                    const uint4 vrh = pack4<kKind>(rh), vrl = pack4<kKind>(rl);
+                    const uint4 vih = pack4<kKind>(ih), vil = pack4<kKind>(il);
+                    const uint4 nih = neg4<kKind>(vih), nil = neg4<kKind>(vil);
+                    const uint32_t b1 = b_off[u] & 0xFFFFFu, b2 = b1 + half_off;
+                    // s = 0 (Re E): [Re T | -Im T];  s = 1 (Im E): [Im T | Re T].  The store order
+                    // alternates with kh so each warp store covers all 8 bank groups
                     if (((b_off[u] >> 28) & 1u) == 0) {
-                        *reinterpret_cast<uint4*>(bh + base) = vh0;
-                        *reinterpret_cast<uint4*>(bh + base + 16) = vh1;
-                        *reinterpret_cast<uint4*>(bl + base) = vl0;
-                        *reinterpret_cast<uint4*>(bl + base + 16) = vl1;
+                        *reinterpret_cast<uint4*>(bh + b1) = vrh;
+                        *reinterpret_cast<uint4*>(bh + b1 + 16) = vih;
+                        *reinterpret_cast<uint4*>(bl + b1) = vrl;
+                        *reinterpret_cast<uint4*>(bl + b1 + 16) = vil;
+                        *reinterpret_cast<uint4*>(bh + b2) = nih;
+                        *reinterpret_cast<uint4*>(bh + b2 + 16) = vrh;
+                        *reinterpret_cast<uint4*>(bl + b2) = nil;
+                        *reinterpret_cast<uint4*>(bl + b2 + 16) = vrl;
                     } else {
-                        *reinterpret_cast<uint4*>(bh + base + 16) = vh1;
-                        *reinterpret_cast<uint4*>(bh + base) = vh0;
-                        *reinterpret_cast<uint4*>(bl + base + 16) = vl1;
-                        *reinterpret_cast<uint4*>(bl + base) = vl0;
+                        *reinterpret_cast<uint4*>(bh + b1 + 16) = vih;
+                        *reinterpret_cast<uint4*>(bh + b1) = vrh;
+                        *reinterpret_cast<uint4*>(bl + b1 + 16) = vil;
+                        *reinterpret_cast<uint4*>(bl + b1) = vrl;
+                        *reinterpret_cast<uint4*>(bh + b2 + 16) = vrh;
+                        *reinterpret_cast<uint4*>(bh + b2) = nih;
+                        *reinterpret_cast<uint4*>(bl + b2 + 16) = vrl;
+                        *reinterpret_cast<uint4*>(bl + b2) = nil;
                     }
                 }
             } else {
@@ -680,6 +699,8 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const size_t smem = fixed + (size_t)tc::kEpiWarps * srows * 768;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     if (tc::kAcol + 2 * (size_t)Kp * EB / 4 > tc::kTmemCols) return SCW_ERR_UNSUPPORTED;   // A (hi, lo) in TMEM
+    // the fast producer path covers at most kMaxKH 16-byte core columns per K half
+    if (tc::t_fast(Mk, kind) && (size_t)Kp * EB / 32 > (size_t)tc::kMaxKH) return SCW_ERR_UNSUPPORTED;
     if (!ctx->tc_err) {
         if (cudaMalloc(&ctx->tc_err, sizeof(int)) != cudaSuccess) return fail(SCW_ERR_NOMEM, "cudaMalloc error flag");
     }

@@ -291,3 +291,18 @@ def test_contraction_tile_shapes_bit_identical(ctx, dz, Nz):
         b = _eval_device(ctx, sep, grid, TF32X3)
         sep.set_tiles(0)
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("M0,method", [(44, 2), (48, 2), (48, 3), (80, 3)])
+def test_tensor_core_wide_synthesis_axis(ctx, M0, method):
+    """The widest synthesis axes the tensor-core kernels take (3xTF32 up to 48 harmonics, split-BF16
+    up to 80): every 16-byte core column of the B operand built, against the FP64 oracle."""
+    from scwatter_gb300 import synthetic
+    from scwatter_gb300.separable import SeparableSet
+    fs = synthetic.make_factored(M0=M0, M1=3, Z=2, size=(2.0 * M0, 6.0, 2.0), seed=13)
+    sep = SeparableSet.from_factored(ctx, fs)
+    grid = (np.float32(-M0), np.float32(-2.5), np.float32(-0.9), np.float32(2.0 * M0 / 149), np.float32(1.0),
+            np.float32(0.6), 150, 6, 3)
+    got = _eval_device(ctx, sep, grid, method)
+    ref = _volume_oracle(fs, grid)
+    assert max(rel_l2(got, ref, floor=0.0)) < TOL[method]

@@ -45,8 +45,11 @@ namespace tc {
 constexpr int kM = 128;          // x-values per tile (TMEM lanes)
 constexpr int kRows = 16;        // output rows per tile
 constexpr int kN = kRows * 6;    // 96 accumulator columns per tile
-constexpr uint32_t kTmemCols = 512;     // accumulators at columns 0 and 128, A above kAcol; whole TMEM (1 CTA / SM)
-constexpr uint32_t kAcol = 256;         // first TMEM column of A (hi), then A (lo)
+constexpr uint32_t kTmemCols = 512;     // the whole TMEM (1 CTA / SM)
+// TMEM layout for kXS x tiles per CTA: the two accumulators at columns 0 and acc_col(kXS), then the
+// A tables from a_col(kXS): x tile t's hi at a_col + 2 t acols, its lo acols further
+__host__ __device__ constexpr uint32_t acc_col(int xs) { return xs == 1 ? 128u : 96u; }
+__host__ __device__ constexpr uint32_t a_col(int xs) { return xs == 1 ? 256u : 192u; }
 constexpr long long kSpinLimit = 1ll << 22;   // polls per mbarrier wait before giving up
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -316,7 +319,10 @@ __device__ __forceinline__ int epi_part_any(int v, int part) {
 }
 constexpr int kWsThreads = (kEpiWarps + kProdWarps + 1) * 32;
 
-template <int kKind>
+// kXS x tiles of 128 columns per CTA: the B operand of a row tile, built once by the producers,
+// serves kXS MMA groups (one per x tile, each into its own accumulator), so the producers' work per
+// output byte falls by kXS.  Work unit u = i kXS + t (row tile i, x tile t) uses accumulator u & 1.
+template <int kKind, int kXS>
 __global__ void __launch_bounds__(kWsThreads, 1)
 synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int nrows, int ncols, int Mk, int Kp,
                 int srows, float* __restrict__ out, int* __restrict__ err) {
@@ -348,7 +354,8 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 8);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(bar + 9);
 
-    const int x0 = blockIdx.x * kM;
+    const int x0 = blockIdx.x * kM * kXS;
+    constexpr uint32_t kAccCol = acc_col(kXS), kACol = a_col(kXS);
     const int ntiles = (nrows + kRows - 1) / kRows;
     const int n_my = blockIdx.y < ntiles ? (ntiles - 1 - (int)blockIdx.y) / (int)gridDim.y + 1 : 0;
 
@@ -370,10 +377,13 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     }
     __syncthreads();
     const uint32_t tmem = *tmem_slot;
-    // A: the phase table of this x tile into TMEM, lane x = x0 + 32 w + lane (warps 0-3), 8 columns
-    // per store: tf32 one element per column, bf16 elements 2c (low half) and 2c + 1 per column c
+    // A: the phase tables of the CTA's x tiles into TMEM, lane x = x0 + 128 t + 32 w + lane (warps
+    // 0-3), 8 columns per store: tf32 one element per column, bf16 elements 2c (low half) and 2c + 1
+    // per column c
     if (warp < 4) {
-        const int xg = x0 + warp * 32 + lane;
+      for (int xt = 0; xt < kXS; xt++) {
+        const int xg = x0 + xt * kM + warp * 32 + lane;
+        const uint32_t acol = kACol + 2u * (uint32_t)xt * acols;
         constexpr int EPW = 4 / EB;                           // elements per 32-bit column
         for (uint32_t c0 = 0; c0 < acols; c0 += 8) {
             uint32_t vh[8], vl[8];
@@ -394,9 +404,10 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                 vl[i] = pack1<kKind>(lo);
             }
             const uint32_t lanes = (uint32_t)(warp * 32) << 16;
-            tmem_st8(tmem + lanes + kAcol + c0, vh);
-            tmem_st8(tmem + lanes + kAcol + acols + c0, vl);
+            tmem_st8(tmem + lanes + acol + c0, vh);
+            tmem_st8(tmem + lanes + acol + acols + c0, vl);
         }
+      }
         tmem_st_wait();
     }
     fence_proxy_async();
@@ -576,28 +587,36 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         const int nksteps = (int)(kbytes / 32);
         int issued = 0;
         if (lane == 0) {
-            for (int i = 0; i < n_my; i++) {
+            bool stop = false;
+            for (int i = 0; i < n_my && !stop; i++) {
                 if (*abort_flag) break;
                 const int s = i & 1;
-                if (!mbar_wait(&full_b[s], (uint32_t)((i >> 1) & 1)) ||
-                    (i >= 2 && !mbar_wait(&acc_empty[s], (uint32_t)(((i >> 1) - 1) & 1)))) {
+                if (!mbar_wait(&full_b[s], (uint32_t)((i >> 1) & 1))) {
                     *abort_flag = 1;
                     break;
                 }
-                tc_fence_after();
-                const uint32_t d = tmem + (uint32_t)(s * 128);
-                const uint32_t a_hi = tmem + kAcol, a_lo = tmem + kAcol + acols;
                 const uint32_t b_hi = smem_u32(sB0 + (2 * s) * b_bytes), b_lo = smem_u32(sB0 + (2 * s + 1) * b_bytes);
-                for (int ks = 0; ks < nksteps; ks++) {
-                    const uint32_t ko = (uint32_t)ks * 256u;    // 32 bytes of K = two 16-byte core columns of B
-                    const uint32_t ka = (uint32_t)ks * 8u;      // the same 32 bytes of K = 8 TMEM columns of A
-                    umma_ta<kKind>(d, a_hi + ka, make_desc(b_hi + ko, 128, sbo), idesc, ks > 0);
-                    umma_ta<kKind>(d, a_hi + ka, make_desc(b_lo + ko, 128, sbo), idesc, 1);
-                    umma_ta<kKind>(d, a_lo + ka, make_desc(b_hi + ko, 128, sbo), idesc, 1);
+                for (int xt = 0; xt < kXS; xt++) {
+                    const int u = i * kXS + xt, a = u & 1;
+                    if (u >= 2 && !mbar_wait(&acc_empty[a], (uint32_t)(((u >> 1) - 1) & 1))) {
+                        *abort_flag = 1;
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d = tmem + (uint32_t)a * kAccCol;
+                    const uint32_t a_hi = tmem + kACol + 2u * (uint32_t)xt * acols, a_lo = a_hi + acols;
+                    for (int ks = 0; ks < nksteps; ks++) {
+                        const uint32_t ko = (uint32_t)ks * 256u;    // 32 bytes of K = two 16-byte core columns of B
+                        const uint32_t ka = (uint32_t)ks * 8u;      // the same 32 bytes of K = 8 TMEM columns of A
+                        umma_ta<kKind>(d, a_hi + ka, make_desc(b_hi + ko, 128, sbo), idesc, ks > 0);
+                        umma_ta<kKind>(d, a_hi + ka, make_desc(b_lo + ko, 128, sbo), idesc, 1);
+                        umma_ta<kKind>(d, a_lo + ka, make_desc(b_hi + ko, 128, sbo), idesc, 1);
+                    }
+                    umma_commit(&acc_full[a]);
+                    issued = u + 1;
                 }
-                umma_commit(&empty_b[s]);
-                umma_commit(&acc_full[s]);
-                issued = i + 1;
+                if (!stop) umma_commit(&empty_b[s]);      // B slot s is free once this row tile's MMAs are done
             }
             // the accumulators must be idle before TMEM is freed: wait for the last commit
             if (issued > 0) mbar_wait(&acc_full[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1));
@@ -616,14 +635,16 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         const int quarter = warp & 3, part = warp >> 2;
         const bool issuer = quarter == 0 && lane == 0;
         float* stage = sOut + part * srows * (kM * 6);
-        const int xw = x0 + quarter * 32;                  // first x of this warp
-        const int nx = min(32, ncols - xw);               // valid x of this warp
-        // every row of this CTA's tiles goes out as one 3 KB copy
-        const bool bulk = x0 + kM <= ncols && (ncols & 1) == 0 && (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
-        for (int i = 0; i < n_my; i++) {
-            const int a = i & 1;
+        const bool aligned = (ncols & 1) == 0 && (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
+        for (int u = 0; u < n_my * kXS; u++) {
+            const int a = u & 1, i = u / kXS;
+            const int xs = x0 + (u - i * kXS) * kM;           // first x of this unit's x tile
+            const int xw = xs + quarter * 32;                 // first x of this warp
+            const int nx = min(32, ncols - xw);              // valid x of this warp
+            // every row of a whole, aligned x tile goes out as one 3 KB copy
+            const bool bulk = xs + kM <= ncols && aligned;
             int stop = *abort_flag;
-            if (!stop && !__all_sync(0xffffffffu, mbar_wait(&acc_full[a], (uint32_t)((i >> 1) & 1)))) stop = 1;
+            if (!stop && !__all_sync(0xffffffffu, mbar_wait(&acc_full[a], (uint32_t)((u >> 1) & 1)))) stop = 1;
             if (epi_part_any(stop, part)) {
                 *abort_flag = 1;
                 break;
@@ -631,7 +652,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             tc_fence_after();
             const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows + part * kEpiRows;
             const uint32_t tbase =
-                tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 128) + (uint32_t)(part * kEpiRows * 6);
+                tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)a * kAccCol + (uint32_t)(part * kEpiRows * 6);
             uint32_t v[kEpiRows * 6];
 #pragma unroll
             for (int c16 = 0; c16 < kEpiRows * 6 / 16; c16++) tmem_ld16(tbase + (uint32_t)(16 * c16), &v[16 * c16]);
@@ -655,7 +676,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                 if (bulk) {
                     if (issuer) {
                         for (int r = g0; r < g0 + srows && r0 + r < nrows; r++)
-                            bulk_store(out + ((long long)(r0 + r) * ncols + x0) * 6, stage + (r - g0) * (kM * 6),
+                            bulk_store(out + ((long long)(r0 + r) * ncols + xs) * 6, stage + (r - g0) * (kM * 6),
                                        (uint32_t)(kM * 6 * sizeof(float)));
                         bulk_commit();
                     }
@@ -698,7 +719,11 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     while (srows > 1 && fixed + (size_t)tc::kEpiWarps * srows * 768 > 227 * 1024) srows /= 2;
     const size_t smem = fixed + (size_t)tc::kEpiWarps * srows * 768;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
-    if (tc::kAcol + 2 * (size_t)Kp * EB / 4 > tc::kTmemCols) return SCW_ERR_UNSUPPORTED;   // A (hi, lo) in TMEM
+    const size_t acols = (size_t)Kp * EB / 4;                 // TMEM columns of one A table (hi or lo)
+    if (tc::a_col(1) + 2 * acols > tc::kTmemCols) return SCW_ERR_UNSUPPORTED;   // A (hi, lo) in TMEM
+    // two x tiles per CTA (B shared) where both A tables fit beside the accumulators and the grid
+    // has more than one x tile
+    const int xs = (tc::a_col(2) + 4 * acols <= tc::kTmemCols && ncols > tc::kM) ? 2 : 1;
     // the fast producer path covers at most kMaxKH 16-byte core columns per K half
     if (tc::t_fast(Mk, kind) && (size_t)Kp * EB / 32 > (size_t)tc::kMaxKH) return SCW_ERR_UNSUPPORTED;
     if (!ctx->tc_err) {
@@ -706,21 +731,21 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     }
     // cleared once per synchronisation: a flag raised by an earlier launch stays raised
     if (!ctx->tc_pending_check) SCW_CUDA_TRY(cudaMemsetAsync(ctx->tc_err, 0, sizeof(int), ctx->stream));
-    const int xt = (ncols + tc::kM - 1) / tc::kM;
+    const int xt = (ncols + tc::kM * xs - 1) / (tc::kM * xs);
     const int ntiles = (nrows + tc::kRows - 1) / tc::kRows;
     int yt = std::max(1, ctx->sm_count / xt);
     yt = std::min(yt, ntiles);
     dim3 grid(xt, yt);
     LaunchTimer lt(ctx, kind == 0 ? "synth_tc_kernel<tf32x3>" : "synth_tc_kernel<bf16x3>");
-    if (kind == 0) {
-        SCW_CUDA_TRY(cudaFuncSetAttribute(tc::synth_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        tc::synth_tc_kernel<0><<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, srows, out,
-                                                                             ctx->tc_err);
-    } else {
-        SCW_CUDA_TRY(cudaFuncSetAttribute(tc::synth_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        tc::synth_tc_kernel<1><<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, srows, out,
-                                                                             ctx->tc_err);
-    }
+    auto launch = [&](auto kernel) -> scw_status {
+        SCW_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kernel<<<grid, tc::kWsThreads, smem, ctx->stream>>>(T, F, nrows, ncols, Mk, Kp, srows, out, ctx->tc_err);
+        return SCW_OK;
+    };
+    scw_status ls;
+    if (kind == 0) ls = xs == 2 ? launch(tc::synth_tc_kernel<0, 2>) : launch(tc::synth_tc_kernel<0, 1>);
+    else ls = xs == 2 ? launch(tc::synth_tc_kernel<1, 2>) : launch(tc::synth_tc_kernel<1, 1>);
+    if (ls != SCW_OK) return ls;
     SCW_CUDA_TRY(cudaGetLastError());
     ctx->launches++;
     ctx->tc_pending_check = true;

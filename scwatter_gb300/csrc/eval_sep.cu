@@ -46,11 +46,12 @@ __global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float*
                                  const double* __restrict__ zb, int J, int nks, float2* __restrict__ Phi) {
     const PGroup g = groups[blockIdx.y];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= 2 * J) return;
     const int l = g.region - 1;
-    const int half = j / J, jj = j - half * J;
-    float2* out = Phi + ((long long)blockIdx.y * 2 * J + j) * nks;
     if (!beta) {
+        // two-half set: one thread per (half, mode), j < 2 J
+        if (j >= 2 * J) return;
+        const int half = j / J, jj = j - half * J;
+        float2* out = Phi + ((long long)blockIdx.y * 2 * J + j) * nks;
         const double2 k = kz[((long long)l * 2 + half) * J + jj];
         const double zref = half == 0 ? zb[l] : zb[l + 1];
         for (int kk = 0; kk < nks; kk++) {
@@ -63,19 +64,25 @@ __global__ void sep_phase_kernel(const PGroup* __restrict__ groups, const float*
         }
         return;
     }
+    // paired set: one thread per mode j < J writes both halves from the same two phases
+    if (j >= J) return;
+    const int jj = j;
+    float2* out0 = Phi + ((long long)blockIdx.y * 2 * J + jj) * nks;
+    float2* out1 = Phi + ((long long)blockIdx.y * 2 * J + J + jj) * nks;
     const double2 kd = kz[(long long)l * 2 * J + jj], ku = kz[((long long)l * 2 + 1) * J + jj];
     const double2 bd = beta[(long long)l * 2 * J + jj], bu = beta[((long long)l * 2 + 1) * J + jj];
-    const double su = half == 0 ? 1.0 : -1.0;
     for (int kk = 0; kk < nks; kk++) {
         if (kk < g.nk) {
             const double z = (double)zlist[g.zi[kk]];
             const float2 fd = phase_fp64(kd.x, kd.y, z - zb[l]);
             const float2 fu = phase_fp64(ku.x, ku.y, z - zb[l + 1]);
-            const double re = bd.x * fd.x - bd.y * fd.y + su * (bu.x * fu.x - bu.y * fu.y);
-            const double im = bd.x * fd.y + bd.y * fd.x + su * (bu.x * fu.y + bu.y * fu.x);
-            out[kk] = make_float2((float)re, (float)im);
+            const double dre = bd.x * fd.x - bd.y * fd.y, dim = bd.x * fd.y + bd.y * fd.x;
+            const double ure = bu.x * fu.x - bu.y * fu.y, uim = bu.x * fu.y + bu.y * fu.x;
+            out0[kk] = make_float2((float)(dre + ure), (float)(dim + uim));
+            out1[kk] = make_float2((float)(dre - ure), (float)(dim - uim));
         } else {
-            out[kk] = make_float2(0.f, 0.f);
+            out0[kk] = make_float2(0.f, 0.f);
+            out1[kk] = make_float2(0.f, 0.f);
         }
     }
 }
@@ -276,19 +283,22 @@ __global__ void sep_rows_kernel(const float2* __restrict__ C, const float2* __re
 
 // Stage 2a for a volume: T[k*Ny + j][c][a] = sum_b Ey[b][j] C[k][c][a*M1 + b].
 // One CTA per (z-plane k, block of kRowsBlk rows j): C[k] is staged transposed ([c][b][a],
-// so lanes with consecutive a read consecutive words) with the block's Ey phases.  Each thread
-// computes a kRowsT x 2 block of outputs (rows j, two adjacent columns (c, a)): per harmonic b
-// it loads kRowsT row phases (the same for the warp: broadcast) and one column pair (16 bytes,
-// consecutive across the warp) for 2 kRowsT complex multiply-adds.
+// so lanes with consecutive a read consecutive words) with the block's Ey phases, also
+// transposed ([b][row], 16-byte aligned).  Each thread computes a kRowsT x 2 block of outputs
+// (rows j, two adjacent columns (c, a)): per harmonic b it loads the kRowsT row phases as
+// kRowsT / 2 16-byte words (the same for the warp: broadcast) and two column values
+// (consecutive across the warp) for 2 kRowsT complex multiply-adds.
 constexpr int kRowsBlk = 64;
-constexpr int kRowsT = 4;
+constexpr int kRowsT = 8;
+// float2 offset of the row phases in the kernel's shared memory (16-byte aligned)
+__host__ __device__ inline int rows_phase_off(int M0, int M1) { return (3 * M0 * M1 + 2 + 1) & ~1; }
 
 __global__ void __launch_bounds__(256)
 sep_rows_volume_kernel(const float2* __restrict__ C, const float2* __restrict__ tabY, int Ny, int M0, int M1,
                        float2* __restrict__ T) {
     extern __shared__ float2 sm2[];
     float2* sC = sm2;                              // [3][M1][M0] (+1 pad entry for odd M0)
-    float2* sR = sm2 + 3 * M0 * M1 + 2;            // [kRowsBlk][M1]
+    float2* sR = sm2 + rows_phase_off(M0, M1);     // [M1][kRowsBlk]
     const int k = blockIdx.y;
     const int j0 = blockIdx.x * kRowsBlk;
     const int MF = M0 * M1;
@@ -299,7 +309,7 @@ sep_rows_volume_kernel(const float2* __restrict__ C, const float2* __restrict__ 
     }
     if (threadIdx.x < 2) sC[3 * MF + threadIdx.x] = make_float2(0.f, 0.f);
     for (int e = threadIdx.x; e < kRowsBlk * M1; e += blockDim.x) {
-        const int r = e / M1, b = e % M1;
+        const int b = e / kRowsBlk, r = e % kRowsBlk;
         sR[e] = (j0 + r < Ny) ? tabY[(long long)b * Ny + j0 + r] : make_float2(0.f, 0.f);
     }
     __syncthreads();
@@ -314,15 +324,22 @@ sep_rows_volume_kernel(const float2* __restrict__ C, const float2* __restrict__ 
         const int c0 = col0 / M0, a0 = col0 % M0, c1 = col1 / M0, a1 = col1 % M0;
         const float2* cp0 = sC + c0 * M1 * M0 + a0;
         const float2* cp1 = sC + c1 * M1 * M0 + a1;
-        const float2* rp = sR + r0 * M1;
+        const float4* rp = reinterpret_cast<const float4*>(sR + r0);
         float acc[kRowsT][2][2];
 #pragma unroll
         for (int i = 0; i < kRowsT; i++) acc[i][0][0] = acc[i][0][1] = acc[i][1][0] = acc[i][1][1] = 0.f;
         for (int b = 0; b < M1; b++) {
             const float2 v0 = cp0[b * M0], v1 = cp1[b * M0];
+            float2 rvs[kRowsT];
+#pragma unroll
+            for (int i2 = 0; i2 < kRowsT / 2; i2++) {
+                const float4 w = rp[b * (kRowsBlk / 2) + i2];
+                rvs[2 * i2] = make_float2(w.x, w.y);
+                rvs[2 * i2 + 1] = make_float2(w.z, w.w);
+            }
 #pragma unroll
             for (int i = 0; i < kRowsT; i++) {
-                const float2 rv = rp[i * M1 + b];
+                const float2 rv = rvs[i];
                 acc[i][0][0] = fmaf(rv.x, v0.x, fmaf(-rv.y, v0.y, acc[i][0][0]));
                 acc[i][0][1] = fmaf(rv.x, v0.y, fmaf(rv.y, v0.x, acc[i][0][1]));
                 acc[i][1][0] = fmaf(rv.x, v1.x, fmaf(-rv.y, v1.y, acc[i][1][0]));
@@ -476,7 +493,8 @@ static scw_status stage1_record(scw_sep s, const SepEvalPlan& p, const char* d_d
             const int nks = max_nk <= 1 ? 1 : max_nk <= 2 ? 2 : max_nk <= 4 ? 4 : 8;
             float2* dPhi = (float2*)cursor;
             cursor += align256(groups.size() * 2 * (size_t)J * nks * sizeof(float2));
-            dim3 gp((2 * J + 255) / 256, (unsigned)groups.size());
+            // one thread per (half, mode) for a two-half set, per mode for a paired set
+            dim3 gp(((s->halves == 1 ? J : 2 * J) + 255) / 256, (unsigned)groups.size());
             {
                 LaunchTimer lt(ctx, "sep_phase_kernel");
                 sep_phase_kernel<<<gp, 256, 0, ctx->stream>>>(dg, dz, s->dKz, s->halves == 1 ? s->dBeta : nullptr,
@@ -657,7 +675,7 @@ scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, 
         if ((st = launch_table(ctx, s->dkx, M0, p.a0, p.da, Na, tabA)) != SCW_OK) return st;
         if ((st = launch_table(ctx, s->dky, M1, p.b0, p.db, Nb, tabB)) != SCW_OK) return st;
         {
-            const size_t smem = (size_t)(3 * M0 * M1 + 2 + kRowsBlk * M1) * sizeof(float2);
+            const size_t smem = (size_t)(rows_phase_off(M0, M1) + kRowsBlk * M1) * sizeof(float2);
             SCW_CUDA_TRY(cudaFuncSetAttribute(sep_rows_volume_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem));
             dim3 grid((Nb + kRowsBlk - 1) / kRowsBlk, Nz);

@@ -433,7 +433,8 @@ def run_ours(args):
         t_step = float(tt.item())
     value = units / t_step
 
-    # per-kernel times of one step (CUDA events around each launch, on the launching stream)
+    # per-kernel times of one step (CUDA events around each launch, on the launching stream); with
+    # timing on, the slab evaluation runs its stages in sequence instead of pipelining the chunks
     ctx.set_timing(True)
     flush.fill_(1.0)
     step()
@@ -578,6 +579,9 @@ def run_ours(args):
                              "read_only_peak_source": "torch sum over a 4 GiB buffer measured in this run (best "
                                                       "of 5); the kernel's traffic is reads but for 12.6 MB of C"},
                 "kernels_ms": {k: v[0] for k, v in kt.items()},
+                "kernels_ms_note": "each kernel's device time in one step run with its stages in sequence; "
+                                   "the timed step (value) pipelines chunks of planes: stage 1 of one chunk "
+                                   "beside stage 2 of the previous one",
                 "synth_roofline": {"bound": "hbm write", "achieved": synth_gbs, "peak": write_peak, "unit": "GB/s",
                                    "frac": synth_gbs / write_peak if synth_gbs else None,
                                    "peak_source": "write-only fill of a 4 GiB buffer measured in this run (best of 5)",
@@ -586,6 +590,7 @@ def run_ours(args):
                                    "note": "the kernel writes the 1.61 GB field and reads 0.13 GB of T and "
                                            "the phase tables; the copy peak counts read and write bytes"},
                 "forms": forms,
+                "forms_note": "each form's kernels summed over one step with its stages in sequence",
                 "plain": {"value": plain_v, "unit": UNIT, "ms": plain_ms,
                           "sample": f"{P}x{P} xy patch in slice {CPU_SLICE}, {len(W32)} waves/point",
                           "sm_count": sm_count,

@@ -23,7 +23,6 @@
 
 namespace scw {
 
-constexpr int kPhaseChunk = 256;
 
 // exp(i kz (z - zref)) with the angle reduced in FP64
 __device__ __forceinline__ float2 phase_fp64(double kr, double ki, double dz) {
@@ -654,8 +653,9 @@ static scw_status sep_eval_plan_planes(const scw_sep_s* s, float a0, float b0, f
 scw_status sep_eval_slab(scw_sep s, float x0, float y0, float z0, float dx, float dy, float dz, int Nx, int Ny,
                          int k_begin, int k_end, float* dE, int method);
 
-// Launches of one planned evaluation (no allocation, no host synchronisation).
-scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, char* scratch, float* dE) {
+// Stage 2 of one planned evaluation (tables, row products, output GEMM) on the context stream;
+// scratch laid out as in sep_eval_record (C, T, two tables, then stage 1's work).
+static scw_status stage2_record(scw_sep s, const SepEvalPlan& p, char* scratch, float* dE) {
     scw_ctx ctx = s->ctx;
     const int M0 = s->M0, M1 = s->M1;
     char* cursor = scratch;
@@ -667,8 +667,7 @@ scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, 
     cursor += p.tab_bytes;
     float2* tabB = (float2*)cursor;
     cursor += p.tab_bytes;
-    scw_status st = stage1_record(s, p, d_desc, dC, cursor);
-    if (st != SCW_OK) return st;
+    scw_status st = SCW_OK;
     const int nrows = p.nrows, ncols = p.ncols, Mk = p.Mk, Na = p.Na, Nb = p.Nb, Nz = p.Nz;
     if (p.kind == 0) {
         // F = Ex table [a][x]; R = Ey table [b][y]
@@ -698,6 +697,14 @@ scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, 
         if ((st = launch_rows(ctx, dC, tabB, 1, 1, 1, 0, nrows, 1, M0, M1, dT)) != SCW_OK) return st;
         return sep_synth(ctx, dT, tabA, nrows, ncols, Mk, dE, p.method);
     }
+}
+
+// Launches of one planned evaluation (no allocation, no host synchronisation).
+scw_status sep_eval_record(scw_sep s, const SepEvalPlan& p, const char* d_desc, char* scratch, float* dE) {
+    const size_t head = p.c_bytes + p.t_bytes + 2 * p.tab_bytes;
+    scw_status st = stage1_record(s, p, d_desc, (float2*)scratch, scratch + head);
+    if (st != SCW_OK) return st;
+    return stage2_record(s, p, scratch, dE);
 }
 
 scw_status sep_eval(scw_sep s, int kind, float a0, float b0, float c, float da, float db, float dz, int Na, int Nb,
@@ -852,10 +859,89 @@ scw_status sep_eval_volume_host(scw_sep s, const float2* Qh, float x0, float y0,
     return scw_ctx_synchronize(ctx);
 }
 
+// Planes k_begin .. k_end-1 in kPipeChunks chunks: stage 1 (phases, contraction; HBM reads) of
+// chunk c on the context stream while stage 2 (row products, output GEMM; tensor cores and HBM
+// writes) of chunk c - 1 runs on a high-priority stream, its output GEMM on half the SMs so that
+// the contraction keeps the rest.  Two scratch sets alternate between the chunks.  Every plane is
+// computed exactly as by the one-pass form (its sums do not depend on the grouping or the grid).
+constexpr int kPipeChunks = 4;
+constexpr int kPipeMinPlanes = 32;
+
+static scw_status sep_eval_slab_pipelined(scw_sep s, float x0, float y0, float z0, float dx, float dy, float dz,
+                                          int Nx, int Ny, int k_begin, int k_end, float* dE, int method) {
+    scw_ctx ctx = s->ctx;
+    const int n = k_end - k_begin;
+    const int per = (n + kPipeChunks - 1) / kPipeChunks;
+    std::vector<SepEvalPlan> plans;
+    std::vector<int> kb;
+    for (int a = k_begin; a < k_end; a += per) {
+        plans.emplace_back();
+        kb.push_back(a);
+        scw_status st = sep_eval_plan_planes(s, x0, y0, z0, dx, dy, dz, Nx, Ny, a, std::min(k_end, a + per), method,
+                                             plans.back());
+        if (st != SCW_OK) return st;
+    }
+    const int nc = (int)plans.size();
+    std::vector<size_t> desc_off(nc);
+    size_t desc_total = 0, scratch = 0;
+    for (int c = 0; c < nc; c++) {
+        desc_off[c] = desc_total;
+        desc_total += align256(plans[c].desc_bytes);
+        scratch = std::max(scratch, align256(plans[c].scratch_bytes));
+    }
+    if (!s->hi_stream) {
+        int least = 0, greatest = 0;
+        SCW_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SCW_CUDA_TRY(cudaStreamCreateWithPriority(&s->hi_stream, cudaStreamNonBlocking, greatest));
+    }
+    while (s->pevents.size() < (size_t)(2 * nc + 1)) {
+        cudaEvent_t e;
+        SCW_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        s->pevents.push_back(e);
+    }
+    scw_status st = ctx->sep_scratch.reserve(2 * scratch);
+    if (st != SCW_OK) return st;
+    SCW_CUDA_TRY(cudaEventSynchronize(ctx->desc_done));
+    if ((st = ctx->host_desc.reserve(desc_total)) != SCW_OK) return st;
+    if ((st = ctx->desc.reserve(desc_total)) != SCW_OK) return st;
+    for (int c = 0; c < nc; c++) sep_eval_desc(plans[c], (char*)ctx->host_desc.ptr + desc_off[c]);
+    SCW_CUDA_TRY(cudaMemcpyAsync(ctx->desc.ptr, ctx->host_desc.ptr, desc_total, cudaMemcpyHostToDevice, ctx->stream));
+    SCW_CUDA_TRY(cudaEventRecord(ctx->desc_done, ctx->stream));
+    cudaEvent_t* ev1 = s->pevents.data() + 1;           // stage 1 of chunk c done
+    cudaEvent_t* ev2 = ev1 + nc;                         // stage 2 of chunk c done
+    SCW_CUDA_TRY(cudaEventRecord(s->pevents[0], ctx->stream));
+    SCW_CUDA_TRY(cudaStreamWaitEvent(s->hi_stream, s->pevents[0], 0));
+    const size_t plane_floats = (size_t)Nx * Ny * 6;
+    const cudaStream_t main_stream = ctx->stream;
+    for (int c = 0; c < nc; c++) {
+        const SepEvalPlan& p = plans[c];
+        char* buf = (char*)ctx->sep_scratch.ptr + (size_t)(c & 1) * scratch;
+        if (c >= 2) SCW_CUDA_TRY(cudaStreamWaitEvent(main_stream, ev2[c - 2], 0));
+        const size_t head = p.c_bytes + p.t_bytes + 2 * p.tab_bytes;
+        if ((st = stage1_record(s, p, (const char*)ctx->desc.ptr + desc_off[c], (float2*)buf, buf + head)) != SCW_OK)
+            return st;
+        SCW_CUDA_TRY(cudaEventRecord(ev1[c], main_stream));
+        SCW_CUDA_TRY(cudaStreamWaitEvent(s->hi_stream, ev1[c], 0));
+        // stage 2 on the high-priority stream, its output GEMM on half the SMs
+        ctx->stream = s->hi_stream;
+        ctx->synth_ctas = std::max(1, ctx->sm_count / 2);
+        st = stage2_record(s, p, buf, dE + (size_t)(kb[c] - k_begin) * plane_floats);
+        ctx->stream = main_stream;
+        ctx->synth_ctas = 0;
+        if (st != SCW_OK) return st;
+        SCW_CUDA_TRY(cudaEventRecord(ev2[c], s->hi_stream));
+    }
+    SCW_CUDA_TRY(cudaStreamWaitEvent(main_stream, ev2[nc - 1], 0));
+    return SCW_OK;
+}
+
 scw_status sep_eval_slab(scw_sep s, float x0, float y0, float z0, float dx, float dy, float dz, int Nx, int Ny,
                          int k_begin, int k_end, float* dE, int method) {
     scw_ctx ctx = s->ctx;
     SCW_ON_DEVICE(ctx->device);
+    // per-kernel timing (scw_ctx_set_timing) times the stages in sequence
+    if (k_end - k_begin >= kPipeMinPlanes && ctx->sm_count >= 8 && !ctx->timing)
+        return sep_eval_slab_pipelined(s, x0, y0, z0, dx, dy, dz, Nx, Ny, k_begin, k_end, dE, method);
     SepEvalPlan p;
     scw_status st = sep_eval_plan_planes(s, x0, y0, z0, dx, dy, dz, Nx, Ny, k_begin, k_end, method, p);
     if (st != SCW_OK) return st;
@@ -888,6 +974,8 @@ static void sep_free(scw_sep s) {
     if (s->dBeta) cudaFree(s->dBeta);
     if (s->dslab) cudaFree(s->dslab);
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->pevents) cudaEventDestroy(e);
+    if (s->hi_stream) cudaStreamDestroy(s->hi_stream);
     if (s->up_stream) cudaStreamDestroy(s->up_stream);
     if (s->down_stream) cudaStreamDestroy(s->down_stream);
     delete s;

@@ -733,7 +733,7 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     if (!ctx->tc_pending_check) SCW_CUDA_TRY(cudaMemsetAsync(ctx->tc_err, 0, sizeof(int), ctx->stream));
     const int xt = (ncols + tc::kM * xs - 1) / (tc::kM * xs);
     const int ntiles = (nrows + tc::kRows - 1) / tc::kRows;
-    int yt = std::max(1, ctx->sm_count / xt);
+    int yt = std::max(1, (ctx->synth_ctas > 0 ? ctx->synth_ctas : ctx->sm_count) / xt);
     yt = std::min(yt, ntiles);
     dim3 grid(xt, yt);
     LaunchTimer lt(ctx, kind == 0 ? "synth_tc_kernel<tf32x3>" : "synth_tc_kernel<bf16x3>");

@@ -91,6 +91,7 @@ struct scw_ctx_s {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int sm_count = 0;
+    int synth_ctas = 0;         // > 0: CTAs of the tensor-core output GEMM (a pipelined caller leaves SMs free)
     int64_t launches = 0;
     scw::DevBuf scratch;        // split-K partial sums of the plain evaluator
     scw::DevBuf desc;           // per-call work descriptors

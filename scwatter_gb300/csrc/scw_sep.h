@@ -75,6 +75,10 @@ struct scw_sep_s {
     // host-streamed evaluation (scw_sep_eval_volume_host): copy streams, events, output slabs
     cudaStream_t up_stream = nullptr, down_stream = nullptr;
     std::vector<cudaEvent_t> events;
+    // pipelined device volumes: stage 2 of one chunk of planes on hi_stream (high priority) while
+    // stage 1 of the next runs on the context stream
+    cudaStream_t hi_stream = nullptr;
+    std::vector<cudaEvent_t> pevents;
     void* dslab = nullptr;                 // output slab ring (device)
     size_t slab_bytes = 0;
     size_t chunk_bytes = 0, slab_target = 0;   // scw_sep_set_streaming (0: defaults)

@@ -235,6 +235,10 @@ SCW_API scw_status scw_sep_set_streaming(scw_sep s, int64_t chunk_bytes, int64_t
  * launches of 1, 2, 4, 8 planes per group; 1 = half as many.  Results are bit-identical; the
  * batch autotuner picks it for its items. */
 SCW_API scw_status scw_sep_set_tiles(scw_sep s, int ctr_shape);
+/* Device slabs of >= 32 planes in `chunks` chunks whose stages overlap on two streams (stage 1 of
+ * a chunk beside stage 2 of the previous, its output GEMM on SM count / synth_sm_div SMs);
+ * chunks 0 or 1 (the default): one pass.  Results are bit-identical either way. */
+SCW_API scw_status scw_sep_set_pipeline(scw_sep s, int chunks, int synth_sm_div);
 SCW_API scw_status scw_sep_eval_plane_device(scw_sep s, int axis, float a_start, float b_start, float c,
                                              float d, int N, float* dE, int method);
 SCW_API scw_status scw_sep_gpu_cw_evaluate(scw_sep s, float* E_xy, float* E_xz, float* E_yz,

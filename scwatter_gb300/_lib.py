@@ -119,6 +119,7 @@ _SIGS = {
     "scw_sep_eval_volume_host": [P, P, F32, F32, F32, F32, F32, F32, I32, I32, I32, P, I32],
     "scw_sep_set_streaming": [P, I64, I64],
     "scw_sep_set_tiles": [P, I32],
+    "scw_sep_set_pipeline": [P, I32, I32],
     "scw_sep_eval_slab_device": [P, F32, F32, F32, F32, F32, F32, I32, I32, I32, I32, P, I32],
     "scw_sep_eval_slab_host": [P, P, F32, F32, F32, F32, F32, F32, I32, I32, I32, I32, P, I32],
     "scw_sep_eval_plane_device": [P, I32, F32, F32, F32, F32, I32, P, I32],

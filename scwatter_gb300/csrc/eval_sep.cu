@@ -859,19 +859,19 @@ scw_status sep_eval_volume_host(scw_sep s, const float2* Qh, float x0, float y0,
     return scw_ctx_synchronize(ctx);
 }
 
-// Planes k_begin .. k_end-1 in kPipeChunks chunks: stage 1 (phases, contraction; HBM reads) of
-// chunk c on the context stream while stage 2 (row products, output GEMM; tensor cores and HBM
-// writes) of chunk c - 1 runs on a high-priority stream, its output GEMM on half the SMs so that
-// the contraction keeps the rest.  Two scratch sets alternate between the chunks.  Every plane is
-// computed exactly as by the one-pass form (its sums do not depend on the grouping or the grid).
-constexpr int kPipeChunks = 4;
+// Planes k_begin .. k_end-1 in s->pipe_chunks chunks: stage 1 (phases, contraction; HBM reads)
+// of chunk c on the context stream while stage 2 (row products, output GEMM; tensor cores and HBM
+// writes) of chunk c - 1 runs on a high-priority stream, its output GEMM on sm_count /
+// pipe_synth_div SMs so that the contraction keeps the rest.  Two scratch sets alternate between
+// the chunks.  Every plane is computed exactly as by the one-pass form (its sums do not depend
+// on the grouping or the grid).  Off by default (scw_sep_set_pipeline).
 constexpr int kPipeMinPlanes = 32;
 
 static scw_status sep_eval_slab_pipelined(scw_sep s, float x0, float y0, float z0, float dx, float dy, float dz,
                                           int Nx, int Ny, int k_begin, int k_end, float* dE, int method) {
     scw_ctx ctx = s->ctx;
     const int n = k_end - k_begin;
-    const int per = (n + kPipeChunks - 1) / kPipeChunks;
+    const int per = (n + s->pipe_chunks - 1) / s->pipe_chunks;
     std::vector<SepEvalPlan> plans;
     std::vector<int> kb;
     for (int a = k_begin; a < k_end; a += per) {
@@ -924,7 +924,7 @@ static scw_status sep_eval_slab_pipelined(scw_sep s, float x0, float y0, float z
         SCW_CUDA_TRY(cudaStreamWaitEvent(s->hi_stream, ev1[c], 0));
         // stage 2 on the high-priority stream, its output GEMM on half the SMs
         ctx->stream = s->hi_stream;
-        ctx->synth_ctas = std::max(1, ctx->sm_count / 2);
+        ctx->synth_ctas = std::max(1, ctx->sm_count / std::max(1, s->pipe_synth_div));
         st = stage2_record(s, p, buf, dE + (size_t)(kb[c] - k_begin) * plane_floats);
         ctx->stream = main_stream;
         ctx->synth_ctas = 0;
@@ -940,7 +940,7 @@ scw_status sep_eval_slab(scw_sep s, float x0, float y0, float z0, float dx, floa
     scw_ctx ctx = s->ctx;
     SCW_ON_DEVICE(ctx->device);
     // per-kernel timing (scw_ctx_set_timing) times the stages in sequence
-    if (k_end - k_begin >= kPipeMinPlanes && ctx->sm_count >= 8 && !ctx->timing)
+    if (s->pipe_chunks > 1 && k_end - k_begin >= kPipeMinPlanes && ctx->sm_count >= 8 && !ctx->timing)
         return sep_eval_slab_pipelined(s, x0, y0, z0, dx, dy, dz, Nx, Ny, k_begin, k_end, dE, method);
     SepEvalPlan p;
     scw_status st = sep_eval_plan_planes(s, x0, y0, z0, dx, dy, dz, Nx, Ny, k_begin, k_end, method, p);
@@ -1204,6 +1204,14 @@ scw_status scw_sep_set_streaming(scw_sep s, int64_t chunk_bytes, int64_t slab_by
     if (!s || chunk_bytes < 0 || slab_bytes < 0) return fail(SCW_ERR_ARG, "scw_sep_set_streaming: bad arguments");
     s->chunk_bytes = (size_t)chunk_bytes;
     s->slab_target = (size_t)slab_bytes;
+    return SCW_OK;
+}
+
+scw_status scw_sep_set_pipeline(scw_sep s, int chunks, int synth_sm_div) {
+    if (!s || chunks < 0 || chunks > 64 || synth_sm_div < 1 || synth_sm_div > 16)
+        return fail(SCW_ERR_ARG, "scw_sep_set_pipeline: bad arguments");
+    s->pipe_chunks = chunks;
+    s->pipe_synth_div = synth_sm_div;
     return SCW_OK;
 }
 

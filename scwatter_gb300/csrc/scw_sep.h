@@ -79,6 +79,8 @@ struct scw_sep_s {
     // stage 1 of the next runs on the context stream
     cudaStream_t hi_stream = nullptr;
     std::vector<cudaEvent_t> pevents;
+    int pipe_chunks = 0;                   // chunks of a pipelined slab (0 or 1: one pass)
+    int pipe_synth_div = 2;                // the pipelined output GEMM runs on sm_count / pipe_synth_div SMs
     void* dslab = nullptr;                 // output slab ring (device)
     size_t slab_bytes = 0;
     size_t chunk_bytes = 0, slab_target = 0;   // scw_sep_set_streaming (0: defaults)

@@ -209,6 +209,10 @@ class SeparableSet:
                   ctypes.c_void_p(_host_ptr(out, "out")), int(method))
         return out
 
+    def set_pipeline(self, chunks: int = 0, synth_sm_div: int = 2):
+        """Overlapped stages of device slabs (``scw_sep_set_pipeline``); 0 or 1 chunk: one pass."""
+        _lib.call("scw_sep_set_pipeline", self.handle, int(chunks), int(synth_sm_div))
+
     def set_tiles(self, ctr_shape: int = 0):
         """Contraction tile shape (``scw_sep_set_tiles``): 0 = default rows per warp, 1 = half."""
         _lib.call("scw_sep_set_tiles", self.handle, int(ctr_shape))

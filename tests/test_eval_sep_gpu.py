@@ -310,14 +310,16 @@ def test_tensor_core_wide_synthesis_axis(ctx, M0, method):
 
 @pytest.mark.parametrize("method", [1, 2, 3])
 def test_pipelined_slab_matches_one_pass_volume(ctx, method):
-    """A slab of >= 32 planes is evaluated in chunks whose two stages overlap on two streams (the
-    output GEMM on half the SMs); every plane equals the one-pass volume bit for bit, and so does
-    the slab evaluated with per-kernel timing on (stages in sequence)."""
+    """With the pipeline on (scw_sep_set_pipeline), a slab of >= 32 planes is evaluated in chunks
+    whose two stages overlap on two streams (the output GEMM on half the SMs); every plane equals
+    the one-pass volume bit for bit, and so does the slab evaluated with per-kernel timing on
+    (stages in sequence)."""
     import torch
     from scwatter_gb300 import synthetic
     from scwatter_gb300.separable import SeparableSet
     ps = synthetic.make_paired(M0=8, M1=6, Z=3, size=(16.0, 12.0, 3.0), seed=21)
     sep = SeparableSet.from_paired(ctx, ps)
+    sep.set_pipeline(4, 2)
     x0, y0, z0, dx, dy, dz, Nx, Ny, Nz = (np.float32(-7), np.float32(-6), np.float32(-1.7), np.float32(0.1),
                                           np.float32(0.2), np.float32(0.05), 200, 64, 70)
     vol = _eval_device(ctx, sep, (x0, y0, z0, dx, dy, dz, Nx, Ny, Nz), method)

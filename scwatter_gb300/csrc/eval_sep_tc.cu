@@ -223,8 +223,8 @@ __device__ __forceinline__ void bulk_store(void* gdst, const void* ssrc, uint32_
                  : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// all but the newest of this thread's committed bulk copy groups have finished reading shared memory
-__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+// this thread's committed bulk copies have finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 // ... and have finished writing global memory
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
@@ -344,9 +344,9 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
     // fast producer path: Mk a multiple of the elements per core row, swizzled T rows
     const bool fast = t_fast(Mk, kKind);
     const int tstr = t_row_stride(Mk, kKind);
-    // output staging: two slots of srows rows of 32 x-values x 6 floats (768 bytes) per epilogue warp
+    // output staging: srows rows of 32 x-values x 6 floats (768 bytes) per epilogue warp
     float* sOut = reinterpret_cast<float*>(sT + kTStages * t_slot);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sOut + kEpiWarps * 2 * srows * 192);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sOut + kEpiWarps * srows * 192);
     uint64_t* full_b = bar;          // [2] producers -> MMA
     uint64_t* empty_b = bar + 2;     // [2] MMA completion -> producers
     uint64_t* acc_full = bar + 4;    // [2] MMA completion -> epilogue
@@ -634,8 +634,7 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
         // decision is taken by a vote on that barrier, so all four reach the same barriers.
         const int quarter = warp & 3, part = warp >> 2;
         const bool issuer = quarter == 0 && lane == 0;
-        float* stage_part = sOut + part * 2 * srows * (kM * 6);   // two slots of srows 3 KB rows
-        int groups_done = 0;                                          // this part's staging groups so far
+        float* stage = sOut + part * srows * (kM * 6);
         const bool aligned = (ncols & 1) == 0 && (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
         for (int u = 0; u < n_my * kXS; u++) {
             const int a = u & 1, i = u / kXS;
@@ -661,11 +660,8 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             tc_fence_before();
             mbar_arrive(&acc_empty[a]);
             for (int g0 = 0; g0 < kEpiRows; g0 += srows) {
-                // slot g & 1 is reusable once the copies of group g - 2 have read it (those of g - 1,
-                // from the other slot, may still be running)
-                float* stage = stage_part + (groups_done & 1) * srows * (kM * 6);
-                groups_done++;
-                if (issuer) bulk_wait_read1();
+                // the staging rows are reusable once the part's earlier bulk copies have read them
+                if (issuer) bulk_wait_read0();
                 epi_part_sync(part);
 #pragma unroll
                 for (int r = 0; r < kEpiRows; r++) {
@@ -717,12 +713,11 @@ scw_status sep_synth_tc(scw_ctx ctx, const float2* T, const float2* F, int nrows
     const int Kp = (2 * Mk + kalign - 1) / kalign * kalign;
     const size_t sbo = (size_t)Kp * EB / 16 * 128;
     const size_t t_tile_bytes = ((size_t)tc::kRows * 3 * tc::t_row_stride(Mk, kind) * 8 + 127) / 128 * 128;
-    // output staging per epilogue warp: two slots of srows rows, 4 (two bulk groups per tile and
-    // part) when shared memory allows
+    // output staging rows per epilogue warp: 8 (one bulk group per tile) when shared memory allows
     const size_t fixed = (tc::kN / 8) * sbo * 4 + tc::kTStages * t_tile_bytes + 128;
-    int srows = tc::kEpiRows / 2;
-    while (srows > 1 && fixed + (size_t)tc::kEpiWarps * 2 * srows * 768 > 227 * 1024) srows /= 2;
-    const size_t smem = fixed + (size_t)tc::kEpiWarps * 2 * srows * 768;
+    int srows = tc::kEpiRows;
+    while (srows > 1 && fixed + (size_t)tc::kEpiWarps * srows * 768 > 227 * 1024) srows /= 2;
+    const size_t smem = fixed + (size_t)tc::kEpiWarps * srows * 768;
     if (smem > 227 * 1024) return SCW_ERR_UNSUPPORTED;
     const size_t acols = (size_t)Kp * EB / 4;                 // TMEM columns of one A table (hi or lo)
     if (tc::a_col(1) + 2 * acols > tc::kTmemCols) return SCW_ERR_UNSUPPORTED;   // A (hi, lo) in TMEM

@@ -645,11 +645,14 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             const bool bulk = xs + kM <= ncols && aligned;
             int stop = *abort_flag;
             if (!stop && !__all_sync(0xffffffffu, mbar_wait(&acc_full[a], (uint32_t)((u >> 1) & 1)))) stop = 1;
+            if (epi_part_any(stop, part)) {
+                *abort_flag = 1;
+                break;
+            }
             tc_fence_after();
             const int r0 = ((int)blockIdx.y + i * (int)gridDim.y) * kRows + part * kEpiRows;
             const uint32_t tbase =
                 tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)a * kAccCol + (uint32_t)(part * kEpiRows * 6);
-            // (after a failed wait the values read are not used: the vote below ends the loop)
             uint32_t v[kEpiRows * 6];
 #pragma unroll
             for (int c16 = 0; c16 < kEpiRows * 6 / 16; c16++) tmem_ld16(tbase + (uint32_t)(16 * c16), &v[16 * c16]);
@@ -657,18 +660,9 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
             tc_fence_before();
             mbar_arrive(&acc_empty[a]);
             for (int g0 = 0; g0 < kEpiRows; g0 += srows) {
-                // the staging rows are reusable once the part's earlier bulk copies have read them;
-                // the first group's barrier is also the part's abort vote
+                // the staging rows are reusable once the part's earlier bulk copies have read them
                 if (issuer) bulk_wait_read0();
-                if (g0 == 0) {
-                    if (epi_part_any(stop, part)) {
-                        *abort_flag = 1;
-                        stop = 1;
-                        break;
-                    }
-                } else {
-                    epi_part_sync(part);
-                }
+                epi_part_sync(part);
 #pragma unroll
                 for (int r = 0; r < kEpiRows; r++) {
                     if (r < g0 || r >= g0 + srows) continue;
@@ -696,7 +690,6 @@ synth_tc_kernel(const float2* __restrict__ T, const float2* __restrict__ F, int 
                     }
                 }
             }
-            if (stop) break;                      // the part's vote ended this unit: all four warps leave
         }
         // every bulk copy of this part has written global memory before the kernel ends
         if (issuer) bulk_wait_all();

@@ -922,7 +922,7 @@ def warm_leg(args):
     import torch
     from scwatter_gb300 import evaluator as ev
     from scwatter_gb300 import samples
-    from scwatter_gb300.warmstart import WarmStart, layer_problems, plain_eig, sorted_desc, warm_eig
+    from scwatter_gb300.warmstart import WarmStart, layer_problems, mixed_eig, plain_eig, sorted_desc, warm_eig
     ctx = ev.Context(0)
     M, Z = args.warm_coef, 32
     def problems(seed0, count):
@@ -954,6 +954,17 @@ def warm_leg(args):
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
     truth = sorted_desc(W0.cpu().numpy())
+    # the production eigen-solver on the same layers: what a warm start has to beat
+    mixed_eig(ctx, PQ[:1])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Wm, _, acc_mixed = mixed_eig(ctx, PQ)
+    torch.cuda.synchronize()
+    t_mixed = time.perf_counter() - t0
+    wm = Wm.cpu().numpy()
+    # eigenvalues as sets: each plain eigenvalue's distance to the nearest mixed one, per layer
+    mixed_dev = max(float(np.abs(truth[l][:, None] - wm[l][None, :]).min(axis=1).max() / np.abs(truth[l]).max())
+                    for l in range(len(wm)))
     t0 = time.perf_counter()
     pred = ws.predict(coef, base)
     _, _, acc, st = warm_eig(ctx, PQ, torch.from_numpy(pred).cuda(), modes)
@@ -971,7 +982,9 @@ def warm_leg(args):
                       "n_gpus": 1, "higher_is_better": True, "dtype": "c128", "data": "synthetic",
                       "config": {"workload": f"GRF layers, coef {M}x{M} (reduced {2 * MF}x{2 * MF}), {Z} layers "
                                              f"per sample, {args.warm} held-out samples, {args.warm_train} training"},
-                      "plain": {"layers_per_s": layers / t_plain, "s": t_plain},
+                      "plain": {"layers_per_s": layers / t_plain, "s": t_plain, "solver": "FP64 QR (scw_zgeev)"},
+                      "mixed": {"layers_per_s": layers / t_mixed, "s": t_mixed, "refined": int((acc_mixed == 1).sum()),
+                                "solver": "scw_zgeev_mixed", "max_eigenvalue_deviation_vs_plain": mixed_dev},
                       "warm": {"layers_per_s": layers / t_warm, "s": t_warm, "accepted": int(acc.sum()),
                                "stats": st},
                       "without_network": {"accepted": int(acc_b.sum()), "stats": st_b},

@@ -263,8 +263,9 @@ SCW_API scw_status scw_zgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int 
 /* Same contract as scw_zgeev (n <= 4096), computed by the mixed-precision solver: FP32
  * Householder + QR + triangular eigenvectors, then Newton refinement of all eigenpairs with FP64
  * residuals (clusters of close eigenvalues solved as small FP64 Schur problems).  Refinement stops
- * once max_i ||A x_i - lambda_i x_i|| / (||A||_1 ||x_i||) <= 1e-14; a matrix still above 1e-12
- * after 10 steps is solved by the FP64 QR solver instead (and only then overwritten).  Optional per-matrix
+ * once max_i ||A x_i - lambda_i x_i|| / (||A||_1 ||x_i||) <= 1e-14; a matrix at or below 1e-12 from
+ * step 10 on is accepted, and one still above 1e-12 after 10 steps (16 for n >= 1600) is solved by
+ * the FP64 QR solver instead (and only then overwritten).  Optional per-matrix
  * outputs: accepted_host (1 = refined result; else why the FP64 solver took it: 2 FP32 QR not
  * converged, 3 a cluster above 64 eigenvalues, 4 singular FP32 eigenvector matrix, 5 a cluster's
  * small Schur solve not converged, 6 residual above 1e-12 after the last step), steps_host

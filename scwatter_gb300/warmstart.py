@@ -89,6 +89,23 @@ def plain_eig(ctx: Context, PQ):
     return W, V
 
 
+def mixed_eig(ctx: Context, PQ):
+    """Eigenpairs of every matrix of the device batch by the mixed-precision solver
+    (scw_zgeev_mixed: FP32 factorisation, FP64 Newton refinement, FP64 QR for matrices it does not
+    accept; copy kept).  Returns (W, V, accepted) with accepted[z] = 1 where the refined result
+    was kept."""
+    import torch
+    A = PQ.clone()
+    Z, n, _ = A.shape
+    W = torch.zeros((Z, n), dtype=torch.complex128, device="cuda")
+    V = torch.zeros((Z, n, n), dtype=torch.complex128, device="cuda")
+    acc = np.zeros(Z, np.int32)
+    torch.cuda.synchronize()
+    _lib.call("scw_zgeev_mixed", ctx.handle, n, _p(A), _p(W), _p(V), Z, ctypes.c_void_p(acc.ctypes.data), None,
+              None)
+    return W, V, acc
+
+
 def warm_eig(ctx: Context, PQ, shifts, modes=None, max_it=12, tol=1e-11):
     """scw_eig_warm on the device batch PQ with device shifts [Z, n] complex128 and optional
     proposed modes [Z, n] (host ints: the start vector of each eigenpair)."""

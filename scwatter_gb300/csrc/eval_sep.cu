@@ -981,10 +981,6 @@ static void sep_free(scw_sep s) {
     delete s;
 }
 
-extern "C" {
-
-}  // extern "C"
-
 static scw_status sep_create(scw_ctx ctx, int M0, int M1, int n_slices, int modes_per_half, const double* kx,
                              const double* ky, const double* z_boundaries, int halves, scw_sep* out) {
     if (!ctx || !out || M0 <= 0 || M1 <= 0 || n_slices < 0 || modes_per_half < 0 || !kx || !ky || !z_boundaries)

@@ -89,9 +89,12 @@ extern "C" scw_status scw_measure_peaks(scw_ctx ctx, double* sincos_ops_per_s, d
     const int blocks = ctx->sm_count * 8;
     void* out = nullptr;
     SCW_CUDA_TRY(cudaMalloc(&out, sizeof(double) * blocks));
-    cudaEvent_t a, b;
-    SCW_CUDA_TRY(cudaEventCreate(&a));
-    SCW_CUDA_TRY(cudaEventCreate(&b));
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        if (a) cudaEventDestroy(a);
+        cudaFree(out);
+        return fail(SCW_ERR_CUDA, "scw_measure_peaks: event creation");
+    }
     auto run = [&](int which, int iters, double ops_per_iter_thread, double* result) -> scw_status {
         for (int rep = 0; rep < 2; rep++) {      // the first launch warms up; the second is timed
             SCW_CUDA_TRY(cudaEventRecord(a, ctx->stream));

@@ -129,6 +129,7 @@ _SIGS = {
     "scw_zgeev": [P, I32, P, P, P, I32, P],
     "scw_zgeev_mixed": [P, I32, P, P, P, I32, P, P, P],
     "scw_cgeev": [P, I32, P, P, P, I32, P],
+    "scw_set_qr_cluster": [I32],
 }
 
 

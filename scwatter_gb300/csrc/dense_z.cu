@@ -13,8 +13,11 @@
 // sequential ones (Hessenberg reduction, QR sweeps) run one CTA per matrix and are batched over
 // the slices of a sample.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <vector>
+
+#include <cooperative_groups.h>
 
 #include "scw_dense.h"
 #include "scw_complex.cuh"
@@ -606,9 +609,11 @@ __device__ __forceinline__ void givens_chase(float2 f, float2 g, float& c, float
     r = make_float2(fs.x * d, fs.y * d);
 }
 
-template <typename C>
-__device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, int ihi, int k0, int k1, C shift,
-                          C* hw, typename CT<C>::R* hc, C* hs) {
+// The chase of rotations k0 .. k1-1 inside the shared-memory window (loaded from H, a block
+// barrier, the chase by warp 0, a block barrier, stored back), the rotations recorded in hc / hs.
+template <typename C, bool kCg>
+__device__ void hqr_chase(C* __restrict__ H, int n, int l, int ihi, int k0, int k1, C shift, C* hw,
+                          typename CT<C>::R* hc, C* hs) {
     using R = typename CT<C>::R;
     constexpr int ldw = kHqrW + 2;
     const int r1 = min(k1 + 1, ihi);
@@ -616,7 +621,7 @@ __device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, in
     const int nr = r1 - k0 + 1, nc = k1 - c0 + 1;
     for (int e = threadIdx.x; e < nr * nc; e += blockDim.x) {
         const int i = e / nc, j = e % nc;
-        hw[i * ldw + j] = H[(long long)(k0 + i) * n + c0 + j];
+        hw[i * ldw + j] = hld<kCg>(H + (long long)(k0 + i) * n + c0 + j);
     }
     __syncthreads();
 #define HW(i, j) hw[((i) - k0) * ldw + ((j) - c0)]
@@ -656,13 +661,21 @@ __device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, in
         H[(long long)(k0 + i) * n + c0 + j] = hw[i * ldw + j];
     }
 #undef HW
-    // Each task streams one stripe of k1 - k0 + 1 values.  The values are loaded kStripe at a
-    // time into registers before the rotations run through them: a load-rotate-store chain
-    // per element would wait a full memory latency per element (the compiler cannot move a
-    // load of the stripe above the store to the element before it).
+}
+
+// The recorded rotations applied, in order, to what lies outside the window: tasks t0, t0 + dt,
+// ... of the stripes (columns right of the window, rows above it, Schur-vector rows).  Each task
+// streams one stripe of k1 - k0 + 1 values.  The values are loaded kStripe at a time into
+// registers before the rotations run through them: a load-rotate-store chain per element would
+// wait a full memory latency per element (the compiler cannot move a load of the stripe above the
+// store to the element before it).
+template <typename C, bool kCg>
+__device__ void hqr_apply(C* __restrict__ H, C* __restrict__ Z, int n, int k0, int k1, const typename CT<C>::R* hc,
+                          const C* hs, int t0, int dt) {
+    using R = typename CT<C>::R;
     constexpr int kStripe = sizeof(R) == sizeof(float) ? 16 : 4;
     const int nright = n - 1 - k1, nabove = k0;
-    for (int t = threadIdx.x; t < nright + nabove + n; t += blockDim.x) {
+    for (int t = t0; t < nright + nabove + n; t += dt) {
         const bool right = t < nright;              // column j (rows k0..k1), else a row (columns k0..k1)
         C* base;
         long long step;
@@ -673,13 +686,13 @@ __device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, in
             base = (t < nright + nabove) ? H + (long long)(t - nright) * n : Z + (long long)(t - nright - nabove) * n;
             step = 1;
         }
-        C x = base[(long long)k0 * step];
+        C x = hld<kCg>(base + (long long)k0 * step);
         for (int kb = k0; kb < k1; kb += kStripe) {
             const int m = min(kStripe, k1 - kb);
             C y[kStripe];
 #pragma unroll
             for (int q = 0; q < kStripe; q++)
-                if (q < m) y[q] = base[(long long)(kb + q + 1) * step];
+                if (q < m) y[q] = hld<kCg>(base + (long long)(kb + q + 1) * step);
 #pragma unroll
             for (int q = 0; q < kStripe; q++) {
                 if (q < m) {
@@ -694,7 +707,39 @@ __device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, in
         }
         base[(long long)k1 * step] = x;
     }
+}
+
+template <typename C>
+__device__ void hqr_chunk(C* __restrict__ H, C* __restrict__ Z, int n, int l, int ihi, int k0, int k1, C shift,
+                          C* hw, typename CT<C>::R* hc, C* hs) {
+    hqr_chase<C, false>(H, n, l, ihi, k0, k1, shift, hw, hc, hs);
+    hqr_apply<C, false>(H, Z, n, k0, k1, hc, hs, threadIdx.x, blockDim.x);
     __syncthreads();
+}
+
+// Shift of the next sweep over [l, ihi]: Wilkinson's from the trailing 2 x 2 block, and
+// exceptional shifts every 10 iterations without a deflation (zlahqr's KEXSH rule).
+template <typename C, bool kCg>
+__device__ C hqr_shift(const C* __restrict__ H, int n, int l, int ihi, int its) {
+    using R = typename CT<C>::R;
+    const C hii = hld<kCg>(H + (long long)ihi * n + ihi);
+    if (its % 20 == 0) return CT<C>::mk(R(0.75) * r_abs(hld<kCg>(H + (long long)ihi * n + ihi - 1).x) + hii.x, hii.y);
+    if (its % 10 == 0) {
+        const C hll = hld<kCg>(H + (long long)l * n + l);
+        return CT<C>::mk(R(0.75) * r_abs(hld<kCg>(H + (long long)(l + 1) * n + l).x) + hll.x, hll.y);
+    }
+    const C a = hld<kCg>(H + (long long)(ihi - 1) * n + ihi - 1);
+    const C b = hld<kCg>(H + (long long)(ihi - 1) * n + ihi);
+    const C c = hld<kCg>(H + (long long)ihi * n + ihi - 1);
+    const C d = hii;
+    const C half = CT<C>::mk(R(0.5) * (a.x - d.x), R(0.5) * (a.y - d.y));
+    const C bc = cmul(b, c);
+    const C disc = cfma(half, half, bc);
+    const C sq = zsqrt(disc);
+    // choose the root that makes the shift closer to d
+    C e1 = cadd(half, sq), e2 = csub(half, sq);
+    const C den = cabs2(e1) >= cabs2(e2) ? e1 : e2;
+    return (cabs2(den) == 0) ? d : csub(d, cdiv(bc, den));
 }
 
 template <typename C>
@@ -753,31 +798,7 @@ hqr_kernel(C* __restrict__ H, C* __restrict__ Z, int n, long long sA, C* __restr
         its++;
         total++;
         // shift; exceptional shifts every 10 iterations without a deflation (zlahqr's KEXSH rule)
-        if (threadIdx.x == 0) {
-            C t;
-            const C hii = H[(long long)ihi * n + ihi];
-            if (its % 20 == 0) {
-                t = CT<C>::mk(R(0.75) * r_abs(H[(long long)ihi * n + ihi - 1].x) + hii.x, hii.y);
-            } else if (its % 10 == 0) {
-                t = CT<C>::mk(R(0.75) * r_abs(H[(long long)(l + 1) * n + l].x) + H[(long long)l * n + l].x,
-                              H[(long long)l * n + l].y);
-            } else {
-                // Wilkinson shift from the trailing 2x2 block
-                const C a = H[(long long)(ihi - 1) * n + ihi - 1];
-                const C b = H[(long long)(ihi - 1) * n + ihi];
-                const C c = H[(long long)ihi * n + ihi - 1];
-                const C d = hii;
-                const C half = CT<C>::mk(R(0.5) * (a.x - d.x), R(0.5) * (a.y - d.y));
-                const C bc = cmul(b, c);
-                const C disc = cfma(half, half, bc);
-                const C sq = zsqrt(disc);
-                // choose the root that makes the shift closer to d
-                C e1 = cadd(half, sq), e2 = csub(half, sq);
-                const C den = cabs2(e1) >= cabs2(e2) ? e1 : e2;
-                t = (cabs2(den) == 0) ? d : csub(d, cdiv(bc, den));
-            }
-            s_s = t;                                      // reuse as shift storage
-        }
+        if (threadIdx.x == 0) s_s = hqr_shift<C, false>(H, n, l, ihi, its);
         __syncthreads();
         const C shift = s_s;
         __syncthreads();
@@ -785,6 +806,119 @@ hqr_kernel(C* __restrict__ H, C* __restrict__ Z, int n, long long sA, C* __restr
         for (int k0 = l; k0 < ihi; k0 += kHqrW) {
             const int k1 = min(k0 + kHqrW, ihi);
             hqr_chunk(H, Z, n, l, ihi, k0, k1, shift, hw, hc, hs);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// The same QR with each matrix on a thread-block cluster of K CTAs (K = the cluster size, 2..8):
+// rank 0 makes every decision (deflations, shift, end) and chases each window as hqr_kernel does;
+// after a cluster barrier every CTA copies the window's rotations from rank 0's shared memory and
+// applies them to its share of the stripes (task t to CTA t / blockDim mod K), then a second
+// barrier.  The CTAs follow the decisions rank 0 leaves in its shared memory before a barrier,
+// so all of them pass the same sequence of barriers and leave together.  H and Z are read through
+// L2 only (other CTAs of the cluster write them) and every thread fences its writes before a
+// barrier.  Each element sees the same operations in the same order as in hqr_kernel, so the
+// results are the same bit for bit; the deferred updates, 72-80 % of a sweep on one CTA (and
+// nearly all of it in FP64, whose rate per SM is low), are spread over K SMs.
+// ------------------------------------------------------------------------------------
+template <typename C>
+__global__ void __launch_bounds__(1024)
+hqr_cluster_kernel(C* __restrict__ H, C* __restrict__ Z, int n, long long sA, C* __restrict__ eig,
+                   int* __restrict__ status, const int* __restrict__ skip) {
+    using R = typename CT<C>::R;
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int K = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int b = blockIdx.x / K;
+    if (skipped(skip, b)) return;                       // the whole cluster, before any barrier
+    H += sA * b;
+    Z += sA * b;
+    eig += (long long)n * b;
+    __shared__ C s_shift;
+    __shared__ int s_red[32];
+    __shared__ int s_cmd[3];                            // rank 0: operation (0 sweep, 1 end), l, ihi
+    extern __shared__ __align__(16) unsigned char hqr_smem[];
+    C* hw = reinterpret_cast<C*>(hqr_smem);
+    C* hs = hw + (kHqrW + 2) * (kHqrW + 2);
+    R* hc = reinterpret_cast<R*>(hs + kHqrW);
+    const int* cmd0 = cluster.map_shared_rank(s_cmd, 0);
+    const C* hs0 = cluster.map_shared_rank(hs, 0);
+    const R* hc0 = cluster.map_shared_rank(hc, 0);
+    int ihi = n - 1;                                    // rank 0's state
+    int its = 0;
+    const int itmax = 30 * max(10, n);
+    int total = 0;
+    while (true) {
+        if (rank == 0) {
+            // deflations until a sweep is due, the matrix is done or the iteration limit is hit
+            int op = 0, l = 0;
+            while (true) {
+                if (ihi < 0) {
+                    op = 1;
+                    break;
+                }
+                int lk = 0;
+                for (int k = ihi - (int)threadIdx.x; k > 0; k -= blockDim.x)
+                    if (hqr_deflates<C, true>(H, n, k, ihi)) {
+                        lk = k;
+                        break;
+                    }
+                lk = __reduce_max_sync(0xffffffffu, lk);
+                if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = lk;
+                __syncthreads();
+                l = 0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); w++) l = max(l, s_red[w]);
+                __syncthreads();
+                if (l > 0 && threadIdx.x == 0) H[(long long)l * n + l - 1] = CT<C>::mk(0, 0);
+                if (l >= ihi) {                           // 1x1 block: eigenvalue converged
+                    if (threadIdx.x == 0) eig[ihi] = hld<true>(H + (long long)ihi * n + ihi);
+                    __syncthreads();
+                    ihi = l - 1;
+                    its = 0;
+                    continue;
+                }
+                if (total > itmax) {
+                    if (threadIdx.x == 0) status[b] = 1;
+                    op = 1;
+                    break;
+                }
+                its++;
+                total++;
+                if (threadIdx.x == 0) s_shift = hqr_shift<C, true>(H, n, l, ihi, its);
+                break;
+            }
+            if (threadIdx.x == 0) {
+                s_cmd[0] = op;
+                s_cmd[1] = l;
+                s_cmd[2] = ihi;
+            }
+        }
+        __threadfence();
+        cluster.sync();
+        const int op = cmd0[0], l = cmd0[1], hi = cmd0[2];
+        if (op != 0) {
+            cluster.sync();                              // rank 0's shared memory stays until all have read
+            return;
+        }
+        // implicit single-shift QR sweep over [l, hi], kHqrW rotations at a time (l < hi)
+        for (int k0 = l; k0 < hi; k0 += kHqrW) {
+            const int k1 = min(k0 + kHqrW, hi);
+            if (rank == 0) hqr_chase<C, true>(H, n, l, hi, k0, k1, s_shift, hw, hc, hs);
+            __threadfence();
+            cluster.sync();
+            if (rank != 0) {
+                for (int i = threadIdx.x; i < k1 - k0; i += blockDim.x) {
+                    hc[i] = hc0[i];
+                    hs[i] = hs0[i];
+                }
+                __syncthreads();
+            }
+            hqr_apply<C, true>(H, Z, n, k0, k1, hc, hs, rank * (int)blockDim.x + (int)threadIdx.x,
+                               K * (int)blockDim.x);
+            __threadfence();
+            cluster.sync();
         }
     }
 }
@@ -958,6 +1092,58 @@ static scw_status gehrd_wide(cudaStream_t st, C* A, C* Q, int n, int batch, C* h
     return SCW_OK;
 }
 
+// CTAs per matrix of the QR sweeps: 0 = chosen per call, 1 = one CTA (hqr_kernel), 2..8 = a
+// cluster of that size (scw_set_qr_cluster)
+static std::atomic<int> g_qr_cluster{0};
+
+// The QR sweeps of `batch` matrices, `active` of them not skipped.  Single solves (wide) put each
+// matrix on a cluster of K CTAs: the largest K <= 8 for which all active matrices' clusters are
+// resident at once (cudaOccupancyMaxActiveClusters) and, in FP32, no larger than the stripes of a
+// window fill (2n tasks for K x 1024 threads; FP64 updates are bound by the FP64 rate of each SM
+// and gain from more SMs down to fewer tasks per CTA).  Otherwise one CTA per matrix.
+template <typename C>
+static scw_status hqr_launch(cudaStream_t st, C* A, C* Q, int n, long long nn, C* W, int* status, const int* skip,
+                             int batch, int active, bool wide) {
+    const size_t smem = z::hqr_smem_bytes<C>();
+    const int force = g_qr_cluster.load();
+    if (wide && force != 1 && active > 0) {
+        int dev = 0, sms = 0;
+        SCW_CUDA_TRY(cudaGetDevice(&dev));
+        SCW_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        SCW_CUDA_TRY(cudaFuncSetAttribute(z::hqr_cluster_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        int kmax = force > 1 ? std::min(force, 8) : std::min(8, sms / active);
+        if (force <= 1 && sizeof(C) == sizeof(float2)) kmax = std::min(kmax, (2 * n + 1023) / 1024);
+        for (int k = kmax; k >= 2; k--) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = (unsigned)k;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3((unsigned)(k * batch));
+            cfg.blockDim = dim3(1024);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = st;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int resident = 0;
+            if (cudaOccupancyMaxActiveClusters(&resident, z::hqr_cluster_kernel<C>, &cfg) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            if (resident >= (force > 1 ? 1 : active)) {
+                SCW_CUDA_TRY(cudaLaunchKernelEx(&cfg, z::hqr_cluster_kernel<C>, A, Q, n, nn, W, status, skip));
+                return SCW_OK;
+            }
+        }
+    }
+    SCW_CUDA_TRY(cudaFuncSetAttribute(z::hqr_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    z::hqr_kernel<C><<<batch, 1024, smem, st>>>(A, Q, n, nn, W, status, skip);
+    SCW_CUDA_TRY(cudaGetLastError());
+    return SCW_OK;
+}
+
 template <typename C>
 scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, int* status, const int* skip,
                 bool wide) {
@@ -968,6 +1154,20 @@ scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, in
     C* Q = work;                             // batch * n * n: Schur vectors
     C* hw = work + nn * batch;               // batch * 3n
     SCW_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * batch, st));
+    // single solves outside a stream capture count the matrices the skip mask leaves (and do
+    // nothing when it leaves none)
+    int active = batch;
+    if (wide && skip) {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        SCW_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+        if (cap == cudaStreamCaptureStatusNone) {
+            std::vector<int> sk(batch);
+            SCW_CUDA_TRY(cudaMemcpyAsync(sk.data(), skip, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
+            SCW_CUDA_TRY(cudaStreamSynchronize(st));
+            active = (int)std::count(sk.begin(), sk.end(), 0);
+            if (active == 0) return SCW_OK;
+        }
+    }
     if (wide && n >= kWideMinN) {
         scw_status s = gehrd_wide<C>(st, A, Q, n, batch, hw, skip);
         if (s != SCW_OK) return s;
@@ -975,10 +1175,10 @@ scw_status geev(cudaStream_t st, C* A, C* W, C* V, int n, int batch, C* work, in
         z::hessenberg_kernel<C><<<batch, 1024, 0, st>>>(A, Q, n, nn, hw, skip);
         SCW_CUDA_TRY(cudaGetLastError());
     }
-    SCW_CUDA_TRY(cudaFuncSetAttribute(z::hqr_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)z::hqr_smem_bytes<C>()));
-    z::hqr_kernel<C><<<batch, 1024, z::hqr_smem_bytes<C>(), st>>>(A, Q, n, nn, W, status, skip);
-    SCW_CUDA_TRY(cudaGetLastError());
+    {
+        scw_status s = hqr_launch<C>(st, A, Q, n, nn, W, status, skip, batch, active, wide);
+        if (s != SCW_OK) return s;
+    }
     // X (triangular eigenvectors) into V, then A := Q X, copied to V
     dim3 gt((n * 32 + 255) / 256, batch);
     z::trevc_kernel<C><<<gt, 256, 0, st>>>(A, V, n, nn, skip);
@@ -1113,6 +1313,12 @@ scw_status scw_cgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, i
         if (status[b]) bad = 1;
     }
     return bad ? fail(SCW_ERR_NUMERIC, "scw_cgeev: QR iteration did not converge") : SCW_OK;
+}
+
+scw_status scw_set_qr_cluster(int ctas) {
+    if (ctas < 0 || ctas > 8) return fail(SCW_ERR_ARG, "scw_set_qr_cluster: 0 (per call), 1 or 2..8 CTAs");
+    scw::g_qr_cluster.store(ctas);
+    return SCW_OK;
 }
 
 }  // extern "C"

@@ -112,24 +112,37 @@ __device__ __forceinline__ void zlartg(C f, C g, typename CT<C>::R& c, C& s, C& 
     r = CT<C>::mk(fs.x * d, fs.y * d);
 }
 
+// load of a matrix element: plain, or (kCg) through L2 only (ld.global.cg), for data that other
+// CTAs of a thread-block cluster write between barriers
+template <bool kCg>
+__device__ __forceinline__ double2 hld(const double2* p) {
+    if constexpr (kCg) return __ldcg(p);
+    else return *p;
+}
+template <bool kCg>
+__device__ __forceinline__ float2 hld(const float2* p) {
+    if constexpr (kCg) return __ldcg(p);
+    else return *p;
+}
+
 // deflation test for the subdiagonal entry h(k, k-1) of the active block ending at ihi
-template <typename C>
+template <typename C, bool kCg = false>
 __device__ __forceinline__ bool hqr_deflates(const C* H, int n, int k, int ihi) {
     using R = typename CT<C>::R;
     const R ulp = CT<C>::ulp;
     const R smlnum = CT<C>::safmin * ((R)n / ulp);
-    const C hkk1 = H[(long long)k * n + k - 1];
+    const C hkk1 = hld<kCg>(H + (long long)k * n + k - 1);
     if (cabs1(hkk1) <= smlnum) return true;
-    R tst = cabs1(H[(long long)(k - 1) * n + k - 1]) + cabs1(H[(long long)k * n + k]);
+    R tst = cabs1(hld<kCg>(H + (long long)(k - 1) * n + k - 1)) + cabs1(hld<kCg>(H + (long long)k * n + k));
     if (tst == 0) {
-        if (k - 2 >= 0) tst += r_abs(H[(long long)(k - 1) * n + k - 2].x);
-        if (k + 1 <= ihi) tst += r_abs(H[(long long)(k + 1) * n + k].x);
+        if (k - 2 >= 0) tst += r_abs(hld<kCg>(H + (long long)(k - 1) * n + k - 2).x);
+        if (k + 1 <= ihi) tst += r_abs(hld<kCg>(H + (long long)(k + 1) * n + k).x);
     }
     if (r_abs(hkk1.x) > ulp * tst) return false;
     // Ahues & Tisseur conservative deflation criterion (as in zlahqr)
-    const C hk1k = H[(long long)(k - 1) * n + k];
-    const C hkk = H[(long long)k * n + k];
-    const C hk1k1 = H[(long long)(k - 1) * n + k - 1];
+    const C hk1k = hld<kCg>(H + (long long)(k - 1) * n + k);
+    const C hkk = hld<kCg>(H + (long long)k * n + k);
+    const C hk1k1 = hld<kCg>(H + (long long)(k - 1) * n + k - 1);
     const R ab = r_max(cabs1(hkk1), cabs1(hk1k));
     const R ba = r_min(cabs1(hkk1), cabs1(hk1k));
     const C dd = csub(hk1k1, hkk);

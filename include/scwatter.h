@@ -276,7 +276,7 @@ SCW_API scw_status scw_cgeev(scw_ctx ctx, int n, void* A, void* W, void* V, int 
 /* CTAs per matrix of the QR sweeps in scw_zgeev, scw_cgeev, scw_zgeev_mixed and scw_solve, for the
  * whole process: 0 (default) chooses per call (a thread-block cluster of up to 8 CTAs per matrix
  * where all matrices' clusters fit on the GPU at once, else one CTA), 1 one CTA per matrix, 2..8
- * a cluster of that size where it fits.  Results are the same bit for bit in every setting.
+ * a cluster of that size where it fits.  Results agree to rounding in every setting.
  * Batches (scw_batch_*) always use one CTA per matrix.  No reference counterpart. */
 SCW_API scw_status scw_set_qr_cluster(int ctas);
 SCW_API scw_status scw_zgeev_mixed(scw_ctx ctx, int n, void* A, void* W, void* V, int batch, int* accepted_host,

@@ -818,9 +818,11 @@ hqr_kernel(C* __restrict__ H, C* __restrict__ Z, int n, long long sA, C* __restr
 // barrier.  The CTAs follow the decisions rank 0 leaves in its shared memory before a barrier,
 // so all of them pass the same sequence of barriers and leave together.  H and Z are read through
 // L2 only (other CTAs of the cluster write them) and every thread fences its writes before a
-// barrier.  Each element sees the same operations in the same order as in hqr_kernel, so the
-// results are the same bit for bit; the deferred updates, 72-80 % of a sweep on one CTA (and
-// nearly all of it in FP64, whose rate per SM is low), are spread over K SMs.
+// barrier.  Each element sees the same rotations in the same order as in hqr_kernel; the two
+// kernels are compiled apart and may fuse multiply-adds differently, so the results agree to
+// rounding (measured: they differ in the last bits even where the second CTA has no stripe to
+// update).  The deferred updates, 72-80 % of a sweep on one CTA (and nearly all of it in FP64,
+// whose rate per SM is low), are spread over K SMs.
 // ------------------------------------------------------------------------------------
 template <typename C>
 __global__ void __launch_bounds__(1024)

@@ -577,36 +577,41 @@ __device__ __forceinline__ void rot_cols(typename CT<C>::R c, C s, C& x, C& y) {
 // Every element sees the same operations in the same order as rotation-by-rotation.
 constexpr int kHqrW = 64;
 
-// Givens generator of the chase: FP64 as zlartg; FP32 from two reciprocal square roots (c =
-// |f| / d, s = conj(g) f / (|f| d), r = f d / |f| with d = sqrt(|f|^2 + |g|^2)), which keeps
-// the rotation unitary to a few ulp.  (One Newton-Raphson step on each reciprocal square root,
-// unitary to about 1 ulp, was measured on two n = 3200 layers: eigenpair residuals 1.6-2.5x
-// larger and fewer layers accepted by the refinement, so the plain form stays.)
-__device__ __forceinline__ void givens_chase(double2 f, double2 g, double& c, double2& s, double2& r) {
-    zlartg(f, g, c, s, r);
-}
-__device__ __forceinline__ void givens_chase(float2 f, float2 g, float& c, float2& s, float2& r) {
-    const float gf = cabs2(g), ff = cabs2(f);
-    if (gf == 0.0f) {
-        c = 1.0f;
-        s = make_float2(0.0f, 0.0f);
+// Givens generator of the chase, from two reciprocal square roots (c = |f| / d,
+// s = conj(g) f / (|f| d), r = f d / |f| with d = sqrt(|f|^2 + |g|^2)), which keeps the rotation
+// unitary to a few ulp.  In FP64 this replaces zlartg's two square roots and five divisions:
+// the chase is one warp working through each rotation's dependent chain, and GB300 issues FP64
+// at about 2 operations per clock per SM, so that chain sets the FP64 sweep's time.  (In FP32,
+// one Newton-Raphson step on each reciprocal square root, unitary to about 1 ulp, was measured on
+// two n = 3200 layers: eigenpair residuals 1.6-2.5x larger and fewer layers accepted by the
+// refinement, so the plain form stays.)
+__device__ __forceinline__ float r_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double r_rsqrt(double x) { return rsqrt(x); }
+
+template <typename C>
+__device__ __forceinline__ void givens_chase(C f, C g, typename CT<C>::R& c, C& s, C& r) {
+    using R = typename CT<C>::R;
+    const R gf = cabs2(g), ff = cabs2(f);
+    if (gf == R(0)) {
+        c = R(1);
+        s = CT<C>::mk(R(0), R(0));
         r = f;
         return;
     }
-    if (ff == 0.0f) {
-        const float ig = rsqrtf(gf);
-        c = 0.0f;
-        s = make_float2(g.x * ig, -g.y * ig);
-        r = make_float2(gf * ig, 0.0f);
+    if (ff == R(0)) {
+        const R ig = r_rsqrt(gf);
+        c = R(0);
+        s = CT<C>::mk(g.x * ig, -g.y * ig);
+        r = CT<C>::mk(gf * ig, R(0));
         return;
     }
-    const float iaf = rsqrtf(ff), id = rsqrtf(ff + gf);
+    const R iaf = r_rsqrt(ff), id = r_rsqrt(ff + gf);
     c = ff * iaf * id;
-    const float2 fs = make_float2(f.x * iaf, f.y * iaf);
-    const float2 t = cmulc(g, fs);
-    s = make_float2(t.x * id, t.y * id);
-    const float d = (ff + gf) * id;
-    r = make_float2(fs.x * d, fs.y * d);
+    const C fs = CT<C>::mk(f.x * iaf, f.y * iaf);
+    const C t = cmulc(g, fs);
+    s = CT<C>::mk(t.x * id, t.y * id);
+    const R d = (ff + gf) * id;
+    r = CT<C>::mk(fs.x * d, fs.y * d);
 }
 
 // The chase of rotations k0 .. k1-1 inside the shared-memory window (loaded from H, a block
